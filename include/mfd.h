@@ -1,0 +1,137 @@
+/* mfd.h -- C ABI of the GB300 FDTD stepping engine (drop-in for Meep's
+ * fields::step() path).
+ *
+ * All entry points return 0 on success and a negative status on failure;
+ * mfd_last_error() then holds a message ("meep: ..." style, like the
+ * reference's meep::abort, src/mympi.cpp:238-254).  Handles are opaque and
+ * not thread-safe (the reference API is not thread-safe either,
+ * src/meep.hpp:1621-1622); each handle owns one CUDA stream.
+ *
+ * Conventions
+ *   component  c = 3*type + direction, type E=0 H=1 D=2 B=3, direction X=0 Y=1 Z=2
+ *              (the reference's enum component orders Ex..Bz with cylindrical
+ *              slots in between, src/meep/vec.hpp:31-56; the C++ drop-in maps it)
+ *   grid       dim 1 uses Z only, dim 2 uses X and Y, dim 3 uses X, Y, Z
+ *              (reference: src/meep/vec.hpp ndim / LOOP_OVER_DIRECTIONS).
+ *              Every component array has n[d]+1 points along each present
+ *              direction; point k of component c sits at half-pixel coordinate
+ *              io[d] + shift_c[d] + 2k (shift = Yee offset, src/meep/vec.hpp:1132-1140).
+ *   arrays     exchanged through this ABI are dense, x slowest, the last present
+ *              direction fastest, (n[d]+1) per present direction, float64.
+ *   precision  64: fields and coefficients in double; 32: float storage and
+ *              arithmetic for fields/coefficients, DFT sums kept in double.
+ */
+#ifndef MFD_ABI_H_
+#define MFD_ABI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mfd_sim mfd_sim;
+
+enum { MFD_E = 0, MFD_H = 1, MFD_D = 2, MFD_B = 3 };
+enum { MFD_X = 0, MFD_Y = 1, MFD_Z = 2 };
+enum { MFD_NCOMP = 12 };
+
+/* Grid and boundary description.
+ * Replaces: structure(grid_volume, material_function&, boundary_region, ...)
+ *           src/meep.hpp:830-839, with pml() src/meep.hpp:732-737 and the
+ *           quadratic profile of src/structure.cpp:252-255. */
+typedef struct mfd_grid {
+  int dim;                    /* 1, 2 or 3 */
+  int n[3];                   /* cells per direction (X, Y, Z); 0 for absent */
+  int io[3];                  /* half-pixel coordinate of the low corner */
+  double a;                   /* resolution (pixels per unit length) */
+  double courant;             /* dt = courant / a */
+  double pml_thickness[3][2]; /* [direction][0=low,1=high]; 0 = no PML */
+  double pml_R[3][2];         /* asymptotic reflection (reference default 1e-15) */
+  double pml_stretch[3][2];   /* mean stretch (reference default 1.0) */
+  int precision;              /* 64 or 32 */
+  int components;             /* bit mask of allocated components (bit c) */
+} mfd_grid;
+
+/* Create / destroy.  Replaces fields::fields(structure*, ...) src/meep.hpp:1740-1742.
+ * Fields start at zero at t = 0, real fields (fields::use_real_fields). */
+int mfd_create(const mfd_grid *grid, mfd_sim **out);
+void mfd_destroy(mfd_sim *sim);
+const char *mfd_last_error(void);
+
+/* Inverse permittivity row entry chi1inv[c][d] for E component c (dense
+ * component-grid array).  Replaces structure_chunk::set_chi1inv
+ * src/anisotropic_averaging.cpp:211.  Off-diagonal entries (d != dir(c)) use
+ * the reference's 4-point averaging (src/step_generic.cpp:580-581). */
+int mfd_set_chi1inv(mfd_sim *sim, int c, int d, const double *values);
+
+/* Conductivity of D or B component c (dense array); condinv = 1/(1+sigma dt/2).
+ * Replaces structure_chunk::set_conductivity src/structure.cpp:868-905 and
+ * update_condinv src/structure.cpp:693-707. */
+int mfd_set_conductivity(mfd_sim *sim, int c, const double *values);
+
+/* Lorentzian / Drude pole on E (field_type E).  sigma[d] is the dense sigma
+ * array of E component d (NULL if the component is absent).  Poles are applied
+ * in the reference's list order (last added first).  Replaces
+ * structure::add_susceptibility src/structure.cpp:477-507 with
+ * lorentzian_susceptibility src/susceptibility.cpp:188-281. */
+int mfd_add_lorentzian(mfd_sim *sim, int field_type, double omega0, double gamma, int drude,
+                       const double *const sigma[3]);
+
+/* Source time functions.  Replaces gaussian_src_time src/sources.cpp:72-110
+ * (both constructors) and continuous_src_time.  With explicit_window == 0 the
+ * Gaussian is gaussian_src_time(freq, fwidth, s) with s = start (0 means the
+ * default 5); otherwise gaussian_src_time(freq, width, start, end).
+ * Returns id >= 0 in *id. */
+int mfd_add_gaussian_src(mfd_sim *sim, double freq, double fwidth_or_width, double start,
+                         double end, int explicit_window, int is_integrated, int *id);
+int mfd_add_continuous_src(mfd_sim *sim, double freq_re, double freq_im, double width,
+                           double start, double end, double slowness, int is_integrated,
+                           int *id);
+
+/* Point list of a source on component c (an E or H component: the current is
+ * applied to the D or B field of that direction).  idx are dense-array linear
+ * indices, amp interleaved (re, im).  Replaces fields::add_volume_source /
+ * src_vol src/sources.cpp:223-312, src/meep_internals.hpp:49-82. */
+int mfd_add_source_points(mfd_sim *sim, int c, int src_id, size_t npts, const int64_t *idx,
+                          const double *amp);
+
+/* DFT monitor on component c over the box lo[d]..hi[d] (point indices of the
+ * component grid, inclusive).  w[d] holds hi[d]-lo[d]+1 per-point weights for
+ * each present direction (the reference's IVEC_LOOP_WEIGHT factors), dV the
+ * volume element, scale the complex stored weight.  centered != 0 averages the
+ * Yee values onto the centred grid (yee2cent_offsets).  Replaces
+ * fields::add_dft src/dft.cpp:175-235 / dft_chunk src/dft.cpp:266-308.
+ * Returns monitor id in *id. */
+int mfd_add_dft(mfd_sim *sim, int c, const int lo[3], const int hi[3], const double *const w[3],
+                double dV, int include_weights, double scale_re, double scale_im, int centered,
+                size_t nfreq, const double *freq, int decimation, int *id);
+
+/* Advance n full time steps (fields::step, src/step.cpp:35-139). */
+int mfd_step(mfd_sim *sim, int n);
+
+/* Current step count t (fields::t) and dt. */
+int mfd_get_time(const mfd_sim *sim, int64_t *t, double *dt);
+
+/* Copy the dense array of component c to host doubles. */
+int mfd_get_field(mfd_sim *sim, int c, double *out);
+
+/* Copy monitor `id` sums to host: npts*nfreq*(re,im), point-major. */
+int mfd_get_dft(mfd_sim *sim, int id, double *out, size_t *npts, size_t *nfreq);
+
+/* Flux spectrum sum_k Re(E_k conj(H_k)) over paired monitors (E[i], H[i]),
+ * accumulated in double on the device.  Replaces dft_flux::flux
+ * src/dft.cpp:542-556. out has nfreq entries. */
+int mfd_flux(mfd_sim *sim, int npairs, const int *idE, const int *idH, double *out);
+
+/* Number of kernel launches issued by this handle so far (for accounting). */
+int64_t mfd_kernel_launches(const mfd_sim *sim);
+
+/* Device-side timing of the last mfd_step call, milliseconds (CUDA events). */
+double mfd_last_step_ms(const mfd_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1105 @@
+// Implementation of the drop-in meep:: API (include/meep_gb300/meep.hpp) over
+// the C ABI in mfd.h.
+//
+// Host-side setup follows the reference's semantics so that the engine sees the
+// same inputs the reference's chunks would hold:
+//   material arrays   structure_chunk::set_chi1inv   src/anisotropic_averaging.cpp:211-324
+//                     structure_chunk::set_conductivity src/structure.cpp:868-905
+//                     structure_chunk::add_susceptibility src/anisotropic_averaging.cpp:330-417
+//   component set     fields::_require_component     src/fields.cpp:552-572
+//   source points     fields::add_volume_source      src/sources.cpp:223-312, 463-489
+//   monitor points    fields::loop_in_chunks         src/loop_in_chunks.cpp:283-540
+//                     compute_boundary_weights       src/loop_in_chunks.cpp:245-281
+//   DFT setup         fields::add_dft / add_dft_flux src/dft.cpp:175-235, 602-652
+//   interpolation     grid_volume::interpolate       src/vec.cpp:527-612
+// The whole cell is one chunk here, so loop_in_chunks reduces to its
+// single-chunk case (identity symmetry, no periodic images).
+#include <meep.hpp>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <map>
+
+#include "mfd.h"
+
+namespace meep {
+
+int verbosity = 1;
+
+void abort(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  char buf[1024];
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw std::runtime_error(std::string("meep: ") + buf);
+}
+
+void master_printf(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vprintf(fmt, ap);
+  va_end(ap);
+}
+
+const char *component_name(component c) {
+  static const char *names[] = {"ex", "ey", "er", "ep", "ez", "hx", "hy", "hr", "hp", "hz",
+                                "dx", "dy", "dr", "dp", "dz", "bx", "by", "br", "bp", "bz",
+                                "eps", "mu", "none"};
+  return names[c];
+}
+
+static int mfd_comp(component c) {
+  int t = type(c);
+  direction d = component_direction(c);
+  if (d > Z) meep::abort("cylindrical components are not supported");
+  return 3 * t + int(d);
+}
+
+static void chk(int status) {
+  if (status != 0) throw std::runtime_error(mfd_last_error());
+}
+
+/* ---------------------------------------------------------- geometry */
+volume::volume(const vec &vec1, const vec &vec2) : dim(vec1.dim), min_corner(vec1.dim), max_corner(vec1.dim) {
+  LOOP_OVER_DIRECTIONS(dim, d) {
+    min_corner.set_direction(d, std::min(vec1.in_direction(d), vec2.in_direction(d)));
+    max_corner.set_direction(d, std::max(vec1.in_direction(d), vec2.in_direction(d)));
+  }
+}
+
+grid_volume::grid_volume(ndim td, double ta, int na, int nb, int nc) : io(td), origin(td) {
+  dim = td;
+  a = ta;
+  inva = 1.0 / ta;
+  num[0] = na;
+  num[1] = nb;
+  num[2] = nc;
+  set_origin(zero_ivec(dim));
+}
+
+void grid_volume::set_origin(const ivec &o) {
+  io = o;
+  origin = operator[](io);
+}
+
+ivec grid_volume::big_corner() const {
+  ivec r = io;
+  LOOP_OVER_DIRECTIONS(dim, d) r.t[d] += 2 * num_direction(d);
+  return r;
+}
+
+ivec grid_volume::iyee_shift(component c) const {
+  ivec out = zero_ivec(dim);
+  LOOP_OVER_DIRECTIONS(dim, d) {
+    if (c == Dielectric || c == Permeability ||
+        ((is_electric(c) || is_D(c)) && d == component_direction(c)) ||
+        ((is_magnetic(c) || is_B(c)) && d != component_direction(c)))
+      out.set_direction(d, 1);
+  }
+  return out;
+}
+
+ivec grid_volume::icenter() const {
+  ivec r = io;
+  LOOP_OVER_DIRECTIONS(dim, d) {
+    int v = num_direction(d);
+    r.t[d] += v - (v >= 0 ? v : -v) % 2;
+  }
+  return r;
+}
+
+bool grid_volume::owns(const ivec &p) const {
+  LOOP_OVER_DIRECTIONS(dim, d) {
+    int o = p.in_direction(d) - io.in_direction(d);
+    if (!(o > 0 && o <= 2 * num_direction(d))) return false;
+  }
+  return true;
+}
+
+double grid_volume::boundary_location(boundary_side b, direction d) const {
+  int i = io.in_direction(d) + (b == High ? 2 * num_direction(d) : 0);
+  return i * (0.5 * inva);
+}
+
+size_t grid_volume::ntot() const {
+  size_t n = 1;
+  LOOP_OVER_DIRECTIONS(dim, d) n *= (size_t)(num_direction(d) + 1);
+  return n;
+}
+
+grid_volume volone(double zsize, double a) { return grid_volume(D1, a, 0, 0, (int)(zsize * a + 0.5)); }
+grid_volume vol1d(double zsize, double a) { return volone(zsize, a); }
+grid_volume voltwo(double xsize, double ysize, double a) {
+  return grid_volume(D2, a, (xsize == 0) ? 1 : (int)(xsize * a + 0.5),
+                     (ysize == 0) ? 1 : (int)(ysize * a + 0.5), 0);
+}
+grid_volume vol2d(double xsize, double ysize, double a) { return voltwo(xsize, ysize, a); }
+grid_volume vol3d(double xsize, double ysize, double zsize, double a) {
+  return grid_volume(D3, a, (xsize == 0) ? 1 : (int)(xsize * a + 0.5),
+                     (ysize == 0) ? 1 : (int)(ysize * a + 0.5),
+                     (zsize == 0) ? 1 : (int)(zsize * a + 0.5));
+}
+
+symmetry identity() { return symmetry(); }
+
+boundary_region pml(double thickness, direction d, boundary_side side, double Rasymptotic,
+                    double mean_stretch) {
+  return boundary_region(boundary_region::PML, thickness, Rasymptotic, mean_stretch, d, side);
+}
+boundary_region pml(double thickness, direction d, double Rasymptotic, double mean_stretch) {
+  return pml(thickness, d, Low, Rasymptotic, mean_stretch) +
+         pml(thickness, d, High, Rasymptotic, mean_stretch);
+}
+boundary_region pml(double thickness, double Rasymptotic, double mean_stretch) {
+  boundary_region r;
+  for (int id = 0; id < 3; ++id)
+    r = r + pml(thickness, (direction)id, Rasymptotic, mean_stretch);
+  return r;
+}
+
+void material_function::eff_chi1inv_row(component c, double chi1inv_row[3], const volume &v,
+                                        double tol, int maxeval) {
+  (void)tol;
+  (void)maxeval;
+  chi1inv_row[0] = chi1inv_row[1] = chi1inv_row[2] = 0.0;
+  chi1inv_row[component_direction(c) % 3] = 1 / chi1p1(type(c), v.center());
+}
+
+std::vector<double> linspace(double freq_min, double freq_max, size_t Nfreq) {
+  std::vector<double> freq(Nfreq);
+  for (size_t i = 0; i < Nfreq; ++i)
+    freq[i] = freq_min + (Nfreq <= 1 ? 0.0 : (freq_max - freq_min) * i / (Nfreq - 1));
+  return freq;
+}
+
+/* Dense component-grid helpers: point k of component c along direction d sits
+   at ivec io + shift + 2k; dense index with x slowest, last direction fastest. */
+struct Dense {
+  ndim dim;
+  int n[3];     // cells per X,Y,Z (0 absent)
+  int ext[3];   // points per X,Y,Z (1 absent)
+  ivec io;
+  explicit Dense(const grid_volume &gv) : dim(gv.dim), io(gv.little_corner()) {
+    for (int d = 0; d < 3; d++) {
+      n[d] = 0;
+      ext[d] = 1;
+    }
+    LOOP_OVER_DIRECTIONS(gv.dim, d) {
+      n[d] = gv.num_direction(d);
+      ext[d] = n[d] + 1;
+    }
+  }
+  size_t count() const { return (size_t)ext[0] * ext[1] * ext[2]; }
+  int64_t index(const int k[3]) const { return ((int64_t)k[0] * ext[1] + k[1]) * ext[2] + k[2]; }
+  // k of an ivec location for component c (no range check)
+  void kof(const grid_volume &gv, component c, const ivec &p, int k[3]) const {
+    ivec sh = gv.iyee_shift(c);
+    k[0] = k[1] = k[2] = 0;
+    LOOP_OVER_DIRECTIONS(dim, d) k[d] = (p.in_direction(d) - io.in_direction(d) - sh.in_direction(d)) / 2;
+  }
+  ivec iloc(const grid_volume &gv, component c, const int k[3]) const {
+    ivec p = io + gv.iyee_shift(c);
+    LOOP_OVER_DIRECTIONS(dim, d) p.t[d] += 2 * k[d];
+    return p;
+  }
+  template <class F> void for_each(F fn) const {
+    int k[3];
+    for (k[0] = 0; k[0] < ext[0]; k[0]++)
+      for (k[1] = 0; k[1] < ext[1]; k[1]++)
+        for (k[2] = 0; k[2] < ext[2]; k[2]++)
+          fn(k, index(k));
+  }
+};
+
+/* ----------------------------------------------------------- structure */
+struct PoleSpec {
+  double omega0, gamma;
+  bool drude;
+  std::vector<double> sigma[3]; // dense per E component direction (empty = absent)
+};
+
+struct structure::impl {
+  std::vector<double> chi1inv[3][3]; // [E component direction][row entry direction]
+  std::vector<double> cond[2][3];    // [0 = D, 1 = B][direction]
+  std::vector<PoleSpec> poles;       // in add order
+};
+
+static volume dV(const grid_volume &gv, const ivec &here, double diameter = 1.0) {
+  const double hinva = 0.5 * gv.inva * diameter;
+  const vec h = gv[here];
+  volume out(gv.dim);
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    out.set_direction_max(d, h.in_direction(d) + hinva);
+    out.set_direction_min(d, h.in_direction(d) - hinva);
+  }
+  return out;
+}
+
+static vec loop_loc(const grid_volume &gv, const ivec &p) {
+  // IVEC_LOOP_LOC: (0.5*is + i)*inva, which equals (0.5*p)*inva exactly
+  vec r(gv.dim);
+  LOOP_OVER_DIRECTIONS(gv.dim, d) r.set_direction(d, (0.5 * p.in_direction(d)) * gv.inva);
+  return r;
+}
+
+structure::structure(const grid_volume &thegv, material_function &eps, const boundary_region &br_,
+                     const symmetry &s, int num_chunks, double Courant_, bool use_aa, double tol,
+                     int maxeval)
+    : gv(thegv), user_volume(thegv), a(thegv.a), Courant(Courant_), dt(Courant_ / thegv.a), br(br_),
+      d(new impl) {
+  (void)s;
+  (void)num_chunks;
+  if (use_aa) meep::abort("subpixel averaging is not supported by the GB300 engine");
+  set_materials(eps, false, tol, maxeval);
+}
+
+static material_function *new_simple(double f(const vec &)) { return new simple_material_function(f); }
+
+structure::structure(const grid_volume &thegv, double epsf(const vec &), const boundary_region &br_,
+                     const symmetry &s, int num_chunks, double Courant_, bool use_aa, double tol,
+                     int maxeval)
+    : gv(thegv), user_volume(thegv), a(thegv.a), Courant(Courant_), dt(Courant_ / thegv.a), br(br_),
+      d(new impl) {
+  (void)s;
+  (void)num_chunks;
+  if (use_aa) meep::abort("subpixel averaging is not supported by the GB300 engine");
+  std::unique_ptr<material_function> m(new_simple(epsf));
+  set_materials(*m, false, tol, maxeval);
+}
+
+structure::~structure() {}
+
+void structure::set_materials(material_function &mat, bool use_aa, double tol, int maxeval) {
+  set_epsilon(mat, use_aa, tol, maxeval);
+  if (mat.has_mu()) meep::abort("mu != 1 is not supported by the GB300 engine");
+  const component dcs[6] = {Dx, Dy, Dz, Bx, By, Bz};
+  for (component c : dcs)
+    if (gv.has_field(c) && mat.has_conductivity(c)) set_conductivity(c, mat);
+  const component ecs[6] = {Ex, Ey, Ez, Hx, Hy, Hz};
+  for (component c : ecs)
+    if (gv.has_field(c) && (mat.has_chi3(c) || mat.has_chi2(c)))
+      meep::abort("nonlinear susceptibilities are not supported by the GB300 engine");
+}
+
+// set_chi1inv without averaging: row from the pixel at the point, off-diagonal
+// entries from the pixel shifted by -1 along the component direction
+// (src/anisotropic_averaging.cpp:211-324).
+void structure::set_epsilon(material_function &mat, bool use_aa, double tol, int maxeval) {
+  if (use_aa) meep::abort("subpixel averaging is not supported by the GB300 engine");
+  Dense dn(gv);
+  const component ecs[3] = {Ex, Ey, Ez};
+  for (component c : ecs) {
+    if (!gv.has_field(c)) continue;
+    int dc = component_direction(c);
+    std::vector<double> arr[3];
+    bool trivial[3] = {true, true, true};
+    for (int q = 0; q < 3; q++)
+      arr[q].assign(dn.count(), 0.0);
+    ivec shift1(gv.dim, 0);
+    shift1.set_direction(direction(dc), 1);
+    dn.for_each([&](const int k[3], int64_t di) {
+      ivec here = dn.iloc(gv, c, k);
+      double row[3], row_off[3];
+      mat.eff_chi1inv_row(c, row, dV(gv, here), tol, maxeval);
+      mat.eff_chi1inv_row(c, row_off, dV(gv, here - shift1), tol, maxeval);
+      for (int q = 0; q < 3; q++) {
+        double v = (q == dc) ? row[q] : row_off[q];
+        arr[q][di] = v;
+        if (v != (q == dc ? 1.0 : 0.0)) trivial[q] = false;
+      }
+    });
+    for (int q = 0; q < 3; q++) {
+      if (q != dc && trivial[q]) arr[q].clear();
+      d->chi1inv[dc][q] = std::move(arr[q]);
+    }
+    if (trivial[0] && trivial[1] && trivial[2]) d->chi1inv[dc][dc].clear();
+  }
+}
+
+void structure::set_conductivity(component c, material_function &C) {
+  if (!gv.has_field(c)) return;
+  direction cd = component_direction(c);
+  if (cd > Z) meep::abort("cylindrical components are not supported");
+  int which = is_H_or_B(c) ? 1 : 0;
+  component cC = direction_component(which ? Bx : Dx, cd);
+  Dense dn(gv);
+  std::vector<double> arr(dn.count(), 0.0);
+  bool trivial = true;
+  const std::vector<double> *multby = nullptr;
+  if (is_electric(c) && !d->chi1inv[cd][cd].empty()) multby = &d->chi1inv[cd][cd];
+  if (is_magnetic(c)) meep::abort("magnetic conductivity with mu is not supported");
+  dn.for_each([&](const int k[3], int64_t di) {
+    vec here = loop_loc(gv, dn.iloc(gv, cC, k));
+    double v = C.conductivity(c, here);
+    if (multby) v = v * (*multby)[di];
+    arr[di] = v;
+    if (v != 0.0) trivial = false;
+  });
+  d->cond[which][cd] = trivial ? std::vector<double>() : arr;
+}
+
+void structure::set_conductivity(component c, double Cfunc(const vec &)) {
+  simple_material_function m(Cfunc);
+  set_conductivity(c, m);
+}
+
+// add_susceptibility: sigma rows per E component; diagonal from the point,
+// off-diagonal from the point shifted by -1 along the component direction
+// (src/anisotropic_averaging.cpp:330-417).
+void structure::add_susceptibility(material_function &sigma, field_type ft,
+                                   const susceptibility &sus) {
+  if (ft != E_stuff) meep::abort("only electric susceptibilities are supported by the GB300 engine");
+  const lorentzian_susceptibility *lz = dynamic_cast<const lorentzian_susceptibility *>(&sus);
+  if (!lz) meep::abort("only Lorentzian/Drude susceptibilities are supported by the GB300 engine");
+  PoleSpec ps;
+  ps.omega0 = lz->omega_0;
+  ps.gamma = lz->gamma;
+  ps.drude = lz->no_omega_0_denominator;
+  Dense dn(gv);
+  const component ecs[3] = {Ex, Ey, Ez};
+  for (component c : ecs) {
+    if (!gv.has_field(c)) continue;
+    int dc = component_direction(c);
+    ivec unit(gv.dim, 0);
+    unit.set_direction(direction(dc), 1);
+    vec shift1 = gv[unit];
+    std::vector<double> arr(dn.count(), 0.0);
+    bool trivial = true;
+    dn.for_each([&](const int k[3], int64_t di) {
+      vec here = loop_loc(gv, dn.iloc(gv, c, k));
+      double row[3], row_off[3];
+      sigma.sigma_row(c, row, here);
+      sigma.sigma_row(c, row_off, here - shift1);
+      for (int q = 0; q < 3; q++)
+        if (q != dc && row_off[q] != 0.0)
+          meep::abort("anisotropic susceptibilities are not supported by the GB300 engine");
+      arr[di] = row[dc];
+      if (row[dc] != 0.0) trivial = false;
+    });
+    if (!trivial) ps.sigma[dc] = std::move(arr);
+  }
+  d->poles.push_back(std::move(ps));
+}
+
+void structure::add_susceptibility(double sigma(const vec &), field_type ft,
+                                   const susceptibility &sus) {
+  simple_material_function m(sigma);
+  add_susceptibility(m, ft, sus);
+}
+
+/* ------------------------------------------------------------- sources */
+gaussian_src_time::gaussian_src_time(double f, double fw, double s) : explicit_window(false) {
+  freq = f;
+  width = 1.0 / fw;
+  peak_time = width * s;
+  cutoff = width * s;
+  fwidth = std::sqrt(-2.0 * std::log(1e-7)) / (width * pi);
+  while (std::exp(-cutoff * cutoff / (2 * width * width)) < 1e-100)
+    cutoff *= 0.9;
+  cutoff = float(cutoff);
+  p[0] = f;
+  p[1] = fw;
+  p[2] = s;
+}
+
+gaussian_src_time::gaussian_src_time(double f, double w, double st, double et) : explicit_window(true) {
+  freq = f;
+  width = w;
+  peak_time = 0.5 * (st + et);
+  cutoff = (et - st) * 0.5;
+  fwidth = std::sqrt(-2.0 * std::log(1e-7)) / (width * pi);
+  while (std::exp(-cutoff * cutoff / (2 * width * width)) < 1e-100)
+    cutoff *= 0.9;
+  cutoff = float(cutoff);
+  p[0] = f;
+  p[1] = w;
+  p[2] = st;
+  p[3] = et;
+}
+
+continuous_src_time::continuous_src_time(std::complex<double> f, double w, double st, double et,
+                                         double s)
+    : freq(f), width(w), start_time(float(st)), end_time(float(et)), slowness(s) {
+  p[0] = f.real();
+  p[1] = f.imag();
+  p[2] = w;
+  p[3] = st;
+  p[4] = et;
+  p[5] = s;
+}
+
+/* --------------------------------------------------------------- fields */
+struct PendingSource {
+  int c;     // mfd component
+  int src;   // index into srcs
+  std::vector<int64_t> idx;
+  std::vector<std::complex<double>> amp;
+};
+
+struct fields::impl {
+  mfd_sim *sim = nullptr;
+  std::vector<std::unique_ptr<src_time>> srcs;
+  std::vector<PendingSource> pending;
+  int components = 0;
+  std::vector<std::unique_ptr<dft_chunk>> chunks; // owned dft chunks
+  std::vector<dft_flux *> fluxes;
+  bool real_fields = false;
+  // cache of downloaded fields for get_field
+  int64_t cache_t[20];
+  std::vector<double> cache[20];
+  impl() {
+    for (int i = 0; i < 20; i++)
+      cache_t[i] = -1;
+  }
+  ~impl() {
+    if (sim) mfd_destroy(sim);
+  }
+};
+
+fields::fields(structure *s_, double m, double beta, bool zcyl, int tdb, int teh)
+    : t(0), dt(s_->dt), a(s_->a), gv(s_->gv), user_volume(s_->user_volume), s(s_), d(new impl) {
+  (void)zcyl;
+  (void)tdb;
+  (void)teh;
+  if (m != 0 || beta != 0) meep::abort("m != 0 / beta != 0 are not supported by the GB300 engine");
+}
+
+fields::~fields() {}
+
+void fields::use_real_fields() { d->real_fields = true; }
+
+static bool is_like(ndim dim, component c1, component c2) {
+  if (dim != D2) return true;
+  auto tm = [](component c) {
+    return c == Hx || c == Hy || c == Bx || c == By || c == Ez || c == Dz;
+  };
+  return !(tm(c1) ^ tm(c2));
+}
+
+// _require_component (src/fields.cpp:552-572): allocate every like component
+static int require_components(const grid_volume &gv, component c, int mask) {
+  if (!gv.has_field(c)) meep::abort("cannot require a %s component in this grid", component_name(c));
+  for (int ci = 0; ci < 20; ci++) {
+    component ca = component(ci);
+    if (gv.has_field(ca) && is_like(gv.dim, c, ca)) mask |= 1 << mfd_comp(ca);
+  }
+  return mask;
+}
+
+static void ensure_engine(fields &f) {
+  fields::impl &I = *f.d;
+  if (I.sim) return;
+  if (!I.components) meep::abort("allocate field components (by adding sources) before stepping");
+  const grid_volume &gv = f.gv;
+  mfd_grid g;
+  std::memset(&g, 0, sizeof(g));
+  g.dim = gv.dim == D1 ? 1 : gv.dim == D2 ? 2 : 3;
+  if (gv.dim == Dcyl) meep::abort("cylindrical coordinates are not supported");
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+    g.n[dd] = gv.num_direction(dd);
+    g.io[dd] = gv.little_corner().in_direction(dd);
+  }
+  g.a = gv.a;
+  g.courant = f.s->Courant;
+  for (const auto &pt : f.s->br.parts) {
+    if (pt.kind != boundary_region::PML) continue;
+    if (pt.d > Z) continue;
+    bool present = false;
+    LOOP_OVER_DIRECTIONS(gv.dim, dd) present = present || dd == pt.d;
+    if (!present || gv.num_direction(pt.d) <= 1) continue;
+    int side = pt.side == Low ? 0 : 1;
+    g.pml_thickness[pt.d][side] = pt.thickness;
+    g.pml_R[pt.d][side] = pt.Rasymptotic;
+    g.pml_stretch[pt.d][side] = pt.mean_stretch;
+  }
+  g.precision = sizeof(realnum) == 8 ? 64 : 32;
+  g.components = I.components;
+  chk(mfd_create(&g, &I.sim));
+  structure::impl &S = *f.s->d;
+  for (int dc = 0; dc < 3; dc++)
+    for (int q = 0; q < 3; q++)
+      if (!S.chi1inv[dc][q].empty() && ((I.components >> (3 * MFD_E + dc)) & 1))
+        chk(mfd_set_chi1inv(I.sim, 3 * MFD_E + dc, q, S.chi1inv[dc][q].data()));
+  for (int w = 0; w < 2; w++)
+    for (int dc = 0; dc < 3; dc++)
+      if (!S.cond[w][dc].empty()) {
+        int c = 3 * (w ? MFD_B : MFD_D) + dc;
+        if ((I.components >> c) & 1) chk(mfd_set_conductivity(I.sim, c, S.cond[w][dc].data()));
+      }
+  for (const PoleSpec &ps : S.poles) {
+    const double *sg[3] = {nullptr, nullptr, nullptr};
+    for (int q = 0; q < 3; q++)
+      if (!ps.sigma[q].empty() && ((I.components >> (3 * MFD_E + q)) & 1)) sg[q] = ps.sigma[q].data();
+    chk(mfd_add_lorentzian(I.sim, MFD_E, ps.omega0, ps.gamma, ps.drude ? 1 : 0, sg));
+  }
+  std::vector<int> ids;
+  for (const auto &st : I.srcs) {
+    int id = -1;
+    if (st->kind() == 0) {
+      const gaussian_src_time *gs = static_cast<const gaussian_src_time *>(st.get());
+      if (gs->explicit_window)
+        chk(mfd_add_gaussian_src(I.sim, gs->p[0], gs->p[1], gs->p[2], gs->p[3], 1,
+                                 st->is_integrated, &id));
+      else
+        chk(mfd_add_gaussian_src(I.sim, gs->p[0], gs->p[1], gs->p[2], 0, 0, st->is_integrated, &id));
+    }
+    else {
+      chk(mfd_add_continuous_src(I.sim, st->p[0], st->p[1], st->p[2], st->p[3], st->p[4], st->p[5],
+                                 st->is_integrated, &id));
+    }
+    ids.push_back(id);
+  }
+  for (const PendingSource &ps : I.pending) {
+    std::vector<double> amp(2 * ps.amp.size());
+    for (size_t j = 0; j < ps.amp.size(); j++) {
+      amp[2 * j] = ps.amp[j].real();
+      amp[2 * j + 1] = ps.amp[j].imag();
+    }
+    chk(mfd_add_source_points(I.sim, ps.c, ids[ps.src], ps.idx.size(), ps.idx.data(), amp.data()));
+  }
+}
+
+/* ----------------------------------------------------- loop_in_chunks */
+struct LoopBox {
+  bool empty = true;
+  ivec is, ie;                // in cgrid ivec coordinates
+  vec s0, s1, e0, e1;         // per-direction weights (absent directions 1)
+  double dV0 = 1.0;
+};
+
+static ivec vec2diel_floor(const vec &pt, double a, const ivec &equal_shift) {
+  ivec ipt(pt.dim);
+  LOOP_OVER_DIRECTIONS(pt.dim, d) {
+    ipt.set_direction(d, 1 + 2 * int(std::floor(pt.in_direction(d) * a - .5)));
+    if (ipt.in_direction(d) == pt.in_direction(d))
+      ipt.set_direction(d, ipt.in_direction(d) + equal_shift.in_direction(d));
+  }
+  return ipt;
+}
+static ivec vec2diel_ceil(const vec &pt, double a, const ivec &equal_shift) {
+  ivec ipt(pt.dim);
+  LOOP_OVER_DIRECTIONS(pt.dim, d) {
+    ipt.set_direction(d, 1 + 2 * int(std::ceil(pt.in_direction(d) * a - .5)));
+    if (ipt.in_direction(d) == pt.in_direction(d))
+      ipt.set_direction(d, ipt.in_direction(d) + equal_shift.in_direction(d));
+  }
+  return ipt;
+}
+
+static void compute_boundary_weights(const grid_volume &gv, const volume &where, ivec &is, ivec &ie,
+                                     bool snap_empty_dimensions, vec &s0, vec &e0, vec &s1, vec &e1) {
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    double w0, w1;
+    w0 = 1. - where.in_direction_min(d) * gv.a + 0.5 * is.in_direction(d);
+    w1 = 1. + where.in_direction_max(d) * gv.a - 0.5 * ie.in_direction(d);
+    if (ie.in_direction(d) >= is.in_direction(d) + 3 * 2) {
+      s0.set_direction(d, w0 * w0 / 2);
+      s1.set_direction(d, 1 - (1 - w0) * (1 - w0) / 2);
+      e0.set_direction(d, w1 * w1 / 2);
+      e1.set_direction(d, 1 - (1 - w1) * (1 - w1) / 2);
+    }
+    else if (ie.in_direction(d) == is.in_direction(d) + 2 * 2) {
+      s0.set_direction(d, w0 * w0 / 2);
+      s1.set_direction(d, 1 - (1 - w0) * (1 - w0) / 2 - (1 - w1) * (1 - w1) / 2);
+      e0.set_direction(d, w1 * w1 / 2);
+      e1.set_direction(d, s1.in_direction(d));
+    }
+    else if (where.in_direction_min(d) == where.in_direction_max(d)) {
+      if (snap_empty_dimensions) {
+        if (w0 > w1) ie.set_direction(d, is.in_direction(d));
+        else is.set_direction(d, ie.in_direction(d));
+        w0 = w1 = 1.0;
+      }
+      s0.set_direction(d, w0);
+      s1.set_direction(d, w1);
+      e0.set_direction(d, w1);
+      e1.set_direction(d, w0);
+    }
+    else if (ie.in_direction(d) == is.in_direction(d) + 1 * 2) {
+      s0.set_direction(d, w0 * w0 / 2 - (1 - w1) * (1 - w1) / 2);
+      e0.set_direction(d, w1 * w1 / 2 - (1 - w0) * (1 - w0) / 2);
+      s1.set_direction(d, e0.in_direction(d));
+      e1.set_direction(d, s0.in_direction(d));
+    }
+    else
+      meep::abort("bug: impossible(?) looping boundaries");
+  }
+}
+
+static LoopBox loop_global(const grid_volume &gv, const volume &where, component cgrid,
+                           bool snap_empty = false) {
+  LoopBox L;
+  vec yee_c(gv.yee_shift(Centered) - gv.yee_shift(cgrid));
+  ivec iyee_c(gv.iyee_shift(Centered) - gv.iyee_shift(cgrid));
+  volume wherec(where + yee_c);
+  ivec is(vec2diel_floor(wherec.get_min_corner(), gv.a, zero_ivec(gv.dim)) - iyee_c);
+  ivec ie(vec2diel_ceil(wherec.get_max_corner(), gv.a, zero_ivec(gv.dim)) - iyee_c);
+  vec s0(gv.dim), e0(gv.dim), s1(gv.dim), e1(gv.dim);
+  compute_boundary_weights(gv, where, is, ie, snap_empty, s0, e0, s1, e1);
+  ivec iscoS = gv.little_owned_corner(cgrid), iecoS = gv.big_owned_corner(cgrid);
+  ivec iscS(max(is, iscoS));
+  ivec iecS(min(ie, iecoS));
+  if (!(iscS <= iecS)) return L;
+  vec s0c(gv.dim, 1.0), s1c(gv.dim, 1.0), e0c(gv.dim, 1.0), e1c(gv.dim, 1.0);
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    if (iscS.in_direction(d) == is.in_direction(d)) {
+      s0c.set_direction(d, s0.in_direction(d));
+      s1c.set_direction(d, s1.in_direction(d));
+    }
+    else if (iscS.in_direction(d) == is.in_direction(d) + 2) {
+      s0c.set_direction(d, s1.in_direction(d));
+    }
+    if (iecS.in_direction(d) == ie.in_direction(d)) {
+      e0c.set_direction(d, e0.in_direction(d));
+      e1c.set_direction(d, e1.in_direction(d));
+    }
+    else if (iecS.in_direction(d) == ie.in_direction(d) - 2) {
+      e0c.set_direction(d, e1.in_direction(d));
+    }
+    if (iecS.in_direction(d) == iscS.in_direction(d)) {
+      double w = std::min(s0c.in_direction(d), e0c.in_direction(d));
+      s0c.set_direction(d, w);
+      e0c.set_direction(d, w);
+      s1c.set_direction(d, w);
+      e1c.set_direction(d, w);
+    }
+    else if (iecS.in_direction(d) == iscS.in_direction(d) + 1 * 2) {
+      double w = std::min(s0c.in_direction(d), e1c.in_direction(d));
+      s0c.set_direction(d, w);
+      e1c.set_direction(d, w);
+      w = std::min(s1c.in_direction(d), e0c.in_direction(d));
+      s1c.set_direction(d, w);
+      e0c.set_direction(d, w);
+    }
+    else if (iecS.in_direction(d) == iscS.in_direction(d) + 2 * 2) {
+      double w = std::min(s1c.in_direction(d), e1c.in_direction(d));
+      s1c.set_direction(d, w);
+      e1c.set_direction(d, w);
+    }
+  }
+  double dV0 = 1.0;
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    if (where.in_direction(d) > 0.0) dV0 *= gv.inva;
+  }
+  L.empty = false;
+  L.is = iscS;
+  L.ie = iecS;
+  L.s0 = s0c;
+  L.s1 = s1c;
+  L.e0 = e0c;
+  L.e1 = e1c;
+  L.dV0 = dV0;
+  return L;
+}
+
+// IVEC_LOOP_WEIGHT1x (src/meep/vec.hpp:365-372)
+static double w1x(const LoopBox &L, int i, int n, direction d) {
+  if (i > 1 && i < n - 2) return 1.0;
+  if (i == 0) return L.s0.in_direction(d);
+  if (i == 1) return L.s1.in_direction(d);
+  if (i == n - 1) return L.e0.in_direction(d);
+  if (i == n - 2) return L.e1.in_direction(d);
+  return 1.0;
+}
+
+/* ------------------------------------------------------ fields: sources */
+static std::complex<double> one_amp(const vec &) { return 1.0; }
+
+void fields::add_point_source(component c, double freq, double width, double peaktime,
+                              double cutoff, const vec &p, std::complex<double> amp, int is_c) {
+  width /= freq;
+  if (is_c) {
+    continuous_src_time src(freq, width, time(), infinity, cutoff);
+    if (is_magnetic(c)) src.is_integrated = false;
+    add_point_source(c, src, p, amp);
+  }
+  else {
+    cutoff = gv.inva + cutoff * width;
+    if (peaktime <= 0.0) peaktime = time() + cutoff;
+    peaktime += is_magnetic(c) ? -dt * 0.5 : dt;
+    gaussian_src_time src(freq, width, peaktime - cutoff, peaktime + cutoff);
+    if (is_magnetic(c)) src.is_integrated = false;
+    add_point_source(c, src, p, amp);
+  }
+}
+
+void fields::add_point_source(component c, const src_time &src, const vec &p,
+                              std::complex<double> amp) {
+  add_volume_source(c, src, volume(p, p), amp);
+}
+
+void fields::add_volume_source(component c, const src_time &src, const volume &where,
+                               std::complex<double> amp) {
+  add_volume_source(c, src, where, one_amp, amp);
+}
+
+void fields::add_volume_source(component c, const src_time &src, const volume &where_,
+                               std::complex<double> A(const vec &), std::complex<double> amp) {
+  if (d->sim) meep::abort("sources must be added before the first step in the GB300 engine");
+  if (!is_electric(c) && !is_magnetic(c))
+    meep::abort("sources on D/B components are not supported by the GB300 engine");
+  volume where(where_);
+  if (gv.dim != where.dim) meep::abort("incorrect source grid_volume dimensionality in add_volume_source");
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+    double w = user_volume.boundary_location(High, dd) - user_volume.boundary_location(Low, dd);
+    if (where.in_direction(dd) > w + gv.inva)
+      meep::abort("Source width > cell width in %s direction!\n", dd == X ? "x" : dd == Y ? "y" : "z");
+    else if (where.in_direction(dd) > w) {
+      double dw = where.in_direction(dd) - w;
+      where.set_direction_min(dd, where.in_direction_min(dd) - dw * 0.5);
+      where.set_direction_max(dd, where.in_direction_min(dd) + w);
+    }
+  }
+  std::complex<double> damp = amp;
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+    if (where.in_direction(dd) == 0.0) damp *= gv.a; // delta-function units
+  }
+  d->srcs.emplace_back(src.clone());
+  int sidx = (int)d->srcs.size() - 1;
+  vec center = (where.get_min_corner() + where.get_max_corner()) * 0.5;
+  LoopBox L = loop_global(gv, where, c);
+  PendingSource ps;
+  ps.c = mfd_comp(c);
+  ps.src = sidx;
+  if (!L.empty) {
+    Dense dn(gv);
+    int k0[3], k1[3], n[3] = {1, 1, 1};
+    dn.kof(gv, c, L.is, k0);
+    dn.kof(gv, c, L.ie, k1);
+    direction ds[3];
+    int nd = 0;
+    LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+      ds[nd] = dd;
+      n[nd] = k1[dd] - k0[dd] + 1;
+      nd++;
+    }
+    // loop order / weight product of LOOP_OVER_IVECS and IVEC_LOOP_WEIGHT:
+    // loop directions (X,Y,Z) in 3-D, (Z absent, X, Y) in 2-D, (Z) in 1-D
+    int k[3];
+    int i[3];
+    for (i[0] = 0; i[0] < n[0]; i[0]++)
+      for (i[1] = 0; i[1] < (nd > 1 ? n[1] : 1); i[1]++)
+        for (i[2] = 0; i[2] < (nd > 2 ? n[2] : 1); i[2]++) {
+          k[0] = k[1] = k[2] = 0;
+          double wd[3] = {1, 1, 1};
+          for (int q = 0; q < nd; q++) {
+            k[ds[q]] = k0[ds[q]] + i[q];
+            wd[q] = w1x(L, i[q], n[q], ds[q]);
+          }
+          double wgt;
+          if (gv.dim == D3) wgt = wd[2] * (wd[1] * (1.0 * wd[0]));
+          else if (gv.dim == D2) wgt = wd[1] * (wd[0] * (1.0 * 1.0));
+          else wgt = 1.0 * (1.0 * (1.0 * wd[0]));
+          ivec iloc = dn.iloc(gv, c, k);
+          if (!gv.owns(iloc)) continue;
+          vec loc = loop_loc(gv, iloc);
+          vec rel = loc - center;
+          ps.idx.push_back(dn.index(k));
+          ps.amp.push_back(wgt * damp * A(rel));
+        }
+  }
+  d->pending.push_back(std::move(ps));
+  d->components = require_components(gv, c, d->components);
+}
+
+/* ------------------------------------------------------- fields: DFT */
+static int auto_decimation(fields &f, const double *freq, size_t Nfreq) {
+  double src_freq_max = 0;
+  bool any_cw = false;
+  for (const auto &s : f.d->srcs) {
+    if (s->get_fwidth() == 0) any_cw = true;
+    else src_freq_max = std::max(src_freq_max, std::abs(s->frequency().real()) + 0.5 * s->get_fwidth());
+  }
+  if (any_cw) return 1;
+  double freq_max = 0;
+  for (size_t i = 0; i < Nfreq; ++i)
+    freq_max = std::max(freq_max, std::abs(freq[i]));
+  if ((freq_max > 0) && (src_freq_max > 0))
+    return std::max(1, int(std::floor(1 / (f.dt * (freq_max + src_freq_max)))));
+  return 1;
+}
+
+// fields::add_dft for one component; returns the new chunk (or nullptr if the
+// component is not allocated), prepended to `next`.
+static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const double *freq,
+                              size_t Nfreq, bool include_dV_and_interp_weights,
+                              std::complex<double> stored_weight, dft_chunk *next,
+                              bool use_centered_grid, int decimation_factor) {
+  fields::impl &I = *f.d;
+  if (component_direction(c) > Z) return next;
+  if (!I.components) meep::abort("allocate field components (by adding sources) before adding dft objects");
+  int mc = mfd_comp(c);
+  if (!((I.components >> mc) & 1)) return next;
+  ensure_engine(f);
+  if (decimation_factor == 0) decimation_factor = auto_decimation(f, freq, Nfreq);
+  const grid_volume &gv = f.gv;
+  component cgrid = use_centered_grid ? Centered : c;
+  LoopBox L = loop_global(gv, where, cgrid);
+  if (L.empty) return next;
+  Dense dn(gv);
+  // array index box of component c (for the centred grid, point k of c is the
+  // base of the average centred at 2k+1)
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+    int off = use_centered_grid ? 1 : gv.iyee_shift(c).in_direction(dd);
+    lo[dd] = (L.is.in_direction(dd) - gv.little_corner().in_direction(dd) - off) / 2;
+    hi[dd] = (L.ie.in_direction(dd) - gv.little_corner().in_direction(dd) - off) / 2;
+  }
+  std::vector<double> w[3];
+  const double *wp[3] = {nullptr, nullptr, nullptr};
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+    int n = hi[dd] - lo[dd] + 1;
+    w[dd].resize(n);
+    for (int i = 0; i < n; i++)
+      w[dd][i] = w1x(L, i, n, dd);
+    wp[dd] = w[dd].data();
+  }
+  std::complex<double> scale = stored_weight * std::complex<double>(1.0, 0.0) *
+                               (f.dt / std::sqrt(2.0 * pi) * decimation_factor);
+  int id = -1;
+  chk(mfd_add_dft(I.sim, mc, lo, hi, wp, L.dV0, include_dV_and_interp_weights ? 1 : 0, scale.real(),
+                  scale.imag(), use_centered_grid ? 1 : 0, Nfreq, freq, decimation_factor, &id));
+  std::unique_ptr<dft_chunk> ch(new dft_chunk);
+  ch->c = c;
+  ch->monitor_id = id;
+  ch->is = L.is;
+  ch->ie = L.ie;
+  ch->omega.resize(Nfreq);
+  for (size_t i = 0; i < Nfreq; i++)
+    ch->omega[i] = 2 * pi * freq[i];
+  size_t npts = 1;
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) npts *= (size_t)(hi[dd] - lo[dd] + 1);
+  ch->N = npts;
+  ch->dft = new std::complex<realnum>[npts * Nfreq]();
+  ch->next_in_dft = next;
+  dft_chunk *raw = ch.get();
+  I.chunks.push_back(std::move(ch));
+  return raw;
+}
+
+dft_flux fields::add_dft_flux(const volume_list *where_, const double *freq, size_t Nfreq,
+                              bool use_symmetry, bool centered_grid, int decimation_factor) {
+  (void)use_symmetry;
+  dft_flux fl;
+  fl.f = this;
+  fl.freq.assign(freq, freq + Nfreq);
+  if (!where_) return fl;
+  dft_chunk *E = nullptr, *H = nullptr;
+  component cE[2] = {Ex, Ey}, cH[2] = {Hy, Hx};
+  for (const volume_list *where = where_; where; where = where->next) {
+    switch (where->c) {
+      case Sx: cE[0] = Ey, cE[1] = Ez, cH[0] = Hz, cH[1] = Hy; break;
+      case Sy: cE[0] = Ez, cE[1] = Ex, cH[0] = Hx, cH[1] = Hz; break;
+      case Sz: cE[0] = Ex, cE[1] = Ey, cH[0] = Hy, cH[1] = Hx; break;
+      default: meep::abort("invalid flux component!");
+    }
+    for (int i = 0; i < 2; ++i) {
+      E = add_dft_one(*this, cE[i], where->v, freq, Nfreq, true, where->weight * double(1 - 2 * i), E,
+                      centered_grid, decimation_factor);
+      H = add_dft_one(*this, cH[i], where->v, freq, Nfreq, false, 1.0, H, centered_grid,
+                      decimation_factor);
+    }
+  }
+  fl.E = E;
+  fl.H = H;
+  fl.cE = cE[0];
+  fl.cH = cH[0];
+  return fl;
+}
+
+dft_flux fields::add_dft_flux(direction dd, const volume &where, double freq_min, double freq_max,
+                              int Nfreq, bool use_symmetry, bool centered_grid, int decimation_factor) {
+  return add_dft_flux(dd, where, linspace(freq_min, freq_max, Nfreq), use_symmetry, centered_grid,
+                      decimation_factor);
+}
+
+dft_flux fields::add_dft_flux(direction dd, const volume &where, const std::vector<double> &freq,
+                              bool use_symmetry, bool centered_grid, int decimation_factor) {
+  volume_list vl(where, direction_component(Sx, dd));
+  return add_dft_flux(&vl, freq.data(), freq.size(), use_symmetry, centered_grid, decimation_factor);
+}
+
+dft_flux fields::add_dft_flux_plane(const volume &where, double freq_min, double freq_max,
+                                    int Nfreq) {
+  direction dd = NO_DIRECTION;
+  LOOP_OVER_DIRECTIONS(gv.dim, q) {
+    if (where.in_direction(q) == 0) dd = q;
+  }
+  if (dd == NO_DIRECTION) meep::abort("add_dft_flux_plane needs a plane");
+  return add_dft_flux(dd, where, freq_min, freq_max, Nfreq);
+}
+
+dft_fields fields::add_dft_fields(component *components, int num_components, const volume where,
+                                  const double *freq, size_t Nfreq, bool use_centered_grid,
+                                  int decimation_factor, bool persist) {
+  if (persist) meep::abort("persistent DFT fields are not supported by the GB300 engine");
+  dft_chunk *chunks = nullptr;
+  for (int nc = 0; nc < num_components; nc++)
+    chunks = add_dft_one(*this, components[nc], where, freq, Nfreq, false, 1.0, chunks,
+                         use_centered_grid, decimation_factor);
+  return dft_fields(chunks, std::vector<double>(freq, freq + Nfreq), where);
+}
+
+dft_fields fields::add_dft_fields(component *components, int num_components, const volume where,
+                                  double freq_min, double freq_max, int Nfreq,
+                                  bool use_centered_grid, int decimation_factor, bool persist) {
+  std::vector<double> fr = linspace(freq_min, freq_max, Nfreq);
+  return add_dft_fields(components, num_components, where, fr.data(), fr.size(),
+                        use_centered_grid, decimation_factor, persist);
+}
+
+double *dft_flux::flux() {
+  size_t nf = freq.size();
+  double *F = new double[nf];
+  for (size_t i = 0; i < nf; i++)
+    F[i] = 0;
+  std::vector<int> idE, idH;
+  for (dft_chunk *e = E, *h = H; e && h; e = e->next_in_dft, h = h->next_in_dft) {
+    idE.push_back(e->monitor_id);
+    idH.push_back(h->monitor_id);
+  }
+  if (!idE.empty()) chk(mfd_flux(f->d->sim, (int)idE.size(), idE.data(), idH.data(), F));
+  return F;
+}
+
+void fields::sync_dfts() {
+  if (!d->sim) return;
+  for (auto &ch : d->chunks) {
+    size_t np = 0, nf = 0;
+    chk(mfd_get_dft(d->sim, ch->monitor_id, nullptr, &np, &nf));
+    std::vector<double> buf(2 * np * nf);
+    chk(mfd_get_dft(d->sim, ch->monitor_id, buf.data(), &np, &nf));
+    for (size_t i = 0; i < np * nf; i++)
+      ch->dft[i] = std::complex<realnum>(realnum(buf[2 * i]), realnum(buf[2 * i + 1]));
+  }
+}
+
+void sync_dfts(fields &f) { f.sync_dfts(); }
+
+/* ------------------------------------------------------- fields: step */
+void fields::step() {
+  ensure_engine(*this);
+  chk(mfd_step(d->sim, 1));
+  t += 1;
+}
+
+double fields::last_step_ms() const { return d->sim ? mfd_last_step_ms(d->sim) : 0.0; }
+long long fields::kernel_launches() const { return d->sim ? mfd_kernel_launches(d->sim) : 0; }
+
+std::vector<double> fields::get_field_array(component c) {
+  ensure_engine(*this);
+  Dense dn(gv);
+  std::vector<double> out(dn.count(), 0.0);
+  int mc = mfd_comp(c);
+  chk(mfd_get_field(d->sim, mc, out.data()));
+  return out;
+}
+
+std::complex<double> fields::get_field(component c, const ivec &iloc, bool parallel) {
+  (void)parallel;
+  if (c >= Dielectric) meep::abort("get_field of a non-field component is not supported");
+  if (!gv.owns(iloc)) return 0.0;
+  int mc = mfd_comp(c);
+  if (!((d->components >> mc) & 1)) return 0.0;
+  ensure_engine(*this);
+  if (d->cache_t[mc] != t) {
+    d->cache[mc] = get_field_array(c);
+    d->cache_t[mc] = t;
+  }
+  Dense dn(gv);
+  int k[3];
+  dn.kof(gv, c, iloc, k);
+  // points not on this component's grid are not owned by it
+  ivec back = dn.iloc(gv, c, k);
+  if (back != iloc) return 0.0;
+  return d->cache[mc][dn.index(k)];
+}
+
+static int my_round(double x) { return int(std::floor(std::fabs(x) + 0.5) * (x < 0 ? -1 : 1)); }
+
+static void stupidsort(ivec *locs, double *w, int l) {
+  while (l) {
+    if (std::fabs(w[0]) < 2e-15) {
+      w[0] = w[l - 1];
+      locs[0] = locs[l - 1];
+      w[l - 1] = 0.0;
+      locs[l - 1] = ivec(locs[0].dim, 0);
+    }
+    else {
+      w += 1;
+      locs += 1;
+    }
+    l -= 1;
+  }
+}
+
+// grid_volume::interpolate(component, vec, ivec[8], double[8]) (src/vec.cpp:555-612)
+static void interpolate(const grid_volume &gv, component c, const vec &pc, ivec locs[8],
+                        double weights[8]) {
+  const double SMALL = 1e-13;
+  const vec p = (pc - gv.yee_shift(c)) * gv.a;
+  ivec middle(gv.dim);
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) middle.set_direction(dd, ((int)std::floor(p.in_direction(dd))) * 2 + 1);
+  middle += gv.iyee_shift(c);
+  const vec midv = gv[middle];
+  const vec dv = (pc - midv) * (2 * gv.a);
+  int already_have = 1;
+  ivec rv(gv.dim);
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) rv.set_direction(dd, my_round(midv.in_direction(dd) * 2 * gv.a));
+  for (int i = 0; i < 8; i++) {
+    locs[i] = rv;
+    weights[i] = 1.0;
+  }
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+    for (int i = 0; i < already_have; i++) {
+      locs[already_have + i] = locs[i];
+      weights[already_have + i] = weights[i];
+      locs[i].set_direction(dd, middle.in_direction(dd) - 1);
+      weights[i] *= 0.5 * (1.0 - dv.in_direction(dd));
+      locs[already_have + i].set_direction(dd, middle.in_direction(dd) + 1);
+      weights[already_have + i] *= 0.5 * (1.0 + dv.in_direction(dd));
+    }
+    already_have *= 2;
+  }
+  for (int i = already_have; i < 8; i++)
+    weights[i] = 0.0;
+  double total_weight = 0.0;
+  for (int i = 0; i < already_have; i++)
+    total_weight += weights[i];
+  for (int i = 0; i < already_have; i++)
+    weights[i] += (1.0 - total_weight) * (1.0 / already_have);
+  for (int i = 0; i < already_have; i++) {
+    if (weights[i] < 0.0) {
+      if (-weights[i] >= SMALL * 1e5) meep::abort("large negative interpolation weight");
+      weights[i] = 0.0;
+    }
+    else if (weights[i] < SMALL)
+      weights[i] = 0.0;
+  }
+  stupidsort(locs, weights, already_have);
+  bool all_same = true;
+  for (int i = 0; i < 8 && weights[i]; i++)
+    if (weights[i] != weights[0]) all_same = false;
+  if (all_same) {
+    int num_weights = 0;
+    for (int i = 0; i < 8 && weights[i]; i++)
+      num_weights++;
+    for (int i = 0; i < 8 && weights[i]; i++)
+      weights[i] = 1.0 / num_weights;
+  }
+}
+
+std::complex<double> fields::get_field(component c, const vec &loc, bool parallel) {
+  (void)parallel;
+  ivec ilocs[8];
+  double w[8];
+  std::complex<double> res = 0.0;
+  interpolate(gv, c, loc, ilocs, w);
+  for (int argh = 0; argh < 8 && w[argh]; argh++)
+    res += w[argh] * get_field(c, ilocs[argh], false);
+  return res;
+}
+
+} // namespace meep

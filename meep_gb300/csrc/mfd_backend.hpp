@@ -1,0 +1,44 @@
+// Interface between the C ABI (mfd_capi.cpp) and an execution backend.  The
+// product links the CUDA backend (mfd_cuda_*.cu); the CPU oracle used by the
+// tests implements the same interface in oracle/cpu_backend.cpp.
+#pragma once
+
+#include <complex>
+#include <vector>
+
+#include "mfd_plan.hpp"
+
+namespace mfd {
+
+// Source amplitudes of one source time function for one full step, taken at
+// the times fields::step() calls calc_sources (src/step.cpp:64-108).
+struct SrcStepValues {
+  std::complex<double> cur_b; // current at t*dt            (step_source(B))
+  std::complex<double> cur_d; // current at (t+1/2)*dt      (step_source(D))
+  std::complex<double> dip_e; // dipole  at (t+1)*dt        (integrated E sources)
+};
+
+class Backend {
+public:
+  virtual ~Backend() {}
+  // Allocate fields and upload materials, PML tables and sources.
+  virtual void setup(Plan &p) = 0;
+  // Upload monitor p.monitors[id] (may be called after setup).
+  virtual void add_monitor(Plan &p, int id) = 0;
+  // One full step from step count t to t+1, then the DFT updates at t+1.
+  virtual void step(Plan &p, int64_t t, const std::vector<SrcStepValues> &vals) = 0;
+  virtual void get_field(Plan &p, int c, double *out_dense) = 0;
+  virtual void get_dft(Plan &p, int id, double *out) = 0;
+  virtual void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) = 0;
+  virtual void synchronize() {}
+  virtual long long launches() const { return 0; }
+  virtual double last_step_ms() const { return 0.0; }
+  // called before a batch of steps / after it (for timing)
+  virtual void begin_steps() {}
+  virtual void end_steps() {}
+};
+
+// Defined by whichever backend is linked in.
+Backend *make_backend(const Plan &p);
+
+} // namespace mfd

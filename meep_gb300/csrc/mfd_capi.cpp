@@ -1,0 +1,301 @@
+// C ABI of the stepping engine (declared in include/mfd.h).  Owns the Plan
+// and the backend; every entry point converts exceptions to a status code and
+// a last-error string, the way the reference's SWIG layer maps meep::abort to
+// a Python exception (python/meep.i:1365-1380).
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "mfd.h"
+#include "mfd_backend.hpp"
+
+using namespace mfd;
+
+struct mfd_sim {
+  std::unique_ptr<Plan> plan;
+  std::unique_ptr<Backend> be;
+  bool setup_done = false;
+  int64_t t = 0;
+};
+
+static thread_local std::string g_last_error;
+
+#define MFD_TRY try {
+#define MFD_CATCH                                                                                  \
+  }                                                                                                \
+  catch (const std::exception &e) {                                                                \
+    g_last_error = e.what();                                                                       \
+    return -1;                                                                                     \
+  }                                                                                                \
+  catch (...) {                                                                                    \
+    g_last_error = "meep: unknown error";                                                          \
+    return -1;                                                                                     \
+  }                                                                                                \
+  return 0;
+
+static void need(bool ok, const char *msg) {
+  if (!ok) throw Error(msg);
+}
+
+static void check_comp(mfd_sim *s, int c) {
+  need(s && s->plan, "null simulation handle");
+  need(c >= 0 && c < NC, "component out of range");
+}
+
+extern "C" {
+
+const char *mfd_last_error(void) { return g_last_error.c_str(); }
+
+int mfd_create(const mfd_grid *grid, mfd_sim **out) {
+  MFD_TRY
+  need(grid && out, "null argument to mfd_create");
+  *out = nullptr;
+  auto s = std::unique_ptr<mfd_sim>(new mfd_sim);
+  s->plan.reset(new Plan(*grid));
+  s->be.reset(make_backend(*s->plan));
+  *out = s.release();
+  MFD_CATCH
+}
+
+void mfd_destroy(mfd_sim *sim) { delete sim; }
+
+int mfd_set_chi1inv(mfd_sim *s, int c, int d, const double *values) {
+  MFD_TRY
+  check_comp(s, c);
+  need(d >= 0 && d < 3, "direction out of range");
+  need(ctype(c) == MFD_E || ctype(c) == MFD_H, "chi1inv is defined for E and H components");
+  need(!s->setup_done, "materials must be set before the first step");
+  need(values != nullptr, "null array");
+  s->plan->chi1inv[c][d].assign(values, values + s->plan->ndense);
+  MFD_CATCH
+}
+
+int mfd_set_conductivity(mfd_sim *s, int c, const double *values) {
+  MFD_TRY
+  check_comp(s, c);
+  need(ctype(c) == MFD_D || ctype(c) == MFD_B, "conductivity is stored on D or B components");
+  need(!s->setup_done, "materials must be set before the first step");
+  need(values != nullptr, "null array");
+  Plan &p = *s->plan;
+  p.cond[c].assign(values, values + p.ndense);
+  bool any = false;
+  for (double v : p.cond[c])
+    any = any || v != 0.0;
+  if (!any) p.cond[c].clear(); // trivial: dropped, as the reference does
+  p.compute_cond_chunks(c);
+  MFD_CATCH
+}
+
+int mfd_add_lorentzian(mfd_sim *s, int ft, double omega0, double gamma, int drude,
+                       const double *const sigma[3]) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  need(ft == MFD_E, "only electric susceptibilities are supported");
+  need(!s->setup_done, "susceptibilities must be added before the first step");
+  need((int)s->plan->poles.size() < MAX_POLES, "too many susceptibility poles");
+  Pole pole;
+  pole.ft = ft;
+  pole.omega0 = omega0;
+  pole.gamma = gamma;
+  pole.drude = drude != 0;
+  for (int d = 0; d < 3; d++)
+    if (sigma && sigma[d]) {
+      pole.sigma[d].assign(sigma[d], sigma[d] + s->plan->ndense);
+      bool any = false;
+      for (double v : pole.sigma[d])
+        any = any || v != 0.0;
+      if (!any) pole.sigma[d].clear();
+    }
+  // the reference prepends each new susceptibility (src/anisotropic_averaging.cpp:414-416)
+  s->plan->poles.insert(s->plan->poles.begin(), pole);
+  MFD_CATCH
+}
+
+int mfd_add_gaussian_src(mfd_sim *s, double freq, double fwidth_or_width, double start,
+                         double end, int explicit_window, int is_integrated, int *id) {
+  MFD_TRY
+  need(s && s->plan && id, "null argument");
+  SrcTime st = explicit_window ? SrcTime::gaussian_window(freq, fwidth_or_width, start, end)
+                               : SrcTime::gaussian(freq, fwidth_or_width, start > 0 ? start : 5.0);
+  st.integrated = is_integrated != 0;
+  s->plan->srcs.push_back(st);
+  *id = (int)s->plan->srcs.size() - 1;
+  MFD_CATCH
+}
+
+int mfd_add_continuous_src(mfd_sim *s, double fre, double fim, double width, double start,
+                           double end, double slowness, int is_integrated, int *id) {
+  MFD_TRY
+  need(s && s->plan && id, "null argument");
+  SrcTime st = SrcTime::continuous({fre, fim}, width, start, end, slowness);
+  st.integrated = is_integrated != 0;
+  s->plan->srcs.push_back(st);
+  *id = (int)s->plan->srcs.size() - 1;
+  MFD_CATCH
+}
+
+int mfd_add_source_points(mfd_sim *s, int c, int src_id, size_t npts, const int64_t *idx,
+                          const double *amp) {
+  MFD_TRY
+  check_comp(s, c);
+  Plan &p = *s->plan;
+  need(ctype(c) == MFD_E || ctype(c) == MFD_H, "sources are given on E or H components");
+  need(p.have[c], "source component is not allocated");
+  need(src_id >= 0 && src_id < (int)p.srcs.size(), "unknown source time id");
+  need(!s->setup_done, "sources must be added before the first step");
+  if (ctype(c) == MFD_H && p.srcs[src_id].integrated)
+    throw Error("integrated magnetic sources are not supported; set is_integrated = false");
+  SourceGroup gsrc;
+  gsrc.c = c;
+  gsrc.src = src_id;
+  for (size_t j = 0; j < npts; j++) {
+    need(idx[j] >= 0 && idx[j] < p.ndense, "source index out of range");
+    gsrc.idx.push_back(idx[j]);
+    gsrc.amp.emplace_back(amp[2 * j], amp[2 * j + 1]);
+  }
+  if (!gsrc.idx.empty()) p.sources.push_back(std::move(gsrc));
+  MFD_CATCH
+}
+
+int mfd_add_dft(mfd_sim *s, int c, const int lo[3], const int hi[3], const double *const w[3],
+                double dV, int include_weights, double scale_re, double scale_im, int centered,
+                size_t nfreq, const double *freq, int decimation, int *id) {
+  MFD_TRY
+  check_comp(s, c);
+  Plan &p = *s->plan;
+  need(p.have[c], "DFT component is not allocated");
+  need(nfreq > 0 && freq, "DFT needs at least one frequency");
+  need(decimation >= 1, "decimation factor must be >= 1");
+  need(id != nullptr, "null id");
+  Monitor m;
+  m.c = c;
+  m.npts = 1;
+  for (int d = 0; d < 3; d++) {
+    m.lo[d] = lo[d];
+    m.hi[d] = hi[d];
+    need(lo[d] <= hi[d] && lo[d] >= 0 && hi[d] < p.ext[d], "DFT box out of range");
+    if (centered && p.present[d] && p.shift[c][d] == 0)
+      need(hi[d] + 1 < p.ext[d], "centred DFT box needs a neighbour point");
+    int n = hi[d] - lo[d] + 1;
+    m.npts *= n;
+    if (p.present[d]) {
+      need(w && w[d], "missing DFT weights");
+      m.w[d].assign(w[d], w[d] + n);
+    }
+  }
+  m.dV = dV;
+  m.include_weights = include_weights != 0;
+  m.scale = {scale_re, scale_im};
+  m.centered = centered != 0;
+  m.freq.assign(freq, freq + nfreq);
+  m.decimation = decimation;
+  p.monitors.push_back(m);
+  *id = (int)p.monitors.size() - 1;
+  if (s->setup_done) s->be->add_monitor(p, *id);
+  MFD_CATCH
+}
+
+int mfd_step(mfd_sim *s, int n) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  Plan &p = *s->plan;
+  if (!s->setup_done) {
+    s->be->setup(p);
+    for (int i = 0; i < (int)p.monitors.size(); i++)
+      s->be->add_monitor(p, i);
+    s->setup_done = true;
+  }
+  std::vector<SrcStepValues> vals(p.srcs.size());
+  s->be->begin_steps();
+  for (int it = 0; it < n; it++) {
+    double time = s->t * p.dt;
+    // calc_sources at t, t+dt/2 and t+dt (src/step.cpp:64-108)
+    for (size_t k = 0; k < p.srcs.size(); k++) {
+      SrcTime &st = p.srcs[k];
+      st.update(time, p.dt);
+      vals[k].cur_b = st.cur_current;
+      st.update(time + 0.5 * p.dt, p.dt);
+      vals[k].cur_d = st.cur_current;
+      st.update(time + p.dt, p.dt);
+      vals[k].dip_e = st.cur_dipole;
+    }
+    s->be->step(p, s->t, vals);
+    s->t += 1;
+  }
+  s->be->end_steps();
+  MFD_CATCH
+}
+
+int mfd_get_time(const mfd_sim *s, int64_t *t, double *dt) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  if (t) *t = s->t;
+  if (dt) *dt = s->plan->dt;
+  MFD_CATCH
+}
+
+int mfd_get_field(mfd_sim *s, int c, double *out) {
+  MFD_TRY
+  check_comp(s, c);
+  need(out != nullptr, "null output");
+  Plan &p = *s->plan;
+  if (!p.have[c]) {
+    std::memset(out, 0, sizeof(double) * p.ndense);
+    return 0;
+  }
+  if (!s->setup_done) {
+    s->be->setup(p);
+    for (int i = 0; i < (int)p.monitors.size(); i++)
+      s->be->add_monitor(p, i);
+    s->setup_done = true;
+  }
+  s->be->get_field(p, c, out);
+  MFD_CATCH
+}
+
+int mfd_get_dft(mfd_sim *s, int id, double *out, size_t *npts, size_t *nfreq) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  Plan &p = *s->plan;
+  need(id >= 0 && id < (int)p.monitors.size(), "unknown monitor id");
+  if (npts) *npts = p.monitors[id].npts;
+  if (nfreq) *nfreq = p.monitors[id].freq.size();
+  if (out) {
+    if (!s->setup_done) {
+      size_t n = p.monitors[id].npts * p.monitors[id].freq.size() * 2;
+      std::memset(out, 0, n * sizeof(double));
+    }
+    else
+      s->be->get_dft(p, id, out);
+  }
+  MFD_CATCH
+}
+
+int mfd_flux(mfd_sim *s, int npairs, const int *idE, const int *idH, double *out) {
+  MFD_TRY
+  need(s && s->plan && out, "null argument");
+  Plan &p = *s->plan;
+  need(npairs >= 1, "flux needs at least one monitor pair");
+  size_t nf = p.monitors[idE[0]].freq.size();
+  for (int k = 0; k < npairs; k++) {
+    need(idE[k] >= 0 && idE[k] < (int)p.monitors.size() && idH[k] >= 0 &&
+             idH[k] < (int)p.monitors.size(),
+         "unknown monitor id");
+    need(p.monitors[idE[k]].npts == p.monitors[idH[k]].npts, "paired monitors differ in size");
+    need(p.monitors[idE[k]].freq.size() == nf && p.monitors[idH[k]].freq.size() == nf,
+         "paired monitors differ in frequencies");
+  }
+  if (!s->setup_done) {
+    for (size_t i = 0; i < nf; i++)
+      out[i] = 0.0;
+    return 0;
+  }
+  s->be->flux(p, npairs, idE, idH, out);
+  MFD_CATCH
+}
+
+int64_t mfd_kernel_launches(const mfd_sim *s) { return s && s->be ? s->be->launches() : 0; }
+
+double mfd_last_step_ms(const mfd_sim *s) { return s && s->be ? s->be->last_step_ms() : 0.0; }
+
+} // extern "C"

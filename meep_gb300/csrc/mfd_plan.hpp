@@ -1,0 +1,147 @@
+// Host-side description of one FDTD problem on a single global Yee grid.
+//
+// The reference splits the cell into chunks: one per PML slab and one for the
+// interior (src/structure.cpp:96-149, effort volumes :509-523), exchanges the
+// not-owned points between chunks every half step (src/step.cpp:225-287) and
+// picks the update formula per chunk (PML or not, src/step_db.cpp:54-60,
+// src/update_eh.cpp:159-160).  Here the whole cell is one device-resident
+// array per component; the chunk a point would belong to is recomputed from its
+// half-pixel coordinate (Plan::region), so every point is advanced with the
+// same formula and coefficients as in the reference, and no halo copies are
+// needed at all.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mfd.h"
+
+namespace mfd {
+
+constexpr int NC = MFD_NCOMP;
+constexpr int MAX_POLES = 4;
+
+inline int ctype(int c) { return c / 3; }
+inline int cdir(int c) { return c % 3; }
+inline int comp(int t, int d) { return 3 * t + d; }
+// cycle_direction for Cartesian directions (src/meep/vec.hpp:586-589)
+inline int cycle(int d, int s) { return (d + s) % 3; }
+
+struct Error : std::runtime_error {
+  explicit Error(const std::string &m) : std::runtime_error("meep: " + m) {}
+};
+
+// Source time dependence: Gaussian (both reference constructors) or CW with a
+// tanh turn-on.  dipole()/current() follow src/sources.cpp:72-110 and
+// src/meep.hpp:978-991 (current is the finite difference of the dipole).
+struct SrcTime {
+  int kind = 0; // 0 gaussian, 1 continuous
+  double freq = 0, fwidth = 0, width = 0, peak_time = 0, cutoff = 0;
+  std::complex<double> cfreq{0, 0};
+  double start = 0, end = 0, slowness = 3;
+  bool integrated = true;
+  // cached values of the last update (src_time::update)
+  double cur_time = -1e300;
+  std::complex<double> cur_dipole{0, 0}, cur_current{0, 0};
+
+  static SrcTime gaussian(double f, double fw, double s = 5.0);
+  static SrcTime gaussian_window(double f, double w, double st, double et);
+  static SrcTime continuous(std::complex<double> f, double w, double st, double et, double s);
+  std::complex<double> dipole(double t) const;
+  std::complex<double> current(double t, double dt) const {
+    return (dipole(t + dt) - dipole(t)) / dt;
+  }
+  void update(double t, double dt) {
+    if (t != cur_time) {
+      cur_dipole = dipole(t);
+      cur_current = current(t, dt);
+      cur_time = t;
+    }
+  }
+  // bandwidth used by the automatic DFT decimation (src/dft.cpp:196-217)
+  double get_fwidth() const { return kind == 0 ? fwidth : 0.0; }
+  double frequency_re() const { return kind == 0 ? freq : cfreq.real(); }
+};
+
+// One source point list on component c (E or H); ft2 = D or B receives it.
+struct SourceGroup {
+  int c = 0;
+  int src = 0;
+  std::vector<int64_t> idx; // dense indices
+  std::vector<std::complex<double>> amp;
+};
+
+struct Pole {
+  int ft = MFD_E;
+  double omega0 = 0, gamma = 0;
+  bool drude = false;
+  std::vector<double> sigma[3]; // dense per E component direction; empty = absent
+};
+
+struct Monitor {
+  int c = 0;
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  std::vector<double> w[3]; // per present direction
+  double dV = 1.0;
+  bool include_weights = true;
+  std::complex<double> scale{1, 0};
+  bool centered = false;
+  std::vector<double> freq;
+  int decimation = 1;
+  size_t npts = 0;
+};
+
+class Plan {
+public:
+  mfd_grid g{};
+  bool present[3] = {false, false, false};
+  int N[3] = {0, 0, 0};
+  int ext[3] = {1, 1, 1};
+  int64_t stride[3] = {0, 0, 0};
+  int64_t ndense = 1, nstore = 1;
+  int fastdir = 2;
+  double dt = 0, inva = 0;
+  int T[3][2] = {{0, 0}, {0, 0}, {0, 0}}; // PML slab thickness in cells
+  bool pml_dir[3] = {false, false, false};
+  std::vector<double> sig[3], kap[3], siginv[3]; // indexed by half-pixel pos 0..2N+1
+  bool have[NC] = {};
+  int shift[NC][3] = {};
+  int klo[NC][3] = {}, khi[NC][3] = {}; // updated (owned, not on a metal wall) range
+
+  // curl plan (D, B components): f -= dtdx (g1[i+s1]-g1[i] + g2[i]-g2[i+s2])
+  struct Curl {
+    int g1 = -1, g2 = -1;
+    int64_t s1 = 0, s2 = 0;
+    bool flip = false; // dtdx negated (g1 missing, g2 moved into its place)
+    int dsig = -1, dsigu = -1;
+  } curl[NC];
+
+  // material data (dense arrays, double)
+  std::vector<double> chi1inv[NC][3];
+  std::vector<double> cond[NC];                     // D/B components
+  std::vector<uint8_t> cond_chunk[NC];              // 27 flags: chunk has nonzero cond
+  std::vector<Pole> poles;                          // reference list order (last added first)
+  std::vector<SrcTime> srcs;
+  std::vector<SourceGroup> sources;
+  std::vector<Monitor> monitors;
+
+  explicit Plan(const mfd_grid &grid);
+
+  // chunk region of half-pixel position pos along d: 0 low slab, 1 interior, 2 high slab
+  int region(int d, int pos) const {
+    if (!present[d]) return 1;
+    if (T[d][0] > 0 && pos <= 2 * T[d][0]) return 0;
+    if (T[d][1] > 0 && pos > 2 * (N[d] - T[d][1])) return 2;
+    return 1;
+  }
+  bool in_slab(int d, int pos) const { return region(d, pos) != 1; }
+  int64_t dense_count() const { return ndense; }
+  int64_t store_index_of_dense(int64_t di) const;
+  void dense_coords(int64_t di, int k[3]) const;
+  void compute_cond_chunks(int c);
+};
+
+} // namespace mfd
