@@ -1,0 +1,270 @@
+"""Benchmark of the FDTD stepping path (one JSON line on stdout).
+
+Workload: the 3-D full-vector non-dispersive case -- 256^3 cells at resolution
+20, 16-cell PML on every face, 60 seeded eps boxes (eps in {2.1, 4, 12}, 20%
+diagonally anisotropic), Gaussian Ex dipole, a 200x200 z-normal flux plane at
+50 frequencies -- run in FP32 (headline) and FP64 through the meep:: C++ API
+(meep_gb300/workloads/bench_main.cpp).  A step is one full leap-frog time step
+of the whole grid including PML and the DFT accumulation.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value      Mcell-updates/s (cells x steps / time) of K steps with all state
+           resident on the GPU, timed with CUDA events on the engine's stream.
+e2e        the same through the public API with a host read of the flux
+           spectrum after every step (fields::step() + dft_flux::flux()).
+roofline   step-level: algorithmic bytes per step (every persistent state
+           array read and written once plus every coefficient array read once,
+           counted per cell from the PML layout, plus the DFT sums) / step time,
+           against the measured HBM copy bandwidth in MEASURED_PEAKS.json.
+cpu_baseline  the CPU oracle port (same C++ driver over oracle/cpu_backend.cpp)
+           on this host's cores, on a bounded sample of the same workload.
+--impl reference  times that CPU implementation alone (the reference arm).
+Multi-GPU: the path is not sharded (replicas only); with N ranks every rank
+runs the full workload on its own GPU and value sums them.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-updates/s FP32 vs FP64 at stated DFT err vs FP64; grad/forward time"
+WORKLOAD = "vec3d_full"
+GRID = (256, 256, 256)
+PML_CELLS = 17          # int(0.8 * 20 + 1 + 0.5): the reference's PML chunk thickness
+FLUX_PTS = 201 * 201    # centred points of the 200x200-cell plane
+NFREQ = 50
+FULL_STEPS = 1000       # the configuration's run length (flux comparison)
+
+
+def algorithmic_bytes_per_step(real_bytes, decimation=58):
+    """Per cell: 2*S + C words, S = persistent state arrays (E, D, B = 9 plus
+    in each PML slab the H copy and the f_w/f_u auxiliaries: 5 per slab
+    direction), C = 3 inverse-permittivity arrays; plus the DFT sums of the 4
+    flux monitors (complex double read+write per point and frequency, every
+    `decimation` steps)."""
+    n = GRID
+    frac = [2.0 * PML_CELLS / n[d] for d in range(3)]   # fraction of cells in a slab per direction
+    mean_slab_dirs = sum(frac)
+    cells = n[0] * n[1] * n[2]
+    words = 2 * (9 + 5 * mean_slab_dirs) + 3
+    field_bytes = cells * words * real_bytes
+    dft_bytes = 4 * FLUX_PTS * NFREQ * 16 * 2 / decimation
+    return field_bytes + dft_bytes
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
+            p = json.load(fp)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_driver(exe, warmup, steps, e2e_steps, total, env=None, timeout=3600):
+    out = subprocess.run([exe, WORKLOAD, str(warmup), str(steps), str(e2e_steps), str(total)],
+                         stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env,
+                         timeout=timeout)
+    if out.returncode != 0:
+        raise RuntimeError("%s failed (%d): %s" % (exe, out.returncode, out.stderr[-2000:]))
+    return json.loads(out.stdout.strip().splitlines()[-1])
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_sample(bits=32, steps=4, warmup=1):
+    """Oracle port on the host cores: a bounded sample of the same workload."""
+    from meep_gb300 import build
+    build.build_oracle()
+    exe = os.path.join(ROOT, "oracle", "_build", "bench_main%d" % bits)
+    thr = cpu_threads()
+    env = dict(os.environ, OMP_NUM_THREADS=str(thr))
+    r = run_driver(exe, warmup, steps, 0, 0, env=env)
+    mcells = r["cells"] * steps / (r["device_ms"] * 1e-3) / 1e6
+    return mcells, thr, "%d steps of %s (FP%d) after %d warm-up, OpenMP %d threads" % (
+        steps, WORKLOAD, bits, warmup, thr)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        # the reference's own CPU code cannot be built on the GPU host (its sources
+        # are not shipped there); its restatement in oracle/ is timed instead
+        per_step = []
+        mcells, thr, sample = cpu_sample(32, steps=max(1, min(args.steps, 4)), warmup=min(args.warmup, 1))
+        line = {"metric": METRIC, "value": mcells, "unit": "Mcell-updates/s", "n_gpus": args.gpus,
+                "steps": max(1, min(args.steps, 4)), "warmup": min(args.warmup, 1),
+                "ms_per_step": GRID[0] * GRID[1] * GRID[2] / (mcells * 1e6) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": "%s: 256^3 cells, res 20, PML 16 cells, 60 eps boxes, Ex dipole, "
+                                       "200x200 flux plane x 50 freqs" % WORKLOAD},
+                "cpu_baseline": {"value": mcells, "unit": "Mcell-updates/s", "cores": thr, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": mcells, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        del per_step
+        print(json.dumps(line))
+        return 0
+
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    from meep_gb300 import build
+    build.build_engine()
+    exes = build.build_bench()
+    exe32, exe64 = exes[1], exes[0]
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        dist.barrier()
+
+    e2e_steps = max(10, args.steps // 4)
+    total = max(FULL_STEPS, args.warmup + args.steps + e2e_steps)
+    with ClockSampler(local) as clk:
+        r32 = run_driver(exe32, args.warmup, args.steps, e2e_steps, total)
+    r64 = run_driver(exe64, args.warmup, args.steps, e2e_steps, total)
+
+    cells = r32["cells"]
+    t32 = r32["device_ms"] * 1e-3
+    t64 = r64["device_ms"] * 1e-3
+    if dist is not None:
+        import torch
+        tt = torch.tensor([t32, t64], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t32, t64 = float(tt[0]), float(tt[1])
+    value = world * cells * args.steps / t32 / 1e6
+    value64 = world * cells * args.steps / t64 / 1e6
+    e2e = world * cells * e2e_steps / (r32["e2e_ms"] * 1e-3) / 1e6
+    flux32, flux64 = r32["flux"], r64["flux"]
+    m = max(abs(x) for x in flux64) or 1.0
+    flux_err = max(abs(a - b) for a, b in zip(flux32, flux64)) / m
+
+    peak, peak_kind = peaks()
+    step_s = t32 / args.steps
+    alg = algorithmic_bytes_per_step(4)
+    achieved = alg / step_s / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_vec3d_full_fp32.json")
+    if os.path.exists(prof):
+        with open(prof) as fp:
+            traffic = json.load(fp).get("dram_bytes_per_step")
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    cpu_val, cpu_thr, cpu_desc = cpu_sample(32)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "%s: 256^3 cells, res 20, PML 16 cells, 60 eps boxes (20%% anisotropic), "
+                               "Ex dipole, 200x200 flux plane x 50 freqs" % WORKLOAD,
+                   "l2": "inputs larger than L2 (state ~2 GB FP32)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": value64, "unit": "Mcell-updates/s", "ms_per_step": t64 / args.steps * 1e3},
+        "fp32_over_fp64": value / value64,
+        "flux_rel_err_fp32_vs_fp64": flux_err,
+        "flux_steps": total,
+        "e2e": {"value": e2e, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 8 * NFREQ,
+                "note": "fields::step() + dft_flux::flux() per step; no per-step host inputs"},
+        "gpu_launches": int(r32["launches"]),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "unit_of_work": "one full time step (all kernels)",
+                     "algorithmic_bytes_per_step": alg},
+        "cpu_baseline": {"value": cpu_val, "unit": "Mcell-updates/s", "cores": cpu_thr, "kind": "port",
+                         "sample": cpu_desc},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

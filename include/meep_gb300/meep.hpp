@@ -610,6 +610,8 @@ public:
 
 // Copy the device DFT sums into the host dft_chunk::dft buffers.
 void sync_dfts(fields &f);
+// Advance n steps in one batched engine call (same result as n calls of step()).
+void step_n(fields &f, int n);
 
 class initialize {
 public:

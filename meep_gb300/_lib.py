@@ -1,0 +1,236 @@
+"""ctypes binding of the C ABI declared in include/mfd.h.
+
+`Engine(path)` loads a library that exports the C ABI: the CUDA engine
+meep_gb300/lib/libmfd.so (the product) or, in the tests, the CPU oracle
+oracle/_build/liboracle_mfd.so.  `Sim` wraps one simulation handle with numpy
+arrays in and out.  Errors raise MeepError with the library's message, as the
+reference's Python layer raises on meep::abort.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PRODUCT_LIB = os.path.join(HERE, "lib", "libmfd.so")
+
+E, H, D, B = 0, 1, 2, 3
+X, Y, Z = 0, 1, 2
+
+
+def comp(ftype, d):
+    return 3 * ftype + d
+
+
+class MeepError(RuntimeError):
+    pass
+
+
+class mfd_grid(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int),
+        ("n", C.c_int * 3),
+        ("io", C.c_int * 3),
+        ("a", C.c_double),
+        ("courant", C.c_double),
+        ("pml_thickness", (C.c_double * 2) * 3),
+        ("pml_R", (C.c_double * 2) * 3),
+        ("pml_stretch", (C.c_double * 2) * 3),
+        ("precision", C.c_int),
+        ("components", C.c_int),
+    ]
+
+
+# (name, restype, argtypes) of every entry point in include/mfd.h
+_P = C.c_void_p
+_DP = C.POINTER(C.c_double)
+_IP = C.POINTER(C.c_int)
+SIGNATURES = [
+    ("mfd_create", C.c_int, [C.POINTER(mfd_grid), C.POINTER(_P)]),
+    ("mfd_destroy", None, [_P]),
+    ("mfd_last_error", C.c_char_p, []),
+    ("mfd_set_chi1inv", C.c_int, [_P, C.c_int, C.c_int, _DP]),
+    ("mfd_set_conductivity", C.c_int, [_P, C.c_int, _DP]),
+    ("mfd_add_lorentzian", C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(_DP)]),
+    ("mfd_add_gaussian_src", C.c_int,
+     [_P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _IP]),
+    ("mfd_add_continuous_src", C.c_int,
+     [_P, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _IP]),
+    ("mfd_add_source_points", C.c_int, [_P, C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_int64), _DP]),
+    ("mfd_add_dft", C.c_int,
+     [_P, C.c_int, _IP, _IP, C.POINTER(_DP), C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
+      C.c_size_t, _DP, C.c_int, _IP]),
+    ("mfd_step", C.c_int, [_P, C.c_int]),
+    ("mfd_get_time", C.c_int, [_P, C.POINTER(C.c_int64), _DP]),
+    ("mfd_get_field", C.c_int, [_P, C.c_int, _DP]),
+    ("mfd_get_dft", C.c_int, [_P, C.c_int, _DP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    ("mfd_flux", C.c_int, [_P, C.c_int, _IP, _IP, _DP]),
+    ("mfd_kernel_launches", C.c_int64, [_P]),
+    ("mfd_last_step_ms", C.c_double, [_P]),
+]
+
+
+class Engine:
+    """One loaded library exporting the C ABI."""
+
+    _cache = {}
+
+    def __new__(cls, path=PRODUCT_LIB):
+        path = os.path.abspath(path)
+        if path in cls._cache:
+            return cls._cache[path]
+        if not os.path.exists(path):
+            raise MeepError("native library %s is missing; run __graft_entry__.build()" % path)
+        self = super().__new__(cls)
+        self.path = path
+        self.lib = C.CDLL(path, mode=C.RTLD_LOCAL)
+        for name, res, args in SIGNATURES:
+            fn = getattr(self.lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        cls._cache[path] = self
+        return self
+
+    def check(self, status):
+        if status != 0:
+            raise MeepError(self.lib.mfd_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+class Sim:
+    """A simulation handle on one engine: dense numpy arrays in and out."""
+
+    def __init__(self, engine, dim, n, io, a, courant=0.5, pml=None, precision=64, components=None):
+        self.eng = engine
+        g = mfd_grid()
+        g.dim = dim
+        for d in range(3):
+            g.n[d] = int(n[d])
+            g.io[d] = int(io[d])
+        g.a = a
+        g.courant = courant
+        for (d, side), (thick, R, stretch) in (pml or {}).items():
+            g.pml_thickness[d][side] = thick
+            g.pml_R[d][side] = R
+            g.pml_stretch[d][side] = stretch
+        g.precision = precision
+        mask = 0
+        for c in components or []:
+            mask |= 1 << c
+        g.components = mask
+        self.dim = dim
+        self.ext = [int(n[d]) + 1 if self._present(d) else 1 for d in range(3)]
+        self.ndense = int(np.prod(self.ext))
+        h = _P()
+        engine.check(engine.lib.mfd_create(C.byref(g), C.byref(h)))
+        self.h = h
+
+    def _present(self, d):
+        return (self.dim == 1 and d == 2) or (self.dim == 2 and d < 2) or self.dim == 3
+
+    def close(self):
+        if self.h:
+            self.eng.lib.mfd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _dense(self, arr):
+        arr = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).reshape(-1))
+        if arr.size != self.ndense:
+            raise MeepError("array has %d points, grid has %d" % (arr.size, self.ndense))
+        return arr
+
+    def set_chi1inv(self, c, d, arr):
+        arr = self._dense(arr)
+        self.eng.check(self.eng.lib.mfd_set_chi1inv(self.h, c, d, _dptr(arr)))
+
+    def set_conductivity(self, c, arr):
+        arr = self._dense(arr)
+        self.eng.check(self.eng.lib.mfd_set_conductivity(self.h, c, _dptr(arr)))
+
+    def add_lorentzian(self, omega0, gamma, drude, sigma):
+        keep = [self._dense(s) if s is not None else None for s in sigma]
+        ptrs = (_DP * 3)(*[_dptr(s) if s is not None else _DP() for s in keep])
+        self.eng.check(self.eng.lib.mfd_add_lorentzian(self.h, E, omega0, gamma, int(drude), ptrs))
+
+    def add_gaussian_src(self, freq, fwidth, integrated=True, s=5.0, window=None):
+        i = C.c_int()
+        if window is None:
+            self.eng.check(self.eng.lib.mfd_add_gaussian_src(self.h, freq, fwidth, s, 0.0, 0, int(integrated),
+                                                             C.byref(i)))
+        else:
+            self.eng.check(self.eng.lib.mfd_add_gaussian_src(self.h, freq, fwidth, window[0], window[1], 1,
+                                                             int(integrated), C.byref(i)))
+        return i.value
+
+    def add_continuous_src(self, freq, width=0.0, start=0.0, end=1e300, slowness=3.0, integrated=True):
+        i = C.c_int()
+        f = complex(freq)
+        self.eng.check(self.eng.lib.mfd_add_continuous_src(self.h, f.real, f.imag, width, start, end, slowness,
+                                                           int(integrated), C.byref(i)))
+        return i.value
+
+    def add_source_points(self, c, src, idx, amp):
+        idx = np.ascontiguousarray(np.asarray(idx, dtype=np.int64))
+        amp = np.asarray(amp, dtype=np.complex128)
+        ri = np.ascontiguousarray(np.stack([amp.real, amp.imag], axis=-1).reshape(-1))
+        self.eng.check(self.eng.lib.mfd_add_source_points(self.h, c, src, idx.size,
+                                                          idx.ctypes.data_as(C.POINTER(C.c_int64)), _dptr(ri)))
+
+    def add_dft(self, c, lo, hi, weights, dV=1.0, include_weights=True, scale=1.0, centered=True,
+                freqs=(0.1,), decimation=1):
+        lo_a = (C.c_int * 3)(*lo)
+        hi_a = (C.c_int * 3)(*hi)
+        keep = [np.ascontiguousarray(np.asarray(w, dtype=np.float64)) if w is not None else None
+                for w in weights]
+        wp = (_DP * 3)(*[_dptr(w) if w is not None else _DP() for w in keep])
+        fr = np.ascontiguousarray(np.asarray(freqs, dtype=np.float64))
+        i = C.c_int()
+        sc = complex(scale)
+        self.eng.check(self.eng.lib.mfd_add_dft(self.h, c, lo_a, hi_a, wp, dV, int(include_weights), sc.real,
+                                                sc.imag, int(centered), fr.size, _dptr(fr), decimation,
+                                                C.byref(i)))
+        return i.value
+
+    def step(self, n=1):
+        self.eng.check(self.eng.lib.mfd_step(self.h, int(n)))
+
+    def time(self):
+        t = C.c_int64()
+        dt = C.c_double()
+        self.eng.check(self.eng.lib.mfd_get_time(self.h, C.byref(t), C.byref(dt)))
+        return t.value, dt.value
+
+    def get_field(self, c):
+        out = np.zeros(self.ndense)
+        self.eng.check(self.eng.lib.mfd_get_field(self.h, c, _dptr(out)))
+        return out.reshape(self.ext)
+
+    def get_dft(self, mid):
+        npts = C.c_size_t()
+        nf = C.c_size_t()
+        self.eng.check(self.eng.lib.mfd_get_dft(self.h, mid, None, C.byref(npts), C.byref(nf)))
+        out = np.zeros(2 * npts.value * nf.value)
+        self.eng.check(self.eng.lib.mfd_get_dft(self.h, mid, _dptr(out), C.byref(npts), C.byref(nf)))
+        return (out[0::2] + 1j * out[1::2]).reshape(npts.value, nf.value)
+
+    def flux(self, idE, idH, nfreq):
+        idE = (C.c_int * len(idE))(*idE)
+        idH = (C.c_int * len(idH))(*idH)
+        out = np.zeros(nfreq)
+        self.eng.check(self.eng.lib.mfd_flux(self.h, len(idE), idE, idH, _dptr(out)))
+        return out
+
+    def launches(self):
+        return self.eng.lib.mfd_kernel_launches(self.h)
+
+    def last_step_ms(self):
+        return self.eng.lib.mfd_last_step_ms(self.h)

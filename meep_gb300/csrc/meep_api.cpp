@@ -211,6 +211,18 @@ struct Dense {
         for (k[2] = 0; k[2] < ext[2]; k[2]++)
           fn(k, index(k));
   }
+  // same, with the slowest direction spread over OpenMP threads (for
+  // material functions that declare themselves thread-safe)
+  template <class F> void for_each_parallel(F fn) const {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k0 = 0; k0 < ext[0]; k0++) {
+      int k[3];
+      k[0] = k0;
+      for (k[1] = 0; k[1] < ext[1]; k[1]++)
+        for (k[2] = 0; k[2] < ext[2]; k[2]++)
+          fn(k, index(k));
+    }
+  }
 };
 
 /* ----------------------------------------------------------- structure */
@@ -299,17 +311,22 @@ void structure::set_epsilon(material_function &mat, bool use_aa, double tol, int
       arr[q].assign(dn.count(), 0.0);
     ivec shift1(gv.dim, 0);
     shift1.set_direction(direction(dc), 1);
-    dn.for_each([&](const int k[3], int64_t di) {
+    auto body = [&](const int k[3], int64_t di) {
       ivec here = dn.iloc(gv, c, k);
       double row[3], row_off[3];
       mat.eff_chi1inv_row(c, row, dV(gv, here), tol, maxeval);
       mat.eff_chi1inv_row(c, row_off, dV(gv, here - shift1), tol, maxeval);
-      for (int q = 0; q < 3; q++) {
-        double v = (q == dc) ? row[q] : row_off[q];
-        arr[q][di] = v;
-        if (v != (q == dc ? 1.0 : 0.0)) trivial[q] = false;
-      }
-    });
+      for (int q = 0; q < 3; q++)
+        arr[q][di] = (q == dc) ? row[q] : row_off[q];
+    };
+    if (mat.is_thread_safe()) dn.for_each_parallel(body);
+    else dn.for_each(body);
+    for (int q = 0; q < 3; q++)
+      for (double v : arr[q])
+        if (v != (q == dc ? 1.0 : 0.0)) {
+          trivial[q] = false;
+          break;
+        }
     for (int q = 0; q < 3; q++) {
       if (q != dc && trivial[q]) arr[q].clear();
       d->chi1inv[dc][q] = std::move(arr[q]);
@@ -983,6 +1000,12 @@ void fields::step() {
   ensure_engine(*this);
   chk(mfd_step(d->sim, 1));
   t += 1;
+}
+
+void step_n(fields &f, int n) {
+  ensure_engine(f);
+  chk(mfd_step(f.d->sim, n));
+  f.t += n;
 }
 
 double fields::last_step_ms() const { return d->sim ? mfd_last_step_ms(d->sim) : 0.0; }

@@ -1,0 +1,952 @@
+// CUDA backend of the FDTD stepping engine, templated on the field precision R
+// (double or float).  Instantiated by mfd_cuda_f64.cu and mfd_cuda_f32.cu.
+//
+// Data layout in HBM: one array per field component over the whole cell
+// (Plan::nstore points, last direction unit-stride and padded to a multiple of
+// 8 points), auxiliary PML/conductivity arrays of the same shape, 1-D PML
+// coefficient tables per direction indexed by half-pixel position.  Every
+// kernel advances the points of one component inside a box of point indices;
+// the reference's per-chunk choice of formula is recomputed per point from its
+// chunk region (see mfd_plan.hpp), so no halo exchange exists.
+//
+// Per-point arithmetic follows, in the same operation order:
+//   curl            step_curl               src/step_generic.cpp:65-249
+//   E/H update      step_update_EDHB        src/step_generic.cpp:566-785
+//   polarisation    lorentzian update_P     src/susceptibility.cpp:188-262
+//   sources         step_source             src/step.cpp:295-318,
+//                   integrated sources      src/update_eh.cpp:126-136
+//   DFT             dft_chunk::update_dft   src/dft.cpp:266-308
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mfd_backend.hpp"
+
+namespace mfd {
+namespace cuda_impl {
+
+static const double kPi = 3.141592653589793238462643383276;
+
+inline void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess)
+    throw Error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+
+// Region geometry shared by all kernels (passed by value).
+struct Geo {
+  int N[3];
+  int T[3][2];
+  int pml[3];        // PML exists along direction
+  long long stride[3];
+  int fast, mid, slow; // direction mapped to grid x / y / z
+};
+
+__device__ __forceinline__ int region_of(const Geo &g, int d, int pos) {
+  if (g.T[d][0] > 0 && pos <= 2 * g.T[d][0]) return 0;
+  if (g.T[d][1] > 0 && pos > 2 * (g.N[d] - g.T[d][1])) return 2;
+  return 1;
+}
+__device__ __forceinline__ bool slab(const Geo &g, int d, int pos) {
+  return g.pml[d] && region_of(g, d, pos) != 1;
+}
+
+struct Box {
+  int lo[3], n[3];
+};
+
+// point indices of this thread inside the box; false if outside
+__device__ __forceinline__ bool box_point(const Geo &g, const Box &b, int k[3]) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  int m = blockIdx.y * blockDim.y + threadIdx.y;
+  int s = blockIdx.z;
+  if (a >= b.n[g.fast] || m >= b.n[g.mid] || s >= b.n[g.slow]) return false;
+  k[g.fast] = b.lo[g.fast] + a;
+  k[g.mid] = b.lo[g.mid] + m;
+  k[g.slow] = b.lo[g.slow] + s;
+  return true;
+}
+
+__device__ __forceinline__ long long lin(const Geo &g, const int k[3]) {
+  return k[0] * g.stride[0] + k[1] * g.stride[1] + k[2] * g.stride[2];
+}
+
+template <typename R> struct Tables {
+  const R *sig[3], *kap[3], *siginv[3];
+};
+
+// ------------------------------------------------------------------ curl
+template <typename R> struct CurlArgs {
+  R *f, *fu, *fcnd;
+  const R *cnd, *cndinv;
+  const R *g1, *g1h, *g2, *g2h; // g*h: H arrays for D curls (null for B curls)
+  int g1dir, g2dir;
+  long long s1, s2;
+  R dtdx, dt2;
+  int dsig, dsigu;
+  int shift[3];
+  unsigned cond_chunks; // bit r: chunk region r (rx*9+ry*3+rz) has conductivity
+  Box box;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) curl_kernel(Geo g, Tables<R> tb, CurlArgs<R> a) {
+  int k[3];
+  if (!box_point(g, a.box, k)) return;
+  const long long i = lin(g, k);
+  const R *G1 = a.g1;
+  if (a.g1h && slab(g, a.g1dir, 2 * k[a.g1dir])) G1 = a.g1h;
+  R X = G1[i + a.s1] - G1[i];
+  if (a.g2) {
+    const R *G2 = a.g2;
+    if (a.g2h && slab(g, a.g2dir, 2 * k[a.g2dir])) G2 = a.g2h;
+    X = X + G2[i] - G2[i + a.s2];
+  }
+  const bool sg = a.dsig >= 0 && slab(g, a.dsig, a.shift[a.dsig] + 2 * k[a.dsig]);
+  const bool su = a.dsigu >= 0 && slab(g, a.dsigu, a.shift[a.dsigu] + 2 * k[a.dsigu]);
+  bool hc = a.cnd != nullptr;
+  if (sg && hc) {
+    int r = region_of(g, 0, a.shift[0] + 2 * k[0]) * 9 + region_of(g, 1, a.shift[1] + 2 * k[1]) * 3 +
+            region_of(g, 2, a.shift[2] + 2 * k[2]);
+    hc = (a.cond_chunks >> r) & 1u;
+  }
+  R *F = a.f;
+  const R one = R(1);
+  if (!sg) {
+    if (!su) {
+      if (hc) F[i] = ((one - a.dt2 * a.cnd[i]) * F[i] - a.dtdx * X) * a.cndinv[i];
+      else F[i] -= a.dtdx * X;
+    }
+    else {
+      const int ku = a.shift[a.dsigu] + 2 * k[a.dsigu];
+      R fprev = a.fu[i];
+      R fun;
+      if (hc) fun = ((one - a.dt2 * a.cnd[i]) * fprev - a.dtdx * X) * a.cndinv[i];
+      else fun = fprev - a.dtdx * X;
+      a.fu[i] = fun;
+      F[i] = tb.siginv[a.dsigu][ku] * ((tb.kap[a.dsigu][ku] - tb.sig[a.dsigu][ku]) * F[i] + fun - fprev);
+    }
+  }
+  else {
+    const int kk = a.shift[a.dsig] + 2 * k[a.dsig];
+    const R ks = tb.kap[a.dsig][kk] - tb.sig[a.dsig][kk], si = tb.siginv[a.dsig][kk];
+    if (!su) {
+      if (hc) {
+        R fcp = a.fcnd[i];
+        R fcn = ((one - a.dt2 * a.cnd[i]) * fcp - a.dtdx * X) * a.cndinv[i];
+        a.fcnd[i] = fcn;
+        F[i] = (ks * F[i] + (fcn - fcp)) * si;
+      }
+      else
+        F[i] = (ks * F[i] - a.dtdx * X) * si;
+    }
+    else {
+      const int ku = a.shift[a.dsigu] + 2 * k[a.dsigu];
+      R fprev = a.fu[i];
+      R fun;
+      if (hc) {
+        R fcp = a.fcnd[i];
+        R fcn = ((one - a.dt2 * a.cnd[i]) * fcp - a.dtdx * X) * a.cndinv[i];
+        a.fcnd[i] = fcn;
+        fun = (ks * fprev + (fcn - fcp)) * si;
+      }
+      else
+        fun = (ks * fprev - a.dtdx * X) * si;
+      a.fu[i] = fun;
+      F[i] = tb.siginv[a.dsigu][ku] * ((tb.kap[a.dsigu][ku] - tb.sig[a.dsigu][ku]) * F[i] + fun - fprev);
+    }
+  }
+}
+
+// ------------------------------------------------- H = B in the PML slab
+template <typename R> struct HArgs {
+  R *h, *fw;
+  const R *b;
+  int dir;
+  int shift[3];
+  Box box;
+};
+
+template <typename R> __global__ void __launch_bounds__(256) h_pml_kernel(Geo g, Tables<R> tb, HArgs<R> a) {
+  int k[3];
+  if (!box_point(g, a.box, k)) return;
+  const int kw = a.shift[a.dir] + 2 * k[a.dir];
+  if (!slab(g, a.dir, kw)) return;
+  const long long i = lin(g, k);
+  R fwprev = a.fw[i], kapwkw = tb.kap[a.dir][kw], sigwkw = tb.sig[a.dir][kw];
+  R fwn = a.b[i];
+  a.fw[i] = fwn;
+  a.h[i] += (kapwkw + sigwkw) * fwn - (kapwkw - sigwkw) * fwprev;
+}
+
+// --------------------------------------------------- E, then its poles
+template <typename R> struct PoleArgs {
+  R *P, *PP;
+  const R *s;
+  R gamma1inv, gamma1, w0, w0d;
+};
+
+template <typename R> struct EArgs {
+  R *e, *fw;
+  const R *dfield, *chi;
+  int dir;
+  int shift[3];
+  int npoles;
+  PoleArgs<R> pole[MAX_POLES];
+  Box box;
+};
+
+template <typename R> struct EPoint {
+  R e, fw;
+  R p[MAX_POLES], pp[MAX_POLES];
+};
+
+// Computes the new E (and f_w, P, P_prev) of one point; srcA is subtracted
+// from D - P (integrated sources), nsrc == 0 for ordinary points.
+template <typename R>
+__device__ __forceinline__ void e_point(const Geo &g, const Tables<R> &tb, const EArgs<R> &a,
+                                        const int k[3], long long i, int nsrc, const R *srcA,
+                                        EPoint<R> &out) {
+  R gs = a.dfield[i];
+  for (int q = 0; q < a.npoles; q++)
+    if (a.pole[q].P) gs -= a.pole[q].P[i];
+  for (int j = 0; j < nsrc; j++)
+    gs -= srcA[j];
+  const R us = a.chi[i];
+  const int kw = a.shift[a.dir] + 2 * k[a.dir];
+  const bool w = slab(g, a.dir, kw);
+  R W;
+  if (w) {
+    R fwprev = a.fw[i], kapwkw = tb.kap[a.dir][kw], sigwkw = tb.sig[a.dir][kw];
+    R fwn = (gs * us);
+    out.fw = fwn;
+    out.e = a.e[i] + ((kapwkw + sigwkw) * fwn - (kapwkw - sigwkw) * fwprev);
+    W = fwn;
+  }
+  else {
+    out.e = (gs * us);
+    out.fw = R(0);
+    W = out.e;
+  }
+  for (int q = 0; q < a.npoles; q++) {
+    const PoleArgs<R> &pl = a.pole[q];
+    if (!pl.P) continue;
+    R pcur = pl.P[i];
+    out.p[q] = pl.gamma1inv * (pcur * (R(2) - pl.w0d) - pl.gamma1 * pl.PP[i] + pl.w0 * (pl.s[i] * W));
+    out.pp[q] = pcur;
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void e_store(const Geo &g, const EArgs<R> &a, const int k[3], long long i,
+                                        const EPoint<R> &v) {
+  a.e[i] = v.e;
+  if (slab(g, a.dir, a.shift[a.dir] + 2 * k[a.dir])) a.fw[i] = v.fw;
+  for (int q = 0; q < a.npoles; q++)
+    if (a.pole[q].P) {
+      a.pole[q].P[i] = v.p[q];
+      a.pole[q].PP[i] = v.pp[q];
+    }
+}
+
+template <typename R> __global__ void __launch_bounds__(256) e_kernel(Geo g, Tables<R> tb, EArgs<R> a) {
+  int k[3];
+  if (!box_point(g, a.box, k)) return;
+  const long long i = lin(g, k);
+  EPoint<R> v;
+  e_point(g, tb, a, k, i, 0, (const R *)nullptr, v);
+  e_store(g, a, k, i, v);
+}
+
+// ----------------------------------------- integrated E sources (sparse)
+// One entry per distinct source point of one E component: up to MAXS source
+// terms, each amp * dipole(src) with the dipole passed per step.
+constexpr int MAXS = 4;
+struct SrcPoint {
+  long long i;          // storage index
+  int k[3];
+  int nterm;
+  int src[MAXS];
+  double amp[MAXS][2];
+};
+
+template <typename R> struct SrcBuf {
+  EPoint<R> *v;
+};
+
+struct DipoleVals {
+  double re[16], im[16];
+};
+
+template <typename R>
+__global__ void src_pre_kernel(Geo g, Tables<R> tb, EArgs<R> a, const SrcPoint *pts, int n,
+                               DipoleVals dv, EPoint<R> *out) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const SrcPoint &sp = pts[j];
+  R A[MAXS];
+  for (int t = 0; t < sp.nterm; t++) {
+    // real part of amp * dipole (std::complex product)
+    double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
+    A[t] = R(re);
+  }
+  e_point(g, tb, a, sp.k, sp.i, sp.nterm, A, out[j]);
+}
+
+template <typename R>
+__global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, const EPoint<R> *in) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  e_store(g, a, pts[j].k, pts[j].i, in[j]);
+}
+
+// current (non-integrated) sources on D or B: f -= Re(amp*J*dt*condinv)
+struct CurPoint {
+  long long i;
+  int src;
+  double amp[2];
+};
+
+template <typename R>
+__global__ void src_current_kernel(R *f, const R *cndinv, const CurPoint *pts, int n,
+                                   DipoleVals cur, double dt) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const CurPoint &p = pts[j];
+  // A = amp * current * dt (* condinv), complex arithmetic of the reference
+  double cre = cur.re[p.src], cim = cur.im[p.src];
+  double are = p.amp[0] * cre - p.amp[1] * cim;
+  double aim = p.amp[0] * cim + p.amp[1] * cre;
+  are = are * dt;
+  aim = aim * dt;
+  if (cndinv) {
+    double ci = double(cndinv[p.i]);
+    are = are * ci;
+  }
+  (void)aim;
+  f[p.i] -= R(are);
+}
+
+// ------------------------------------------------------------------ DFT
+template <typename R> struct DftArgs {
+  const R *f, *fb;   // component array; fb = B array for H components (else null)
+  int hdir;          // direction of the H component (H/B selection)
+  int hshift;        // shift of the component along hdir
+  const double *w[3];
+  double dV;
+  int include_weights;
+  int dim;
+  int lo[3], n[3];
+  int ad0, ad1; // averaging directions (-1 none)
+  double2 *acc;
+  const double2 *ph;
+  int nf;
+  long long npts;
+};
+
+template <typename R>
+__device__ __forceinline__ R dft_val(const Geo &g, const DftArgs<R> &a, const int k[3]) {
+  const long long i = lin(g, k);
+  if (a.fb && !slab(g, a.hdir, a.hshift + 2 * k[a.hdir])) return a.fb[i];
+  return a.f[i];
+}
+
+static __global__ void dft_phase_kernel(const double *freq, int nf, double time, double sre, double sim,
+                                 double2 *ph) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nf) return;
+  double s, c;
+  sincos(2 * kPi * freq[w] * time, &s, &c);
+  ph[w] = make_double2(c * sre - s * sim, c * sim + s * sre);
+}
+
+template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long total = a.npts * a.nf;
+  if (t >= total) return;
+  long long p = t / a.nf;
+  int w = int(t - p * a.nf);
+  int q[3];
+  q[2] = int(p % a.n[2]);
+  long long r = p / a.n[2];
+  q[1] = int(r % a.n[1]);
+  q[0] = int(r / a.n[1]);
+  int k[3] = {a.lo[0] + q[0], a.lo[1] + q[1], a.lo[2] + q[2]};
+  double wgt = 1.0;
+  if (a.include_weights) {
+    double wx = a.w[0] ? a.w[0][q[0]] : 1.0;
+    double wy = a.w[1] ? a.w[1][q[1]] : 1.0;
+    double wz = a.w[2] ? a.w[2][q[2]] : 1.0;
+    if (a.dim == 2) wgt = wy * (wx * (a.dV * 1.0));
+    else if (a.dim == 3) wgt = wz * (wy * (a.dV * wx));
+    else wgt = 1.0 * (1.0 * (a.dV * wz));
+  }
+  R fv;
+  if (a.ad1 >= 0) {
+    int k1[3] = {k[0], k[1], k[2]}, k2[3] = {k[0], k[1], k[2]}, k3[3] = {k[0], k[1], k[2]};
+    k1[a.ad0]++;
+    k2[a.ad1]++;
+    k3[a.ad0]++;
+    k3[a.ad1]++;
+    fv = R((wgt * 0.25) * (dft_val(g, a, k) + dft_val(g, a, k1) + dft_val(g, a, k2) + dft_val(g, a, k3)));
+  }
+  else if (a.ad0 >= 0) {
+    int k1[3] = {k[0], k[1], k[2]};
+    k1[a.ad0]++;
+    fv = R((wgt * 0.5) * (dft_val(g, a, k) + dft_val(g, a, k1)));
+  }
+  else
+    fv = R(wgt * dft_val(g, a, k));
+  double2 ph = a.ph[w];
+  double2 acc = a.acc[t];
+  acc.x += double(fv) * ph.x;
+  acc.y += double(fv) * ph.y;
+  a.acc[t] = acc;
+}
+
+// flux: out[w] = sum_k Re(E conj H), one block per frequency, double reduction
+static __global__ void flux_kernel(const double2 *E, const double2 *H, long long npts, int nf, double *out) {
+  int w = blockIdx.x;
+  double s = 0;
+  for (long long k = threadIdx.x; k < npts; k += blockDim.x) {
+    double2 e = E[k * nf + w], h = H[k * nf + w];
+    s += e.x * h.x + e.y * h.y;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[w] += red[0];
+}
+
+// ---------------------------------------------------------------- backend
+template <typename R> class CudaBackend : public Backend {
+public:
+  explicit CudaBackend(const Plan &p) {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+    cuda_check(cudaEventCreate(&ev0), "event");
+    cuda_check(cudaEventCreate(&ev1), "event");
+    (void)p;
+  }
+  ~CudaBackend() override {
+    for (void *ptr : allocs)
+      cudaFree(ptr);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaStreamDestroy(stream);
+  }
+
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<void *> allocs;
+  Geo geo{};
+  Tables<R> tb{};
+  R *f[NC] = {}, *fu[NC] = {}, *fw[NC] = {}, *fcnd[NC] = {}, *chi[NC] = {}, *cnd[NC] = {},
+    *cndinv[NC] = {};
+  struct DPole {
+    R *P[3] = {}, *PP[3] = {}, *s[3] = {};
+    R gamma1inv, gamma1, w0, w0d;
+  };
+  std::vector<DPole> poles;
+  // sources
+  SrcPoint *d_srcpts[3] = {};
+  int nsrcpts[3] = {};
+  EPoint<R> *d_srcbuf[3] = {};
+  CurPoint *d_cur[NC] = {};
+  int ncur[NC] = {};
+  // monitors
+  struct DMon {
+    double2 *acc = nullptr, *ph = nullptr;
+    double *freq = nullptr;
+    double *w[3] = {};
+  };
+  std::vector<DMon> mons;
+  long long nlaunch = 0;
+  double *d_flux = nullptr;
+  size_t flux_cap = 0;
+  double ms = 0;
+  bool timing = false;
+
+  template <typename T> T *dalloc(size_t n) {
+    void *ptr = nullptr;
+    if (n == 0) n = 1;
+    cuda_check(cudaMalloc(&ptr, n * sizeof(T)), "cudaMalloc");
+    allocs.push_back(ptr);
+    return (T *)ptr;
+  }
+  template <typename T> T *dzeros(size_t n) {
+    T *ptr = dalloc<T>(n);
+    cuda_check(cudaMemsetAsync(ptr, 0, n * sizeof(T), stream), "memset");
+    return ptr;
+  }
+  template <typename T> T *dupload(const std::vector<T> &h) {
+    T *ptr = dalloc<T>(h.size());
+    cuda_check(cudaMemcpyAsync(ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, stream),
+               "upload");
+    cuda_check(cudaStreamSynchronize(stream), "sync");
+    return ptr;
+  }
+  std::vector<R> to_store(const Plan &p, const std::vector<double> &dense, double dflt) {
+    std::vector<R> out(p.nstore, R(0));
+    for (int64_t di = 0; di < p.ndense; di++)
+      out[p.store_index_of_dense(di)] = R(dense.empty() ? dflt : dense[di]);
+    return out;
+  }
+
+  void setup(Plan &p) override {
+    for (int d = 0; d < 3; d++) {
+      geo.N[d] = p.N[d];
+      geo.T[d][0] = p.T[d][0];
+      geo.T[d][1] = p.T[d][1];
+      geo.pml[d] = p.pml_dir[d];
+      geo.stride[d] = p.stride[d];
+    }
+    if (p.g.dim == 3) {
+      geo.fast = 2;
+      geo.mid = 1;
+      geo.slow = 0;
+    }
+    else if (p.g.dim == 2) {
+      geo.fast = 1;
+      geo.mid = 0;
+      geo.slow = 2;
+    }
+    else {
+      geo.fast = 2;
+      geo.mid = 0;
+      geo.slow = 1;
+    }
+    for (int d = 0; d < 3; d++) {
+      size_t n = p.sig[d].size();
+      std::vector<R> s(n), k(n), si(n);
+      for (size_t i = 0; i < n; i++) {
+        s[i] = R(p.sig[d][i]);
+        k[i] = R(p.kap[d][i]);
+        si[i] = (p.sig[d][i] == 0.0 && p.kap[d][i] == 1.0) ? R(1) : R(1) / (k[i] + s[i]);
+      }
+      tb.sig[d] = dupload(s);
+      tb.kap[d] = dupload(k);
+      tb.siginv[d] = dupload(si);
+    }
+    for (int c = 0; c < NC; c++) {
+      if (!p.have[c]) continue;
+      int t = ctype(c), d = cdir(c);
+      f[c] = dzeros<R>(p.nstore);
+      if (t == MFD_D || t == MFD_B) {
+        const Plan::Curl &cp = p.curl[c];
+        if (cp.dsigu >= 0) fu[c] = dzeros<R>(p.nstore);
+        if (!p.cond[c].empty()) {
+          std::vector<R> cs = to_store(p, p.cond[c], 0.0), ci(p.nstore);
+          for (int64_t i = 0; i < p.nstore; i++)
+            ci[i] = R(1 / (1 + double(cs[i]) * p.dt * 0.5));
+          cnd[c] = dupload(cs);
+          cndinv[c] = dupload(ci);
+          if (cp.dsig >= 0) fcnd[c] = dzeros<R>(p.nstore);
+        }
+      }
+      if ((t == MFD_E || t == MFD_H) && p.pml_dir[d]) fw[c] = dzeros<R>(p.nstore);
+      if (t == MFD_E) {
+        for (int dd = 0; dd < 3; dd++)
+          if (dd != d && !p.chi1inv[c][dd].empty())
+            for (double v : p.chi1inv[c][dd])
+              if (v != 0.0) throw Error("off-diagonal chi1inv is not supported yet by the CUDA engine");
+        chi[c] = dupload(to_store(p, p.chi1inv[c][d], 1.0));
+      }
+      if (t == MFD_H)
+        for (int dd = 0; dd < 3; dd++)
+          if (!p.chi1inv[c][dd].empty())
+            for (double v : p.chi1inv[c][dd])
+              if (v != (dd == d ? 1.0 : 0.0)) throw Error("mu != 1 is not supported");
+    }
+    for (const Pole &pl : p.poles) {
+      DPole dp;
+      R omega_0 = R(pl.omega0), gamma = R(pl.gamma), dt = R(p.dt);
+      const R omega2pi = R(2 * kPi * omega_0), g2pi = R(gamma * 2 * kPi);
+      dp.w0 = omega2pi * omega2pi * dt * dt;
+      dp.gamma1inv = R(1) / (R(1) + g2pi * dt / R(2));
+      dp.gamma1 = (R(1) - g2pi * dt / R(2));
+      dp.w0d = pl.drude ? R(0) : dp.w0;
+      for (int d = 0; d < 3; d++) {
+        int ec = comp(MFD_E, d);
+        if (!p.have[ec] || pl.sigma[d].empty()) continue;
+        dp.s[d] = dupload(to_store(p, pl.sigma[d], 0.0));
+        dp.P[d] = dzeros<R>(p.nstore);
+        dp.PP[d] = dzeros<R>(p.nstore);
+      }
+      poles.push_back(dp);
+    }
+    setup_sources(p);
+    cuda_check(cudaStreamSynchronize(stream), "setup sync");
+  }
+
+  void setup_sources(Plan &p) {
+    if (p.srcs.size() > 16) throw Error("at most 16 source time functions are supported");
+    // integrated E sources grouped per (component, point), in list order
+    for (int d = 0; d < 3; d++) {
+      std::vector<SrcPoint> pts;
+      std::vector<int64_t> keys;
+      for (const SourceGroup &sg : p.sources) {
+        if (sg.c != comp(MFD_E, d) || !p.srcs[sg.src].integrated) continue;
+        for (size_t j = 0; j < sg.idx.size(); j++) {
+          int64_t di = sg.idx[j];
+          size_t q = std::find(keys.begin(), keys.end(), di) - keys.begin();
+          if (q == keys.size()) {
+            keys.push_back(di);
+            SrcPoint sp{};
+            sp.i = p.store_index_of_dense(di);
+            p.dense_coords(di, sp.k);
+            pts.push_back(sp);
+          }
+          SrcPoint &sp = pts[q];
+          if (sp.nterm >= MAXS) throw Error("too many sources on one point");
+          sp.src[sp.nterm] = sg.src;
+          sp.amp[sp.nterm][0] = sg.amp[j].real();
+          sp.amp[sp.nterm][1] = sg.amp[j].imag();
+          sp.nterm++;
+        }
+      }
+      // points outside the updated range are never advanced (metal walls)
+      std::vector<SrcPoint> keep;
+      int ec = comp(MFD_E, d);
+      for (const SrcPoint &sp : pts) {
+        bool in = true;
+        for (int q = 0; q < 3; q++)
+          in = in && sp.k[q] >= p.klo[ec][q] && sp.k[q] <= p.khi[ec][q];
+        if (in) keep.push_back(sp);
+      }
+      nsrcpts[d] = (int)keep.size();
+      if (!keep.empty()) {
+        d_srcpts[d] = dupload(keep);
+        d_srcbuf[d] = dalloc<EPoint<R>>(keep.size());
+      }
+    }
+    // current sources (non-integrated) on D or B
+    for (int c = 0; c < NC; c++) {
+      int t = ctype(c);
+      if (t != MFD_D && t != MFD_B) continue;
+      std::vector<CurPoint> pts;
+      int srct = t == MFD_D ? MFD_E : MFD_H;
+      for (const SourceGroup &sg : p.sources) {
+        if (sg.c != comp(srct, cdir(c)) || p.srcs[sg.src].integrated) continue;
+        for (size_t j = 0; j < sg.idx.size(); j++) {
+          CurPoint cp{};
+          cp.i = p.store_index_of_dense(sg.idx[j]);
+          cp.src = sg.src;
+          cp.amp[0] = sg.amp[j].real();
+          cp.amp[1] = sg.amp[j].imag();
+          pts.push_back(cp);
+        }
+      }
+      ncur[c] = (int)pts.size();
+      if (!pts.empty()) d_cur[c] = dupload(pts);
+    }
+  }
+
+  void add_monitor(Plan &p, int id) override {
+    if ((int)mons.size() <= id) mons.resize(id + 1);
+    const Monitor &m = p.monitors[id];
+    DMon &dm = mons[id];
+    dm.acc = dzeros<double2>(m.npts * m.freq.size());
+    dm.ph = dalloc<double2>(m.freq.size());
+    dm.freq = dupload(m.freq);
+    for (int d = 0; d < 3; d++)
+      if (!m.w[d].empty()) dm.w[d] = dupload(m.w[d]);
+    cuda_check(cudaStreamSynchronize(stream), "monitor sync");
+  }
+
+  Box full_box(const Plan &p, int c) const {
+    Box b;
+    for (int d = 0; d < 3; d++) {
+      b.lo[d] = p.klo[c][d];
+      b.n[d] = p.khi[c][d] - p.klo[c][d] + 1;
+    }
+    return b;
+  }
+
+  void launch_dims(const Box &b, dim3 &grid, dim3 &block) const {
+    int nf = b.n[geo.fast], nm = b.n[geo.mid], ns = b.n[geo.slow];
+    int bx = nf >= 128 ? 128 : (nf >= 64 ? 64 : 32);
+    int by = 256 / bx;
+    block = dim3(bx, by, 1);
+    grid = dim3((nf + bx - 1) / bx, (nm + by - 1) / by, ns);
+  }
+  bool box_empty(const Box &b) const { return b.n[0] <= 0 || b.n[1] <= 0 || b.n[2] <= 0; }
+
+  void curl(Plan &p, int c) {
+    const Plan::Curl &cp = p.curl[c];
+    if (cp.g1 < 0) return;
+    CurlArgs<R> a{};
+    a.f = f[c];
+    a.fu = fu[c];
+    a.fcnd = fcnd[c];
+    a.cnd = cnd[c];
+    a.cndinv = cndinv[c];
+    bool dcurl = ctype(c) == MFD_D;
+    auto src_ptrs = [&](int gc, const R *&gp, const R *&gh, int &gdir) {
+      gdir = cdir(gc);
+      if (dcurl) {
+        gp = f[comp(MFD_B, gdir)];
+        gh = p.pml_dir[gdir] ? f[gc] : nullptr;
+      }
+      else {
+        gp = f[gc];
+        gh = nullptr;
+      }
+    };
+    src_ptrs(cp.g1, a.g1, a.g1h, a.g1dir);
+    if (cp.g2 >= 0) src_ptrs(cp.g2, a.g2, a.g2h, a.g2dir);
+    a.s1 = cp.s1;
+    a.s2 = cp.s2;
+    a.dtdx = cp.flip ? -R(p.g.courant) : R(p.g.courant);
+    a.dt2 = R(p.dt) * R(0.5);
+    a.dsig = cp.dsig;
+    a.dsigu = cp.dsigu;
+    for (int d = 0; d < 3; d++)
+      a.shift[d] = p.shift[c][d];
+    a.cond_chunks = 0;
+    if (!p.cond_chunk[c].empty())
+      for (int r = 0; r < 27; r++)
+        if (p.cond_chunk[c][r]) a.cond_chunks |= 1u << r;
+    a.box = full_box(p, c);
+    if (box_empty(a.box)) return;
+    dim3 grid, block;
+    launch_dims(a.box, grid, block);
+    curl_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+    nlaunch++;
+  }
+
+  void update_h(Plan &p, int hc) {
+    int d = cdir(hc);
+    if (!p.pml_dir[d]) return;
+    HArgs<R> a{};
+    a.h = f[hc];
+    a.fw = fw[hc];
+    a.b = f[comp(MFD_B, d)];
+    a.dir = d;
+    for (int q = 0; q < 3; q++)
+      a.shift[q] = p.shift[hc][q];
+    Box full = full_box(p, hc);
+    // the two slabs along d: positions 2k <= 2T_lo and 2k > 2(N - T_hi)
+    for (int side = 0; side < 2; side++) {
+      if (p.T[d][side] == 0) continue;
+      Box b = full;
+      int lo = full.lo[d], hi = full.lo[d] + full.n[d] - 1;
+      if (side == 0) hi = std::min(hi, p.T[d][0]);
+      else lo = std::max(lo, p.N[d] - p.T[d][1] + 1);
+      b.lo[d] = lo;
+      b.n[d] = hi - lo + 1;
+      if (box_empty(b)) continue;
+      a.box = b;
+      dim3 grid, block;
+      launch_dims(b, grid, block);
+      h_pml_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+      nlaunch++;
+    }
+  }
+
+  EArgs<R> eargs(Plan &p, int d) {
+    int ec = comp(MFD_E, d);
+    EArgs<R> a{};
+    a.e = f[ec];
+    a.fw = fw[ec];
+    a.dfield = f[comp(MFD_D, d)];
+    a.chi = chi[ec];
+    a.dir = d;
+    for (int q = 0; q < 3; q++)
+      a.shift[q] = p.shift[ec][q];
+    a.npoles = (int)poles.size();
+    for (int q = 0; q < a.npoles; q++) {
+      a.pole[q].P = poles[q].P[d];
+      a.pole[q].PP = poles[q].PP[d];
+      a.pole[q].s = poles[q].s[d];
+      a.pole[q].gamma1inv = poles[q].gamma1inv;
+      a.pole[q].gamma1 = poles[q].gamma1;
+      a.pole[q].w0 = poles[q].w0;
+      a.pole[q].w0d = poles[q].w0d;
+    }
+    a.box = full_box(p, ec);
+    return a;
+  }
+
+  void update_e(Plan &p, const DipoleVals &dip) {
+    for (int d = 0; d < 3; d++) {
+      int ec = comp(MFD_E, d);
+      if (!p.have[ec]) continue;
+      EArgs<R> a = eargs(p, d);
+      if (box_empty(a.box)) continue;
+      int ns = nsrcpts[d];
+      if (ns) {
+        src_pre_kernel<R><<<(ns + 127) / 128, 128, 0, stream>>>(geo, tb, a, d_srcpts[d], ns, dip,
+                                                               d_srcbuf[d]);
+        nlaunch++;
+      }
+      dim3 grid, block;
+      launch_dims(a.box, grid, block);
+      e_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+      nlaunch++;
+      if (ns) {
+        src_post_kernel<R><<<(ns + 127) / 128, 128, 0, stream>>>(geo, a, d_srcpts[d], ns, d_srcbuf[d]);
+        nlaunch++;
+      }
+    }
+  }
+
+  void step_current(Plan &p, int ft, const DipoleVals &cur) {
+    for (int d = 0; d < 3; d++) {
+      int c = comp(ft, d);
+      if (!ncur[c]) continue;
+      src_current_kernel<R><<<(ncur[c] + 127) / 128, 128, 0, stream>>>(f[c], cndinv[c], d_cur[c],
+                                                                       ncur[c], cur, p.dt);
+      nlaunch++;
+    }
+  }
+
+  void dft(Plan &p, int id, double time) {
+    const Monitor &m = p.monitors[id];
+    DMon &dm = mons[id];
+    int nf = (int)m.freq.size();
+    dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(),
+                                                            m.scale.imag(), dm.ph);
+    nlaunch++;
+    DftArgs<R> a{};
+    a.f = f[m.c];
+    a.fb = nullptr;
+    if (ctype(m.c) == MFD_H) {
+      int d = cdir(m.c);
+      a.hdir = d;
+      a.hshift = p.shift[m.c][d];
+      a.fb = f[comp(MFD_B, d)];
+      if (!p.pml_dir[d]) a.f = a.fb;
+    }
+    for (int d = 0; d < 3; d++) {
+      a.w[d] = dm.w[d];
+      a.lo[d] = m.lo[d];
+      a.n[d] = m.hi[d] - m.lo[d] + 1;
+    }
+    a.dV = m.dV;
+    a.include_weights = m.include_weights;
+    a.dim = p.g.dim;
+    a.ad0 = a.ad1 = -1;
+    if (m.centered)
+      for (int d = 0; d < 3; d++)
+        if (p.present[d] && p.shift[m.c][d] == 0) {
+          if (a.ad0 >= 0) a.ad1 = d;
+          else a.ad0 = d;
+        }
+    a.acc = dm.acc;
+    a.ph = dm.ph;
+    a.nf = nf;
+    a.npts = (long long)m.npts;
+    long long total = a.npts * nf;
+    int bs = 256;
+    long long nb = (total + bs - 1) / bs;
+    dft_kernel<R><<<(unsigned)nb, bs, 0, stream>>>(geo, a);
+    nlaunch++;
+  }
+
+  void step(Plan &p, int64_t t, const std::vector<SrcStepValues> &vals) override {
+    DipoleVals curb{}, curd{}, dip{};
+    for (size_t k = 0; k < vals.size() && k < 16; k++) {
+      curb.re[k] = vals[k].cur_b.real();
+      curb.im[k] = vals[k].cur_b.imag();
+      curd.re[k] = vals[k].cur_d.real();
+      curd.im[k] = vals[k].cur_d.imag();
+      dip.re[k] = vals[k].dip_e.real();
+      dip.im[k] = vals[k].dip_e.imag();
+    }
+    for (int d = 0; d < 3; d++)
+      if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
+    step_current(p, MFD_B, curb);
+    for (int d = 0; d < 3; d++)
+      if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
+    for (int d = 0; d < 3; d++)
+      if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
+    step_current(p, MFD_D, curd);
+    update_e(p, dip);
+    int64_t tn = t + 1;
+    for (size_t id = 0; id < p.monitors.size(); id++) {
+      const Monitor &m = p.monitors[id];
+      if (tn % m.decimation != 0) continue;
+      double timeE = tn * p.dt;
+      double time = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? timeE - 0.5 * p.dt : timeE;
+      dft(p, (int)id, time);
+    }
+  }
+
+  void begin_steps() override {
+    cuda_check(cudaEventRecord(ev0, stream), "event record");
+  }
+  void end_steps() override {
+    cuda_check(cudaEventRecord(ev1, stream), "event record");
+    cuda_check(cudaEventSynchronize(ev1), "event sync");
+    float fms = 0;
+    cuda_check(cudaEventElapsedTime(&fms, ev0, ev1), "elapsed");
+    ms = fms;
+    cuda_check(cudaGetLastError(), "kernel launch");
+  }
+  double last_step_ms() const override { return ms; }
+  long long launches() const override { return nlaunch; }
+  void synchronize() override { cuda_check(cudaStreamSynchronize(stream), "sync"); }
+
+  void get_field(Plan &p, int c, double *out) override {
+    std::vector<R> h(p.nstore), hb;
+    cuda_check(cudaMemcpyAsync(h.data(), f[c], p.nstore * sizeof(R), cudaMemcpyDeviceToHost, stream),
+               "download");
+    int t = ctype(c), d = cdir(c);
+    bool sepH = t == MFD_H;
+    if (sepH) {
+      hb.resize(p.nstore);
+      cuda_check(cudaMemcpyAsync(hb.data(), f[comp(MFD_B, d)], p.nstore * sizeof(R),
+                                 cudaMemcpyDeviceToHost, stream),
+                 "download");
+    }
+    cuda_check(cudaStreamSynchronize(stream), "download sync");
+    for (int64_t di = 0; di < p.ndense; di++) {
+      int k[3];
+      p.dense_coords(di, k);
+      int64_t i = k[0] * p.stride[0] + k[1] * p.stride[1] + k[2] * p.stride[2];
+      if (sepH && !(p.pml_dir[d] && p.in_slab(d, p.shift[c][d] + 2 * k[d]))) out[di] = double(hb[i]);
+      else out[di] = double(h[i]);
+    }
+  }
+
+  void get_dft(Plan &p, int id, double *out) override {
+    const Monitor &m = p.monitors[id];
+    size_t n = m.npts * m.freq.size();
+    cuda_check(cudaMemcpyAsync(out, mons[id].acc, n * sizeof(double2), cudaMemcpyDeviceToHost, stream),
+               "download dft");
+    cuda_check(cudaStreamSynchronize(stream), "download sync");
+  }
+
+  void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) override {
+    size_t nf = p.monitors[idE[0]].freq.size();
+    if (flux_cap < nf) {
+      d_flux = dalloc<double>(nf);
+      flux_cap = nf;
+    }
+    double *d_out = d_flux;
+    cuda_check(cudaMemsetAsync(d_out, 0, nf * sizeof(double), stream), "memset");
+    for (int q = 0; q < npairs; q++) {
+      flux_kernel<<<(unsigned)nf, 256, 0, stream>>>(mons[idE[q]].acc, mons[idH[q]].acc,
+                                                     (long long)p.monitors[idE[q]].npts, (int)nf, d_out);
+      nlaunch++;
+    }
+    cuda_check(cudaMemcpyAsync(out, d_out, nf * sizeof(double), cudaMemcpyDeviceToHost, stream),
+               "download flux");
+    cuda_check(cudaStreamSynchronize(stream), "flux sync");
+  }
+};
+
+} // namespace cuda_impl
+} // namespace mfd

@@ -17,6 +17,8 @@
  * the same structure. */
 #include <meep.hpp>
 
+#include "cases.hpp"
+
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -125,245 +127,63 @@ static std::vector<double> dump_dft_chunks(dft_chunk *chunks, component c, const
   return out;
 }
 
-/* --------------------------------------------------------------- geometry */
-struct Cyl {
-  double x, y, r;
-};
-struct Box {
-  double lo[3], hi[3];
-  double eps[3]; // diagonal entries (equal unless anisotropic)
-};
+/* ------------------------------------------------------------------ cases */
+using namespace workloads;
 
-class case_material : public material_function {
-public:
-  int dim = 2;
-  double eps_bg = 1.0;
-  std::vector<Cyl> cyls;
-  double cyl_eps = 12.0;
-  std::vector<Box> boxes;
-  // dispersive / conductive layers split at z = split_z (3-D) or y (2-D)
-  bool layered = false;
-  double split = 0.0;
-  double sigma_lower = 0.0; // susceptibility strength below the split
-  double cond_upper = 0.0;  // D conductivity above the split
-
-  double coord_split(const vec &r) const { return dim == 3 ? r.z() : r.y(); }
-
-  void eps_diag(const vec &r, double e[3]) const {
-    e[0] = e[1] = e[2] = eps_bg;
-    for (const Cyl &c : cyls) {
-      double dx = r.x() - c.x, dy = r.y() - c.y;
-      if (dx * dx + dy * dy < c.r * c.r) e[0] = e[1] = e[2] = cyl_eps;
-    }
-    for (const Box &b : boxes) {
-      bool in = true;
-      for (int d = 0; d < dim; d++) {
-        double v = d == 0 ? r.x() : (d == 1 ? r.y() : r.z());
-        if (!(v > b.lo[d] && v < b.hi[d])) in = false;
-      }
-      if (in) {
-        e[0] = b.eps[0];
-        e[1] = b.eps[1];
-        e[2] = b.eps[2];
-      }
-    }
-  }
-  virtual double chi1p1(field_type ft, const vec &r) {
-    if (ft == H_stuff) return 1.0;
-    double e[3];
-    eps_diag(r, e);
-    return e[0];
-  }
-  virtual void eff_chi1inv_row(component c, double row[3], const volume &v, double tol,
-                               int maxeval) {
-    (void)tol;
-    (void)maxeval;
-    row[0] = row[1] = row[2] = 0.0;
-    double e[3];
-    if (type(c) == H_stuff) {
-      row[component_direction(c) % 3] = 1.0;
-      return;
-    }
-    eps_diag(v.center(), e);
-    row[component_direction(c) % 3] = 1.0 / e[component_direction(c) % 3];
-  }
-  virtual bool has_conductivity(component c) { return cond_upper != 0.0 && is_D(c); }
-  virtual double conductivity(component c, const vec &r) {
-    (void)c;
-    return coord_split(r) > split ? cond_upper : 0.0;
-  }
-  virtual void sigma_row(component c, double row[3], const vec &r) {
-    row[0] = row[1] = row[2] = 0.0;
-    row[component_direction(c) % 3] = coord_split(r) < split ? sigma_lower : 0.0;
-  }
-};
-
-/* A sigma function that is `scale` below the split and 0 above, for one pole. */
-class pole_sigma : public material_function {
-public:
-  int dim;
-  double split, scale;
-  pole_sigma(int d, double s, double k) : dim(d), split(s), scale(k) {}
-  virtual void sigma_row(component c, double row[3], const vec &r) {
-    row[0] = row[1] = row[2] = 0.0;
-    double v = dim == 3 ? r.z() : r.y();
-    row[component_direction(c) % 3] = v < split ? scale : 0.0;
-  }
-};
-
-static std::vector<double> linspace(double a, double b, int n) {
-  std::vector<double> v(n);
-  for (int i = 0; i < n; i++)
-    v[i] = n > 1 ? a + (b - a) * i / (n - 1) : a;
-  return v;
+static void run_steps(Workload &wl, int steps) {
+  for (int i = 0; i < steps; i++)
+    wl.f->step();
+  sync_dfts(*wl.f);
 }
 
-/* ------------------------------------------------------------------ cases */
+static void write_flux(Writer &w, Workload &wl) {
+  double *F = wl.flux->flux();
+  w.rec("flux", std::vector<double>(F, F + wl.nfreq));
+  delete[] F;
+}
 
-/* 2-D TM (Ez, Hx, Hy): cylinders of eps=12 in air, PML on all sides, Gaussian
-   Ez point source at the centre, x-normal flux line.  The full-size variant is
-   512x512 cells at resolution 16 with 40 cylinders, 4000 steps, a 400-cell
-   flux line at 51 frequencies. */
 static void case_tm2d(Writer &w, int ncells_x, int ncells_y, double res, double dpml, int ncyl,
                       uint64_t seed, int steps, int flux_cells, int nfreq, bool dump_fields,
                       int decimation) {
-  double sx = ncells_x / res, sy = ncells_y / res;
-  grid_volume gv = vol2d(sx, sy, res);
-  gv.center_origin();
-  case_material mat;
-  mat.dim = 2;
-  std::mt19937_64 rng(seed);
-  std::uniform_real_distribution<double> ux(-sx / 2 + dpml, sx / 2 - dpml);
-  std::uniform_real_distribution<double> uy(-sy / 2 + dpml, sy / 2 - dpml);
-  std::uniform_real_distribution<double> ur(0.5, 2.0);
-  for (int i = 0; i < ncyl; i++) {
-    Cyl c;
-    c.x = ux(rng);
-    c.y = uy(rng);
-    c.r = ur(rng) * (res >= 16 ? 1.0 : 0.25);
-    mat.cyls.push_back(c);
-  }
-  structure s(gv, mat, pml(dpml), identity(), 0, 0.5, false);
-  fields f(&s);
-  f.use_real_fields();
-  double fcen = 0.15, df = 0.1;
-  gaussian_src_time src(fcen, df);
-  f.add_point_source(Ez, src, vec(0.0, 0.0));
-  double xf = 0.25 * sx;
-  double half = 0.5 * flux_cells / res;
-  volume fv(vec(xf, -half), vec(xf, half));
-  dft_flux fl = f.add_dft_flux(X, fv, fcen - df / 2, fcen + df / 2, nfreq, true, true, decimation);
-  for (int i = 0; i < steps; i++)
-    f.step();
-  sync_dfts(f);
-  double *F = fl.flux();
-  w.rec("flux", std::vector<double>(F, F + nfreq));
-  delete[] F;
-  w.scalar("t", f.time());
+  auto wl = make_tm2d(ncells_x, ncells_y, res, dpml, ncyl, seed, flux_cells, nfreq, decimation);
+  run_steps(*wl, steps);
+  write_flux(w, *wl);
+  w.scalar("t", wl->f->time());
   if (dump_fields) {
-    w.rec("Ez", global_field(f, gv, Ez));
-    w.rec("Hx", global_field(f, gv, Hx));
-    w.rec("Hy", global_field(f, gv, Hy));
-    w.rec("dft_Ez", dump_dft_chunks(fl.E, Ez, gv));
-    w.rec("dft_Hy", dump_dft_chunks(fl.H, Hy, gv));
+    w.rec("Ez", global_field(*wl->f, wl->gv, Ez));
+    w.rec("Hx", global_field(*wl->f, wl->gv, Hx));
+    w.rec("Hy", global_field(*wl->f, wl->gv, Hy));
+    w.rec("dft_Ez", dump_dft_chunks(wl->flux->E, Ez, wl->gv));
+    w.rec("dft_Hy", dump_dft_chunks(wl->flux->H, Hy, wl->gv));
   }
 }
 
-/* 3-D full-vector, non-dispersive: boxes of eps in {2.1, 4, 12}, 20% of them
-   diagonally anisotropic, PML on all faces, Gaussian Ex dipole, z-normal flux
-   plane. */
 static void case_vec3d(Writer &w, int nx, int ny, int nz, double res, double dpml, int nbox,
                        uint64_t seed, int steps, int flux_cells, int nfreq, bool dump_fields) {
-  double sx = nx / res, sy = ny / res, sz = nz / res;
-  grid_volume gv = vol3d(sx, sy, sz, res);
-  gv.center_origin();
-  case_material mat;
-  mat.dim = 3;
-  std::mt19937_64 rng(seed);
-  std::uniform_real_distribution<double> u01(0.0, 1.0);
-  const double choices[3] = {2.1, 4.0, 12.0};
-  double L[3] = {sx, sy, sz};
-  for (int i = 0; i < nbox; i++) {
-    Box b;
-    for (int d = 0; d < 3; d++) {
-      double lo = -L[d] / 2 + dpml, hi = L[d] / 2 - dpml;
-      double c = lo + (hi - lo) * u01(rng);
-      double h = (0.05 + 0.2 * u01(rng)) * (hi - lo);
-      b.lo[d] = c - h;
-      b.hi[d] = c + h;
-    }
-    double e = choices[std::min(2, int(3 * u01(rng)))];
-    b.eps[0] = b.eps[1] = b.eps[2] = e;
-    if (u01(rng) < 0.2)
-      for (int d = 0; d < 3; d++)
-        b.eps[d] = 2.0 + 10.0 * u01(rng);
-    mat.boxes.push_back(b);
-  }
-  structure s(gv, mat, pml(dpml), identity(), 0, 0.5, false);
-  fields f(&s);
-  f.use_real_fields();
-  double fcen = 0.2, df = 0.2;
-  gaussian_src_time src(fcen, df);
-  f.add_point_source(Ex, src, vec(0.1 / res, -0.3 / res, -0.25 * sz));
-  double half = 0.5 * flux_cells / res;
-  volume fv(vec(-half, -half, 0.25 * sz), vec(half, half, 0.25 * sz));
-  dft_flux fl = f.add_dft_flux(Z, fv, fcen - df / 2, fcen + df / 2, nfreq);
-  for (int i = 0; i < steps; i++)
-    f.step();
-  sync_dfts(f);
-  double *F = fl.flux();
-  w.rec("flux", std::vector<double>(F, F + nfreq));
-  delete[] F;
-  w.scalar("t", f.time());
+  auto wl = make_vec3d(nx, ny, nz, res, dpml, nbox, seed, flux_cells, nfreq);
+  run_steps(*wl, steps);
+  write_flux(w, *wl);
+  w.scalar("t", wl->f->time());
   if (dump_fields) {
     const component cs[6] = {Ex, Ey, Ez, Hx, Hy, Hz};
     const char *names[6] = {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"};
     for (int i = 0; i < 6; i++)
-      w.rec(names[i], global_field(f, gv, cs[i]));
-    w.rec("dft_Ex", dump_dft_chunks(fl.E, Ex, gv));
-    w.rec("dft_Hy", dump_dft_chunks(fl.H, Hy, gv));
+      w.rec(names[i], global_field(*wl->f, wl->gv, cs[i]));
+    w.rec("dft_Ex", dump_dft_chunks(wl->flux->E, Ex, wl->gv));
+    w.rec("dft_Hy", dump_dft_chunks(wl->flux->H, Hy, wl->gv));
   }
 }
 
-/* 3-D dispersive: lower half (z < 0) is a Drude pole (omega 1e-5, gamma 0.05,
-   sigma 50) plus a Lorentz pole (omega 0.8, gamma 0.1, sigma 2); the upper half
-   has D conductivity 0.01.  A line of Gaussian Ez sources along x; DFT fields
-   of Ez on a full xy plane. */
 static void case_disp3d(Writer &w, int nx, int ny, int nz, double res, double dpml, int steps,
                         int nfreq, bool dump_fields, int decimation) {
-  double sx = nx / res, sy = ny / res, sz = nz / res;
-  grid_volume gv = vol3d(sx, sy, sz, res);
-  gv.center_origin();
-  case_material mat;
-  mat.dim = 3;
-  mat.layered = true;
-  mat.split = 0.0;
-  mat.cond_upper = 0.01;
-  structure s(gv, mat, pml(dpml), identity(), 0, 0.5, false);
-  pole_sigma drude(3, 0.0, 50.0), lorentz(3, 0.0, 2.0);
-  s.add_susceptibility(drude, E_stuff, lorentzian_susceptibility(1e-5, 0.05, true));
-  s.add_susceptibility(lorentz, E_stuff, lorentzian_susceptibility(0.8, 0.1, false));
-  fields f(&s);
-  f.use_real_fields();
-  double fcen = 0.5, df = 0.6;
-  gaussian_src_time src(fcen, df);
-  double zs = 0.25 * sz;
-  f.add_volume_source(Ez, src, volume(vec(-0.5 * sx + dpml, 0.0, zs), vec(0.5 * sx - dpml, 0.0, zs)),
-                      complex<double>(1.0, 0.0));
-  component cz = Ez;
-  double zm = -0.125 * sz;
-  volume plane(vec(-0.5 * sx, -0.5 * sy, zm), vec(0.5 * sx, 0.5 * sy, zm));
-  std::vector<double> freqs = linspace(fcen - df / 2, fcen + df / 2, nfreq);
-  dft_fields dfld = f.add_dft_fields(&cz, 1, plane, freqs.data(), freqs.size(), true, decimation);
-  for (int i = 0; i < steps; i++)
-    f.step();
-  sync_dfts(f);
-  w.scalar("t", f.time());
-  w.rec("dft_Ez", dump_dft_chunks(dfld.chunks, Ez, gv));
+  auto wl = make_disp3d(nx, ny, nz, res, dpml, nfreq, decimation);
+  run_steps(*wl, steps);
+  w.scalar("t", wl->f->time());
+  w.rec("dft_Ez", dump_dft_chunks(wl->dftf->chunks, Ez, wl->gv));
   if (dump_fields) {
-    w.rec("Ex", global_field(f, gv, Ex));
-    w.rec("Ez", global_field(f, gv, Ez));
-    w.rec("Hy", global_field(f, gv, Hy));
+    w.rec("Ex", global_field(*wl->f, wl->gv, Ex));
+    w.rec("Ez", global_field(*wl->f, wl->gv, Ez));
+    w.rec("Hy", global_field(*wl->f, wl->gv, Hy));
   }
 }
 

@@ -1,0 +1,139 @@
+"""Shared helpers for the tests: run the golden driver builds, compare records,
+and build seeded random problems for the C ABI."""
+import os
+import subprocess
+
+import numpy as np
+
+from meep_gb300 import _lib
+from records import read_records
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+ORACLE_DRIVER = {64: os.path.join(ROOT, "oracle", "_build", "golden_driver64"),
+                 32: os.path.join(ROOT, "oracle", "_build", "golden_driver32")}
+GPU_DRIVER = {64: os.path.join(ROOT, "meep_gb300", "lib", "golden_driver64"),
+              32: os.path.join(ROOT, "meep_gb300", "lib", "golden_driver32")}
+
+
+def golden(case, prec="f64"):
+    return read_records(os.path.join(GOLDEN, "%s.%s.bin" % (case, prec)))
+
+
+def run_driver(exe, case, tmpdir, steps=None, threads=8):
+    out = os.path.join(str(tmpdir), "%s.%s.bin" % (case, os.path.basename(exe)))
+    cmd = [exe, case, out] + ([str(steps)] if steps else [])
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    subprocess.run(cmd, check=True, env=env, timeout=1800)
+    return read_records(out)
+
+
+def relerr(a, b):
+    """max |a - b| / max |b| (infinity-norm relative error, as the reference's
+    ApproxComparisonTestCase.assertClose does, python/tests/utils.py:10-29)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    m = np.abs(b).max()
+    return float(np.abs(a - b).max() / m) if m > 0 else float(np.abs(a - b).max())
+
+
+DFT_LAYOUT = {"tm2d_small": (2, 11), "tm2d_small_dec1": (2, 11), "vec3d_small": (3, 9),
+              "disp3d_small": (3, 7)}
+
+
+def split_dft(rec, case):
+    """A dft_* record holds, per point, its ivec coordinates then (re, im) per
+    frequency; return (coords, complex values[npts, nfreq])."""
+    dim, nf = DFT_LAYOUT[case]
+    arr = np.asarray(rec).reshape(-1, dim + 2 * nf)
+    return arr[:, :dim], arr[:, dim::2] + 1j * arr[:, dim + 1::2]
+
+
+def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
+    """Per-record relative errors, DFT records split into coordinates (must be
+    equal) and values."""
+    errs = {}
+    for k, v in ref.items():
+        if k in skip:
+            continue
+        assert k in out, k
+        if k.startswith("dft_"):
+            c0, v0 = split_dft(v, case)
+            c1, v1 = split_dft(out[k], case)
+            assert np.array_equal(c0, c1), (case, k, "coordinates differ")
+            m = np.abs(v0).max()
+            errs[k] = float(np.abs(v1 - v0).max() / m) if m else float(np.abs(v1 - v0).max())
+        else:
+            errs[k] = relerr(out[k], v)
+    return errs
+
+
+def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
+                   nsrc=3, steps=60):
+    """Build the same seeded random problem on one engine and return outputs.
+
+    Random inverse permittivities, conductivities and Lorentz/Drude sigma
+    arrays on a small grid with PML; integrated E sources at random points and
+    a current source; two DFT monitors.  Returns dict of field arrays and DFT
+    sums after `steps` steps."""
+    rng = np.random.default_rng(seed)
+    if dim == 2:
+        n = (int(rng.integers(28, 40)), int(rng.integers(24, 36)), 0)
+        comps = [_lib.comp(_lib.E, _lib.Z), _lib.comp(_lib.D, _lib.Z), _lib.comp(_lib.H, _lib.X),
+                 _lib.comp(_lib.B, _lib.X), _lib.comp(_lib.H, _lib.Y), _lib.comp(_lib.B, _lib.Y)]
+    else:
+        n = (int(rng.integers(18, 24)), int(rng.integers(16, 22)), int(rng.integers(14, 20)))
+        comps = [_lib.comp(t, d) for t in range(4) for d in range(3)]
+    io = [-(n[d] - n[d] % 2) for d in range(3)]
+    a = 10.0
+    pmlspec = {}
+    if pml:
+        for d in range(dim if dim == 3 else 2):
+            for side in (0, 1):
+                pmlspec[(d, side)] = (float(rng.choice([0.3, 0.5])), 1e-15, 1.0)
+    sim = sim_factory(dim=dim, n=n, io=io, a=a, courant=0.5, pml=pmlspec, precision=precision,
+                      components=comps)
+    ext = sim.ext
+    shape = tuple(ext)
+    for c in comps:
+        if c // 3 == _lib.E:
+            sim.set_chi1inv(c, c % 3, 1.0 / rng.uniform(1.0, 12.0, size=shape))
+    if cond:
+        for c in comps:
+            if c // 3 == _lib.D:
+                arr = np.where(rng.uniform(size=shape) < 0.3, rng.uniform(0, 0.5, size=shape), 0.0)
+                sim.set_conductivity(c, arr)
+    if poles:
+        for (w0, g, dr) in ((1e-5, 0.05, True), (0.8, 0.1, False)):
+            sig = []
+            for d in range(3):
+                c = _lib.comp(_lib.E, d)
+                sig.append(rng.uniform(0, 2.0, size=shape) if c in comps else None)
+            sim.add_lorentzian(w0, g, dr, sig)
+    ecomps = [c for c in comps if c // 3 == _lib.E]
+    s_int = sim.add_gaussian_src(0.6, 2.0, integrated=True)
+    s_cur = sim.add_gaussian_src(0.5, 1.5, integrated=False)
+    ndense = int(np.prod(shape))
+    for j in range(nsrc):
+        c = ecomps[j % len(ecomps)]
+        idx = rng.choice(ndense, size=4, replace=False)
+        amp = rng.normal(size=4) + 1j * rng.normal(size=4)
+        sim.add_source_points(c, s_int if j else s_cur, idx, amp)
+    # an H current source
+    hc = [c for c in comps if c // 3 == _lib.H][0]
+    sim.add_source_points(hc, s_cur, rng.choice(ndense, size=3, replace=False), rng.normal(size=3))
+    mons = []
+    for c in (ecomps[0], [c for c in comps if c // 3 == _lib.H][-1]):
+        lo = [1 if ext[d] > 1 else 0 for d in range(3)]
+        hi = [ext[d] - 3 if ext[d] > 1 else 0 for d in range(3)]
+        w = [rng.uniform(0.2, 1.0, size=hi[d] - lo[d] + 1) if ext[d] > 1 else None for d in range(3)]
+        mons.append(sim.add_dft(c, lo, hi, w, dV=0.01, include_weights=True, scale=0.3 - 0.2j,
+                                centered=True, freqs=np.linspace(0.3, 0.9, 5), decimation=2))
+    sim.step(steps)
+    out = {"c%d" % c: sim.get_field(c) for c in comps}
+    for m in mons:
+        out["dft%d" % m] = sim.get_dft(m)
+    out["flux"] = sim.flux([mons[0]], [mons[1]], 5)
+    sim.close()
+    return out
