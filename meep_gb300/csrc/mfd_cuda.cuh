@@ -306,6 +306,12 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
   e_store(g, a, pts[j].k, pts[j].i, in[j]);
 }
 
+} // namespace cuda_impl
+} // namespace mfd
+#include "mfd_fused.cuh"
+namespace mfd {
+namespace cuda_impl {
+
 // current (non-integrated) sources on D or B: f -= Re(amp*J*dt*condinv)
 struct CurPoint {
   long long i;
@@ -463,6 +469,7 @@ public:
   SrcPoint *d_srcpts[3] = {};
   int nsrcpts[3] = {};
   EPoint<R> *d_srcbuf[3] = {};
+  DEOut<R> *d_fsrcbuf[3] = {};
   CurPoint *d_cur[NC] = {};
   int ncur[NC] = {};
   // monitors
@@ -472,6 +479,8 @@ public:
     double *w[3] = {};
   };
   std::vector<DMon> mons;
+  int fused_mask = -1; // component mask of an available fused kernel set, -1 none
+  bool has_b_current = false;
   long long nlaunch = 0;
   double *d_flux = nullptr;
   size_t flux_cap = 0;
@@ -587,7 +596,137 @@ public:
       poles.push_back(dp);
     }
     setup_sources(p);
+    int mask = 0;
+    for (int c = 0; c < NC; c++)
+      if (p.have[c]) mask |= 1 << c;
+    if ((p.g.dim == 3 && mask == MASK3) || (p.g.dim == 2 && (mask == MASK_TM || mask == MASK_TE)) ||
+        (p.g.dim == 1 && mask == MASK_1D))
+      fused_mask = mask;
+    for (int d = 0; d < 3; d++)
+      has_b_current = has_b_current || ncur[comp(MFD_B, d)] > 0;
+    if (getenv("MFD_GENERIC_KERNELS")) fused_mask = -1;
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
+  }
+
+  static constexpr int MASK3 = 0xFFF;
+  static constexpr int MASK_TM = (1 << 2) | (1 << 3) | (1 << 4) | (1 << 8) | (1 << 9) | (1 << 10);
+  static constexpr int MASK_TE = (1 << 0) | (1 << 1) | (1 << 5) | (1 << 6) | (1 << 7) | (1 << 11);
+  static constexpr int MASK_1D = (1 << 0) | (1 << 4) | (1 << 6) | (1 << 10);
+
+  FusedArgs<R> fused_args(const Plan &p, bool fuse_h) {
+    FusedArgs<R> a;
+    std::memset(&a, 0, sizeof(a));
+    for (int d = 0; d < 3; d++) {
+      a.e[d] = f[comp(MFD_E, d)];
+      a.d[d] = f[comp(MFD_D, d)];
+      a.b[d] = f[comp(MFD_B, d)];
+      a.h[d] = f[comp(MFD_H, d)];
+      for (int t = 2; t < 4; t++) {
+        int c = comp(t, d);
+        a.fu[t][d] = fu[c];
+        a.fcnd[t][d] = fcnd[c];
+        a.cnd[t][d] = cnd[c];
+        a.cndinv[t][d] = cndinv[c];
+        unsigned m = 0;
+        if (!p.cond_chunk[c].empty())
+          for (int r = 0; r < 27; r++)
+            if (p.cond_chunk[c][r]) m |= 1u << r;
+        a.cond_chunks[t][d] = m;
+      }
+      a.fw[0][d] = fw[comp(MFD_E, d)];
+      a.fw[1][d] = fw[comp(MFD_H, d)];
+      a.chi[d] = chi[comp(MFD_E, d)];
+      a.N[d] = p.N[d];
+      a.T[d][0] = p.T[d][0];
+      a.T[d][1] = p.T[d][1];
+      a.pml[d] = p.pml_dir[d];
+      a.s[d] = p.stride[d];
+      a.sig[d] = tb.sig[d];
+      a.kap[d] = tb.kap[d];
+      a.siginv[d] = tb.siginv[d];
+    }
+    a.npoles = (int)poles.size();
+    for (int q = 0; q < a.npoles; q++) {
+      for (int d = 0; d < 3; d++) {
+        a.P[q][d] = poles[q].P[d];
+        a.PP[q][d] = poles[q].PP[d];
+        a.ps[q][d] = poles[q].s[d];
+      }
+      a.pg1inv[q] = poles[q].gamma1inv;
+      a.pg1[q] = poles[q].gamma1;
+      a.pw0[q] = poles[q].w0;
+      a.pw0d[q] = poles[q].w0d;
+    }
+    a.dtdx = R(p.g.courant);
+    a.dt2 = R(p.dt) * R(0.5);
+    a.fuse_h = fuse_h;
+    return a;
+  }
+
+  void fused_dims(const Plan &p, dim3 &grid, dim3 &block) const {
+    if (p.g.dim == 3) {
+      block = dim3(32, 8, 1);
+      grid = dim3((p.N[2] + 31) / 32, (p.N[1] + 7) / 8, p.N[0]);
+    }
+    else if (p.g.dim == 2) {
+      block = dim3(32, 8, 1);
+      grid = dim3((p.N[1] + 31) / 32, (p.N[0] + 7) / 8, 1);
+    }
+    else {
+      block = dim3(256, 1, 1);
+      grid = dim3((p.N[2] + 255) / 256, 1, 1);
+    }
+  }
+
+  template <int DIM, int MASK>
+  void fused_step_t(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
+    FusedArgs<R> a = fused_args(p, !has_b_current);
+    dim3 grid, block;
+    fused_dims(p, grid, block);
+    fused_b_kernel<R, DIM, MASK><<<grid, block, 0, stream>>>(a);
+    nlaunch++;
+    if (has_b_current) {
+      step_current(p, MFD_B, curb);
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
+    }
+    bool dcur = false;
+    for (int d = 0; d < 3; d++)
+      dcur = dcur || ncur[comp(MFD_D, d)] > 0;
+    if (dcur) {
+      // current sources on D act between the curl and the E update: run the
+      // generic D curl, the current kernel, then the fused kernel's E part is
+      // not usable; fall back to the generic D/E sequence
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
+      step_current(p, MFD_D, curd);
+      update_e(p, dip);
+      return;
+    }
+    for (int d = 0; d < 3; d++)
+      if (nsrcpts[d]) {
+        fused_src_pre_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(
+            a, d_srcpts[d], nsrcpts[d], d, dip, d_fsrcbuf[d]);
+        nlaunch++;
+      }
+    fused_de_kernel<R, DIM, MASK><<<grid, block, 0, stream>>>(a);
+    nlaunch++;
+    for (int d = 0; d < 3; d++)
+      if (nsrcpts[d]) {
+        fused_src_post_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(
+            a, d_srcpts[d], nsrcpts[d], d, d_fsrcbuf[d]);
+        nlaunch++;
+      }
+  }
+
+  void fused_step(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
+    switch (fused_mask) {
+      case MASK3: fused_step_t<3, MASK3>(p, curb, curd, dip); break;
+      case MASK_TM: fused_step_t<2, MASK_TM>(p, curb, curd, dip); break;
+      case MASK_TE: fused_step_t<2, MASK_TE>(p, curb, curd, dip); break;
+      case MASK_1D: fused_step_t<1, MASK_1D>(p, curb, curd, dip); break;
+      default: throw Error("no fused kernel for this component set");
+    }
   }
 
   void setup_sources(Plan &p) {
@@ -629,6 +768,7 @@ public:
       if (!keep.empty()) {
         d_srcpts[d] = dupload(keep);
         d_srcbuf[d] = dalloc<EPoint<R>>(keep.size());
+        d_fsrcbuf[d] = dalloc<DEOut<R>>(keep.size());
       }
     }
     // current sources (non-integrated) on D or B
@@ -865,15 +1005,18 @@ public:
       dip.re[k] = vals[k].dip_e.real();
       dip.im[k] = vals[k].dip_e.imag();
     }
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
-    step_current(p, MFD_B, curb);
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
-    step_current(p, MFD_D, curd);
-    update_e(p, dip);
+    if (fused_mask >= 0) fused_step(p, curb, curd, dip);
+    else {
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
+      step_current(p, MFD_B, curb);
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
+      step_current(p, MFD_D, curd);
+      update_e(p, dip);
+    }
     int64_t tn = t + 1;
     for (size_t id = 0; id < p.monitors.size(); id++) {
       const Monitor &m = p.monitors[id];

@@ -1,0 +1,389 @@
+// Fused half-step kernels: one launch advances every component of one field
+// type (B with its PML H copy, then D with E and the polarisations) over the
+// whole cell.  Component wiring (which E/H component and stride enter each
+// curl, Yee shifts, PML directions) is resolved at compile time from the grid
+// dimension and the allocated-component mask, so each thread runs straight-line
+// code; blocks that lie entirely in the interior chunk take a branch-free path
+// with no PML loads at all.  Arithmetic per point is the same sequence as the
+// generic kernels in mfd_cuda.cuh (reference: step_curl, step_update_EDHB,
+// lorentzian update_P), so results are identical to them.
+#pragma once
+
+namespace mfd {
+namespace cuda_impl {
+
+template <int DIM> __host__ __device__ constexpr bool dpresent(int d) {
+  return DIM == 3 || (DIM == 2 && d < 2) || (DIM == 1 && d == 2);
+}
+__host__ __device__ constexpr bool has_comp(int mask, int t, int d) { return (mask >> (3 * t + d)) & 1; }
+// Yee shift of a component of type t, direction dc, along d
+template <int DIM> __host__ __device__ constexpr int yshift(int t, int dc, int d) {
+  return dpresent<DIM>(d) ? (((t == 0 || t == 2) && d == dc) || ((t == 1 || t == 3) && d != dc) ? 1 : 0) : 0;
+}
+
+template <typename R> struct FusedArgs {
+  R *e[3], *d[3], *b[3], *h[3];
+  R *fu[4][3];   // [type D=2 / B=3][dir] (index by type)
+  R *fw[2][3];   // [type E=0 / H=1][dir]
+  R *fcnd[4][3];
+  const R *chi[3];
+  const R *cnd[4][3], *cndinv[4][3];
+  unsigned cond_chunks[4][3];
+  int npoles;
+  R *P[MAX_POLES][3], *PP[MAX_POLES][3];
+  const R *ps[MAX_POLES][3];
+  R pg1inv[MAX_POLES], pg1[MAX_POLES], pw0[MAX_POLES], pw0d[MAX_POLES];
+  R dtdx, dt2;
+  int N[3], T[3][2], pml[3];
+  long long s[3];
+  const R *sig[3], *kap[3], *siginv[3]; // PML tables by half-pixel position
+  bool fuse_h;   // update H in the PML slab right after B
+  __device__ __forceinline__ R tbs(int d, int p) const { return sig[d][p]; }
+  __device__ __forceinline__ R tbk(int d, int p) const { return kap[d][p]; }
+  __device__ __forceinline__ R tbsi(int d, int p) const { return siginv[d][p]; }
+};
+
+template <typename R> __device__ __forceinline__ bool fslab(const FusedArgs<R> &a, int d, int pos) {
+  return a.pml[d] && ((a.T[d][0] > 0 && pos <= 2 * a.T[d][0]) ||
+                      (a.T[d][1] > 0 && pos > 2 * (a.N[d] - a.T[d][1])));
+}
+template <typename R> __device__ __forceinline__ int fregion(const FusedArgs<R> &a, int d, int pos) {
+  if (a.T[d][0] > 0 && pos <= 2 * a.T[d][0]) return 0;
+  if (a.T[d][1] > 0 && pos > 2 * (a.N[d] - a.T[d][1])) return 2;
+  return 1;
+}
+
+// thread -> point; axis mapping: fast = last present direction
+template <int DIM> __device__ __forceinline__ void fused_coords(int k[3]) {
+  if (DIM == 3) {
+    k[2] = blockIdx.x * blockDim.x + threadIdx.x;
+    k[1] = blockIdx.y * blockDim.y + threadIdx.y;
+    k[0] = blockIdx.z;
+  }
+  else if (DIM == 2) {
+    k[1] = blockIdx.x * blockDim.x + threadIdx.x;
+    k[0] = blockIdx.y * blockDim.y + threadIdx.y;
+    k[2] = 0;
+  }
+  else {
+    k[2] = blockIdx.x * blockDim.x + threadIdx.x;
+    k[0] = k[1] = 0;
+  }
+}
+
+// block entirely inside the interior chunk along every PML direction: all
+// positions 2k..2k+1 of the block satisfy 2T_lo < pos <= 2(N - T_hi)
+template <typename R, int DIM> __device__ __forceinline__ bool block_interior(const FusedArgs<R> &a) {
+  int lo[3], hi[3];
+  if (DIM == 3) {
+    lo[2] = blockIdx.x * blockDim.x;
+    hi[2] = lo[2] + blockDim.x - 1;
+    lo[1] = blockIdx.y * blockDim.y;
+    hi[1] = lo[1] + blockDim.y - 1;
+    lo[0] = hi[0] = blockIdx.z;
+  }
+  else if (DIM == 2) {
+    lo[1] = blockIdx.x * blockDim.x;
+    hi[1] = lo[1] + blockDim.x - 1;
+    lo[0] = blockIdx.y * blockDim.y;
+    hi[0] = lo[0] + blockDim.y - 1;
+    lo[2] = hi[2] = 0;
+  }
+  else {
+    lo[2] = blockIdx.x * blockDim.x;
+    hi[2] = lo[2] + blockDim.x - 1;
+    lo[0] = hi[0] = lo[1] = hi[1] = 0;
+  }
+  bool in = true;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (a.pml[d]) in = in && lo[d] >= a.T[d][0] + 1 && hi[d] <= a.N[d] - a.T[d][1] - 1;
+  return in;
+}
+
+template <typename R, int DIM, int T, int DC>
+__device__ __forceinline__ bool comp_in_range(const FusedArgs<R> &a, const int k[3]) {
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (dpresent<DIM>(d)) {
+      const int lo = yshift<DIM>(T, DC, d) ? 0 : 1;
+      ok = ok && k[d] >= lo && k[d] <= a.N[d] - 1;
+    }
+  return ok;
+}
+
+// Curl update of component (T = D or B, direction DC) at point i: the new
+// field value and the new auxiliaries (f_u, f_cond), nothing stored.
+template <typename R> struct CurlOut {
+  R f, fu, fc;
+  bool wfu, wfc;
+};
+
+template <typename R, int DIM, int MASK, int T, int DC>
+__device__ __forceinline__ CurlOut<R> curl_point(const FusedArgs<R> &a, const int k[3], long long i,
+                                                 bool interior) {
+  constexpr int SRC = (T == 3) ? 0 : 1; // B <- E, D <- H
+  constexpr int PD = (DC + 2) % 3, PDER = (DC + 1) % 3, MD = (DC + 1) % 3, MDER = (DC + 2) % 3;
+  constexpr bool HP = dpresent<DIM>(PDER) && has_comp(MASK, SRC, PD);
+  constexpr bool HM = dpresent<DIM>(MDER) && has_comp(MASK, SRC, MD);
+  constexpr int G1D = HP ? PD : MD, G1DER = HP ? PDER : MDER;
+  constexpr bool TWO = HP && HM;
+  constexpr bool FLIP = !HP;
+  CurlOut<R> o;
+  o.wfu = o.wfc = false;
+  R *F = (T == 3) ? a.b[DC] : a.d[DC];
+  const R fold = F[i];
+  o.fu = o.fc = R(0);
+  if (!HP && !HM) { // component without curl terms (not instantiated in practice)
+    o.f = fold;
+    return o;
+  }
+  const long long sg = (T == 3) ? 1 : -1;
+  const long long s1 = sg * a.s[G1DER];
+  const long long s2 = TWO ? sg * a.s[MDER] : 0;
+  const R *G1, *G2 = nullptr;
+  if (T == 3) {
+    G1 = a.e[G1D];
+    if (TWO) G2 = a.e[MD];
+  }
+  else {
+    // H is a separate array only inside the PML slab along its own direction
+    G1 = (!interior && fslab(a, G1D, 2 * k[G1D])) ? a.h[G1D] : a.b[G1D];
+    if (TWO) G2 = (!interior && fslab(a, MD, 2 * k[MD])) ? a.h[MD] : a.b[MD];
+  }
+  R X = G1[i + s1] - G1[i];
+  if (TWO) X = X + G2[i] - G2[i + s2];
+  const R dtdx = FLIP ? -a.dtdx : a.dtdx;
+  const R *cnd = a.cnd[T][DC];
+  const R one = R(1);
+  if (interior) {
+    o.f = cnd ? ((one - a.dt2 * cnd[i]) * fold - dtdx * X) * a.cndinv[T][DC][i] : fold - dtdx * X;
+    return o;
+  }
+  constexpr int DS = (DC + 1) % 3, DU = (DC + 2) % 3;
+  const int ps = yshift<DIM>(T, DC, DS) + 2 * k[DS];
+  const int pu = yshift<DIM>(T, DC, DU) + 2 * k[DU];
+  const bool sgm = dpresent<DIM>(DS) && fslab(a, DS, ps);
+  const bool su = dpresent<DIM>(DU) && fslab(a, DU, pu);
+  bool hc = cnd != nullptr;
+  if (sgm && hc) {
+    int r = fregion(a, 0, yshift<DIM>(T, DC, 0) + 2 * k[0]) * 9 +
+            fregion(a, 1, yshift<DIM>(T, DC, 1) + 2 * k[1]) * 3 + fregion(a, 2, yshift<DIM>(T, DC, 2) + 2 * k[2]);
+    hc = (a.cond_chunks[T][DC] >> r) & 1u;
+  }
+  if (!sgm) {
+    if (!su) {
+      o.f = hc ? ((one - a.dt2 * cnd[i]) * fold - dtdx * X) * a.cndinv[T][DC][i] : fold - dtdx * X;
+      return o;
+    }
+    R fprev = a.fu[T][DC][i];
+    R fun = hc ? ((one - a.dt2 * cnd[i]) * fprev - dtdx * X) * a.cndinv[T][DC][i] : fprev - dtdx * X;
+    o.fu = fun;
+    o.wfu = true;
+    o.f = a.tbsi(DU, pu) * ((a.tbk(DU, pu) - a.tbs(DU, pu)) * fold + fun - fprev);
+    return o;
+  }
+  const R ks = a.tbk(DS, ps) - a.tbs(DS, ps), si = a.tbsi(DS, ps);
+  if (!su) {
+    if (hc) {
+      R fcp = a.fcnd[T][DC][i];
+      R fcn = ((one - a.dt2 * cnd[i]) * fcp - dtdx * X) * a.cndinv[T][DC][i];
+      o.fc = fcn;
+      o.wfc = true;
+      o.f = (ks * fold + (fcn - fcp)) * si;
+    }
+    else
+      o.f = (ks * fold - dtdx * X) * si;
+    return o;
+  }
+  R fprev = a.fu[T][DC][i];
+  R fun;
+  if (hc) {
+    R fcp = a.fcnd[T][DC][i];
+    R fcn = ((one - a.dt2 * cnd[i]) * fcp - dtdx * X) * a.cndinv[T][DC][i];
+    o.fc = fcn;
+    o.wfc = true;
+    fun = (ks * fprev + (fcn - fcp)) * si;
+  }
+  else
+    fun = (ks * fprev - dtdx * X) * si;
+  o.fu = fun;
+  o.wfu = true;
+  o.f = a.tbsi(DU, pu) * ((a.tbk(DU, pu) - a.tbs(DU, pu)) * fold + fun - fprev);
+  return o;
+}
+
+template <typename R, int T, int DC>
+__device__ __forceinline__ void curl_store_aux(const FusedArgs<R> &a, long long i, const CurlOut<R> &o) {
+  if (o.wfu) a.fu[T][DC][i] = o.fu;
+  if (o.wfc) a.fcnd[T][DC][i] = o.fc;
+}
+
+// ------------------------------------------------------------ B (+ H) kernel
+template <typename R, int DIM, int MASK, int DC>
+__device__ __forceinline__ void b_comp(const FusedArgs<R> &a, const int k[3], long long i, bool interior) {
+  if constexpr (has_comp(MASK, 3, DC)) {
+  if (!comp_in_range<R, DIM, 3, DC>(a, k)) return;
+  const CurlOut<R> co = curl_point<R, DIM, MASK, 3, DC>(a, k, i, interior);
+  curl_store_aux<R, 3, DC>(a, i, co);
+  const R bn = co.f;
+  a.b[DC][i] = bn;
+  // H = B through the PML f_w ODE inside the slab along DC (update_eh for H,
+  // src/step_generic.cpp:692-698 with u == NULL)
+  if (a.fuse_h && !interior && dpresent<DIM>(DC)) {
+    const int kw = 2 * k[DC];
+    if (fslab(a, DC, kw)) {
+      R *fw = a.fw[1][DC];
+      R fwprev = fw[i], kapwkw = a.tbk(DC, kw), sigwkw = a.tbs(DC, kw);
+      fw[i] = bn;
+      a.h[DC][i] += (kapwkw + sigwkw) * bn - (kapwkw - sigwkw) * fwprev;
+    }
+  }
+  }
+}
+
+template <typename R, int DIM, int MASK>
+__global__ void __launch_bounds__(256) fused_b_kernel(FusedArgs<R> a) {
+  int k[3];
+  fused_coords<DIM>(k);
+  if ((dpresent<DIM>(0) && k[0] >= a.N[0]) || (dpresent<DIM>(1) && k[1] >= a.N[1]) ||
+      (dpresent<DIM>(2) && k[2] >= a.N[2]))
+    return;
+  const bool interior = block_interior<R, DIM>(a);
+  const long long i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
+  b_comp<R, DIM, MASK, 0>(a, k, i, interior);
+  b_comp<R, DIM, MASK, 1>(a, k, i, interior);
+  b_comp<R, DIM, MASK, 2>(a, k, i, interior);
+}
+
+// --------------------------------------------------- D, E and poles kernel
+template <typename R> struct DEOut {
+  CurlOut<R> c;
+  R d, e, fw;
+  R p[MAX_POLES], pp[MAX_POLES];
+};
+
+// New D, E (f_w) and polarisations of component DC at point i, nothing stored
+// except the D-curl auxiliaries.  srcA: integrated source terms subtracted from
+// D - P (update_eh f_minus_p, src/update_eh.cpp:108-137).
+template <typename R, int DIM, int MASK, int DC>
+__device__ __forceinline__ void de_point(const FusedArgs<R> &a, const int k[3], long long i, bool interior,
+                                         int nsrc, const R *srcA, DEOut<R> &o) {
+  o.c = curl_point<R, DIM, MASK, 2, DC>(a, k, i, interior);
+  o.d = o.c.f;
+  R gs = o.d;
+#pragma unroll
+  for (int q = 0; q < MAX_POLES; q++)
+    if (q < a.npoles && a.P[q][DC]) gs -= a.P[q][DC][i];
+  for (int j = 0; j < nsrc; j++)
+    gs -= srcA[j];
+  const R us = a.chi[DC][i];
+  R W;
+  const int kw = 2 * k[DC] + yshift<DIM>(0, DC, DC);
+  if (!interior && dpresent<DIM>(DC) && fslab(a, DC, kw)) {
+    R fwprev = a.fw[0][DC][i], kapwkw = a.tbk(DC, kw), sigwkw = a.tbs(DC, kw);
+    R fwn = (gs * us);
+    o.fw = fwn;
+    o.e = a.e[DC][i] + ((kapwkw + sigwkw) * fwn - (kapwkw - sigwkw) * fwprev);
+    W = fwn;
+  }
+  else {
+    o.e = (gs * us);
+    o.fw = R(0);
+    W = o.e;
+  }
+#pragma unroll
+  for (int q = 0; q < MAX_POLES; q++)
+    if (q < a.npoles && a.P[q][DC]) {
+      R pcur = a.P[q][DC][i];
+      o.p[q] = a.pg1inv[q] * (pcur * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][DC][i] + a.pw0[q] * (a.ps[q][DC][i] * W));
+      o.pp[q] = pcur;
+    }
+}
+
+template <typename R, int DIM, int DC>
+__device__ __forceinline__ void de_store(const FusedArgs<R> &a, const int k[3], long long i, bool interior,
+                                         const DEOut<R> &o) {
+  curl_store_aux<R, 2, DC>(a, i, o.c);
+  a.d[DC][i] = o.d;
+  a.e[DC][i] = o.e;
+  const int kw = 2 * k[DC] + yshift<DIM>(0, DC, DC);
+  if (!interior && dpresent<DIM>(DC) && fslab(a, DC, kw)) a.fw[0][DC][i] = o.fw;
+#pragma unroll
+  for (int q = 0; q < MAX_POLES; q++)
+    if (q < a.npoles && a.P[q][DC]) {
+      a.P[q][DC][i] = o.p[q];
+      a.PP[q][DC][i] = o.pp[q];
+    }
+}
+
+template <typename R, int DIM, int MASK, int DC>
+__device__ __forceinline__ void de_comp(const FusedArgs<R> &a, const int k[3], long long i, bool interior) {
+  if constexpr (has_comp(MASK, 2, DC)) {
+    if (!comp_in_range<R, DIM, 2, DC>(a, k)) return;
+    DEOut<R> o;
+    de_point<R, DIM, MASK, DC>(a, k, i, interior, 0, (const R *)nullptr, o);
+    de_store<R, DIM, DC>(a, k, i, interior, o);
+  }
+}
+
+template <typename R, int DIM, int MASK>
+__global__ void __launch_bounds__(256) fused_de_kernel(FusedArgs<R> a) {
+  int k[3];
+  fused_coords<DIM>(k);
+  if ((dpresent<DIM>(0) && k[0] >= a.N[0]) || (dpresent<DIM>(1) && k[1] >= a.N[1]) ||
+      (dpresent<DIM>(2) && k[2] >= a.N[2]))
+    return;
+  const bool interior = block_interior<R, DIM>(a);
+  const long long i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
+  de_comp<R, DIM, MASK, 0>(a, k, i, interior);
+  de_comp<R, DIM, MASK, 1>(a, k, i, interior);
+  de_comp<R, DIM, MASK, 2>(a, k, i, interior);
+}
+
+// Integrated E sources: the new D/E/P of each source point, computed from the
+// state before the fused D/E kernel (pre) and written after it (post).
+template <typename R, int DIM, int MASK>
+__global__ void fused_src_pre_kernel(FusedArgs<R> a, const SrcPoint *pts, int n, int dc, DipoleVals dv,
+                                     DEOut<R> *out) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const SrcPoint &sp = pts[j];
+  R A[MAXS];
+  for (int t = 0; t < sp.nterm; t++) {
+    double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
+    A[t] = R(re);
+  }
+  int k[3] = {sp.k[0], sp.k[1], sp.k[2]};
+  // the general (non-interior) path gives identical values in the interior
+  if (dc == 0) {
+    if constexpr (has_comp(MASK, 2, 0)) de_point<R, DIM, MASK, 0>(a, k, sp.i, false, sp.nterm, A, out[j]);
+  }
+  else if (dc == 1) {
+    if constexpr (has_comp(MASK, 2, 1)) de_point<R, DIM, MASK, 1>(a, k, sp.i, false, sp.nterm, A, out[j]);
+  }
+  else {
+    if constexpr (has_comp(MASK, 2, 2)) de_point<R, DIM, MASK, 2>(a, k, sp.i, false, sp.nterm, A, out[j]);
+  }
+}
+
+template <typename R, int DIM, int MASK>
+__global__ void fused_src_post_kernel(FusedArgs<R> a, const SrcPoint *pts, int n, int dc, const DEOut<R> *in) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const SrcPoint &sp = pts[j];
+  int k[3] = {sp.k[0], sp.k[1], sp.k[2]};
+  if (dc == 0) {
+    if constexpr (has_comp(MASK, 2, 0)) de_store<R, DIM, 0>(a, k, sp.i, false, in[j]);
+  }
+  else if (dc == 1) {
+    if constexpr (has_comp(MASK, 2, 1)) de_store<R, DIM, 1>(a, k, sp.i, false, in[j]);
+  }
+  else {
+    if constexpr (has_comp(MASK, 2, 2)) de_store<R, DIM, 2>(a, k, sp.i, false, in[j]);
+  }
+}
+
+} // namespace cuda_impl
+} // namespace mfd
