@@ -605,6 +605,7 @@ public:
     for (int d = 0; d < 3; d++)
       has_b_current = has_b_current || ncur[comp(MFD_B, d)] > 0;
     if (getenv("MFD_GENERIC_KERNELS")) fused_mask = -1;
+    if (fused_mask >= 0) plan_boxes(p);
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
   }
 
@@ -640,7 +641,7 @@ public:
       a.T[d][0] = p.T[d][0];
       a.T[d][1] = p.T[d][1];
       a.pml[d] = p.pml_dir[d];
-      a.s[d] = p.stride[d];
+      a.s[d] = (int)p.stride[d];
       a.sig[d] = tb.sig[d];
       a.kap[d] = tb.kap[d];
       a.siginv[d] = tb.siginv[d];
@@ -663,28 +664,80 @@ public:
     return a;
   }
 
-  void fused_dims(const Plan &p, dim3 &grid, dim3 &block) const {
-    if (p.g.dim == 3) {
-      block = dim3(32, 8, 1);
-      grid = dim3((p.N[2] + 31) / 32, (p.N[1] + 7) / 8, p.N[0]);
+  // Interior box (no PML slab, no wall point for any component) and the boxes
+  // around it, in point indices 0..N-1 per present direction.
+  BoxList box_int{}, box_bnd{};
+  dim3 fblock{32, 8, 1};
+
+  static void add_box(BoxList &L, const int lo[3], const int hi[3], int dim, dim3 blk) {
+    int ext[3];
+    for (int d = 0; d < 3; d++) {
+      ext[d] = hi[d] - lo[d] + 1;
+      if (ext[d] <= 0) return;
     }
-    else if (p.g.dim == 2) {
-      block = dim3(32, 8, 1);
-      grid = dim3((p.N[1] + 31) / 32, (p.N[0] + 7) / 8, 1);
+    const int FA = dim == 2 ? 1 : 2, MA = dim == 2 ? 0 : (dim == 3 ? 1 : 0), SA = dim == 3 ? 0 : (dim == 2 ? 2 : 1);
+    int q = L.n++;
+    for (int d = 0; d < 3; d++) {
+      L.lo[q][d] = lo[d];
+      L.ext[q][d] = ext[d];
     }
-    else {
-      block = dim3(256, 1, 1);
-      grid = dim3((p.N[2] + 255) / 256, 1, 1);
+    L.bx[q] = (ext[FA] + blk.x - 1) / blk.x;
+    L.by[q] = (ext[MA] + blk.y - 1) / blk.y;
+    L.blk0[q + 1] = L.blk0[q] + L.bx[q] * L.by[q] * ext[SA];
+  }
+
+  void plan_boxes(const Plan &p) {
+    if (p.nstore >= (1LL << 31)) throw Error("grid too large for 32-bit indexing");
+    const int dim = p.g.dim;
+    fblock = dim == 1 ? dim3(256, 1, 1) : dim3(32, 8, 1);
+    int glo[3], ghi[3], ilo[3], ihi[3];
+    for (int d = 0; d < 3; d++) {
+      if (!p.present[d]) {
+        glo[d] = ghi[d] = ilo[d] = ihi[d] = 0;
+        continue;
+      }
+      glo[d] = 0;
+      ghi[d] = p.N[d] - 1;
+      ilo[d] = p.T[d][0] + 1;
+      ihi[d] = p.N[d] - p.T[d][1] - 1;
+      if (ihi[d] < ilo[d]) ihi[d] = ilo[d] - 1; // empty interior
+    }
+    box_int = BoxList{};
+    box_bnd = BoxList{};
+    add_box(box_int, ilo, ihi, dim, fblock);
+    // shell around the interior: slabs peeled off direction by direction
+    int lo[3], hi[3], clo[3], chi_[3];
+    for (int d = 0; d < 3; d++) {
+      clo[d] = glo[d];
+      chi_[d] = ghi[d];
+    }
+    for (int d = 0; d < 3; d++) {
+      if (!p.present[d]) continue;
+      for (int q = 0; q < 3; q++) {
+        lo[q] = clo[q];
+        hi[q] = chi_[q];
+      }
+      hi[d] = ilo[d] - 1;
+      add_box(box_bnd, lo, hi, dim, fblock);
+      lo[d] = ihi[d] + 1;
+      hi[d] = chi_[d];
+      add_box(box_bnd, lo, hi, dim, fblock);
+      clo[d] = ilo[d];
+      chi_[d] = ihi[d];
     }
   }
 
   template <int DIM, int MASK>
   void fused_step_t(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
     FusedArgs<R> a = fused_args(p, !has_b_current);
-    dim3 grid, block;
-    fused_dims(p, grid, block);
-    fused_b_kernel<R, DIM, MASK><<<grid, block, 0, stream>>>(a);
-    nlaunch++;
+    if (box_int.n) {
+      fused_b_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
+      nlaunch++;
+    }
+    if (box_bnd.n) {
+      fused_b_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
+      nlaunch++;
+    }
     if (has_b_current) {
       step_current(p, MFD_B, curb);
       for (int d = 0; d < 3; d++)
@@ -709,8 +762,14 @@ public:
             a, d_srcpts[d], nsrcpts[d], d, dip, d_fsrcbuf[d]);
         nlaunch++;
       }
-    fused_de_kernel<R, DIM, MASK><<<grid, block, 0, stream>>>(a);
-    nlaunch++;
+    if (box_int.n) {
+      fused_de_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
+      nlaunch++;
+    }
+    if (box_bnd.n) {
+      fused_de_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
+      nlaunch++;
+    }
     for (int d = 0; d < 3; d++)
       if (nsrcpts[d]) {
         fused_src_post_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(

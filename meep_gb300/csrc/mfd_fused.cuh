@@ -35,7 +35,7 @@ template <typename R> struct FusedArgs {
   R pg1inv[MAX_POLES], pg1[MAX_POLES], pw0[MAX_POLES], pw0d[MAX_POLES];
   R dtdx, dt2;
   int N[3], T[3][2], pml[3];
-  long long s[3];
+  int s[3];
   const R *sig[3], *kap[3], *siginv[3]; // PML tables by half-pixel position
   bool fuse_h;   // update H in the PML slab right after B
   __device__ __forceinline__ R tbs(int d, int p) const { return sig[d][p]; }
@@ -51,54 +51,6 @@ template <typename R> __device__ __forceinline__ int fregion(const FusedArgs<R> 
   if (a.T[d][0] > 0 && pos <= 2 * a.T[d][0]) return 0;
   if (a.T[d][1] > 0 && pos > 2 * (a.N[d] - a.T[d][1])) return 2;
   return 1;
-}
-
-// thread -> point; axis mapping: fast = last present direction
-template <int DIM> __device__ __forceinline__ void fused_coords(int k[3]) {
-  if (DIM == 3) {
-    k[2] = blockIdx.x * blockDim.x + threadIdx.x;
-    k[1] = blockIdx.y * blockDim.y + threadIdx.y;
-    k[0] = blockIdx.z;
-  }
-  else if (DIM == 2) {
-    k[1] = blockIdx.x * blockDim.x + threadIdx.x;
-    k[0] = blockIdx.y * blockDim.y + threadIdx.y;
-    k[2] = 0;
-  }
-  else {
-    k[2] = blockIdx.x * blockDim.x + threadIdx.x;
-    k[0] = k[1] = 0;
-  }
-}
-
-// block entirely inside the interior chunk along every PML direction: all
-// positions 2k..2k+1 of the block satisfy 2T_lo < pos <= 2(N - T_hi)
-template <typename R, int DIM> __device__ __forceinline__ bool block_interior(const FusedArgs<R> &a) {
-  int lo[3], hi[3];
-  if (DIM == 3) {
-    lo[2] = blockIdx.x * blockDim.x;
-    hi[2] = lo[2] + blockDim.x - 1;
-    lo[1] = blockIdx.y * blockDim.y;
-    hi[1] = lo[1] + blockDim.y - 1;
-    lo[0] = hi[0] = blockIdx.z;
-  }
-  else if (DIM == 2) {
-    lo[1] = blockIdx.x * blockDim.x;
-    hi[1] = lo[1] + blockDim.x - 1;
-    lo[0] = blockIdx.y * blockDim.y;
-    hi[0] = lo[0] + blockDim.y - 1;
-    lo[2] = hi[2] = 0;
-  }
-  else {
-    lo[2] = blockIdx.x * blockDim.x;
-    hi[2] = lo[2] + blockDim.x - 1;
-    lo[0] = hi[0] = lo[1] = hi[1] = 0;
-  }
-  bool in = true;
-#pragma unroll
-  for (int d = 0; d < 3; d++)
-    if (a.pml[d]) in = in && lo[d] >= a.T[d][0] + 1 && hi[d] <= a.N[d] - a.T[d][1] - 1;
-  return in;
 }
 
 template <typename R, int DIM, int T, int DC>
@@ -121,7 +73,7 @@ template <typename R> struct CurlOut {
 };
 
 template <typename R, int DIM, int MASK, int T, int DC>
-__device__ __forceinline__ CurlOut<R> curl_point(const FusedArgs<R> &a, const int k[3], long long i,
+__device__ __forceinline__ CurlOut<R> curl_point(const FusedArgs<R> &a, const int k[3], int i,
                                                  bool interior) {
   constexpr int SRC = (T == 3) ? 0 : 1; // B <- E, D <- H
   constexpr int PD = (DC + 2) % 3, PDER = (DC + 1) % 3, MD = (DC + 1) % 3, MDER = (DC + 2) % 3;
@@ -139,9 +91,8 @@ __device__ __forceinline__ CurlOut<R> curl_point(const FusedArgs<R> &a, const in
     o.f = fold;
     return o;
   }
-  const long long sg = (T == 3) ? 1 : -1;
-  const long long s1 = sg * a.s[G1DER];
-  const long long s2 = TWO ? sg * a.s[MDER] : 0;
+  const int s1 = (T == 3) ? a.s[G1DER] : -a.s[G1DER];
+  const int s2 = TWO ? ((T == 3) ? a.s[MDER] : -a.s[MDER]) : 0;
   const R *G1, *G2 = nullptr;
   if (T == 3) {
     G1 = a.e[G1D];
@@ -215,16 +166,16 @@ __device__ __forceinline__ CurlOut<R> curl_point(const FusedArgs<R> &a, const in
 }
 
 template <typename R, int T, int DC>
-__device__ __forceinline__ void curl_store_aux(const FusedArgs<R> &a, long long i, const CurlOut<R> &o) {
+__device__ __forceinline__ void curl_store_aux(const FusedArgs<R> &a, int i, const CurlOut<R> &o) {
   if (o.wfu) a.fu[T][DC][i] = o.fu;
   if (o.wfc) a.fcnd[T][DC][i] = o.fc;
 }
 
 // ------------------------------------------------------------ B (+ H) kernel
 template <typename R, int DIM, int MASK, int DC>
-__device__ __forceinline__ void b_comp(const FusedArgs<R> &a, const int k[3], long long i, bool interior) {
+__device__ __forceinline__ void b_comp(const FusedArgs<R> &a, const int k[3], int i, bool interior) {
   if constexpr (has_comp(MASK, 3, DC)) {
-  if (!comp_in_range<R, DIM, 3, DC>(a, k)) return;
+  if (!interior && !comp_in_range<R, DIM, 3, DC>(a, k)) return;
   const CurlOut<R> co = curl_point<R, DIM, MASK, 3, DC>(a, k, i, interior);
   curl_store_aux<R, 3, DC>(a, i, co);
   const R bn = co.f;
@@ -243,18 +194,43 @@ __device__ __forceinline__ void b_comp(const FusedArgs<R> &a, const int k[3], lo
   }
 }
 
-template <typename R, int DIM, int MASK>
-__global__ void __launch_bounds__(256) fused_b_kernel(FusedArgs<R> a) {
+// Boxes of points covered by one launch (the interior box, or the PML and
+// wall boxes around it); blocks are assigned to boxes in order.
+struct BoxList {
+  int n;
+  int lo[7][3], ext[7][3];
+  int blk0[8]; // first block of each box; blk0[n] = total
+  int bx[7], by[7]; // blocks along the fast / mid axis of each box
+};
+
+// point of this thread; false if outside its box
+template <int DIM> __device__ __forceinline__ bool box_coords(const BoxList &L, int k[3]) {
+  int b = blockIdx.x, q = 0;
+  while (q + 1 < L.n && b >= L.blk0[q + 1])
+    q++;
+  b -= L.blk0[q];
+  const int FA = DIM == 2 ? 1 : 2, MA = DIM == 2 ? 0 : (DIM == 3 ? 1 : 0), SA = DIM == 3 ? 0 : (DIM == 2 ? 2 : 1);
+  const int bfast = b % L.bx[q];
+  b /= L.bx[q];
+  const int bmid = b % L.by[q];
+  const int bslow = b / L.by[q];
+  const int tf = bfast * blockDim.x + threadIdx.x;
+  const int tm = bmid * blockDim.y + threadIdx.y;
+  if (tf >= L.ext[q][FA] || tm >= L.ext[q][MA]) return false;
+  k[FA] = L.lo[q][FA] + tf;
+  k[MA] = L.lo[q][MA] + tm;
+  k[SA] = L.lo[q][SA] + bslow;
+  return true;
+}
+
+template <typename R, int DIM, int MASK, bool INTERIOR>
+__global__ void __launch_bounds__(256) fused_b_kernel(FusedArgs<R> a, BoxList L) {
   int k[3];
-  fused_coords<DIM>(k);
-  if ((dpresent<DIM>(0) && k[0] >= a.N[0]) || (dpresent<DIM>(1) && k[1] >= a.N[1]) ||
-      (dpresent<DIM>(2) && k[2] >= a.N[2]))
-    return;
-  const bool interior = block_interior<R, DIM>(a);
-  const long long i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
-  b_comp<R, DIM, MASK, 0>(a, k, i, interior);
-  b_comp<R, DIM, MASK, 1>(a, k, i, interior);
-  b_comp<R, DIM, MASK, 2>(a, k, i, interior);
+  if (!box_coords<DIM>(L, k)) return;
+  const int i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
+  b_comp<R, DIM, MASK, 0>(a, k, i, INTERIOR);
+  b_comp<R, DIM, MASK, 1>(a, k, i, INTERIOR);
+  b_comp<R, DIM, MASK, 2>(a, k, i, INTERIOR);
 }
 
 // --------------------------------------------------- D, E and poles kernel
@@ -268,7 +244,7 @@ template <typename R> struct DEOut {
 // except the D-curl auxiliaries.  srcA: integrated source terms subtracted from
 // D - P (update_eh f_minus_p, src/update_eh.cpp:108-137).
 template <typename R, int DIM, int MASK, int DC>
-__device__ __forceinline__ void de_point(const FusedArgs<R> &a, const int k[3], long long i, bool interior,
+__device__ __forceinline__ void de_point(const FusedArgs<R> &a, const int k[3], int i, bool interior,
                                          int nsrc, const R *srcA, DEOut<R> &o) {
   o.c = curl_point<R, DIM, MASK, 2, DC>(a, k, i, interior);
   o.d = o.c.f;
@@ -303,7 +279,7 @@ __device__ __forceinline__ void de_point(const FusedArgs<R> &a, const int k[3], 
 }
 
 template <typename R, int DIM, int DC>
-__device__ __forceinline__ void de_store(const FusedArgs<R> &a, const int k[3], long long i, bool interior,
+__device__ __forceinline__ void de_store(const FusedArgs<R> &a, const int k[3], int i, bool interior,
                                          const DEOut<R> &o) {
   curl_store_aux<R, 2, DC>(a, i, o.c);
   a.d[DC][i] = o.d;
@@ -319,27 +295,23 @@ __device__ __forceinline__ void de_store(const FusedArgs<R> &a, const int k[3], 
 }
 
 template <typename R, int DIM, int MASK, int DC>
-__device__ __forceinline__ void de_comp(const FusedArgs<R> &a, const int k[3], long long i, bool interior) {
+__device__ __forceinline__ void de_comp(const FusedArgs<R> &a, const int k[3], int i, bool interior) {
   if constexpr (has_comp(MASK, 2, DC)) {
-    if (!comp_in_range<R, DIM, 2, DC>(a, k)) return;
+      if (!interior && !comp_in_range<R, DIM, 2, DC>(a, k)) return;
     DEOut<R> o;
     de_point<R, DIM, MASK, DC>(a, k, i, interior, 0, (const R *)nullptr, o);
     de_store<R, DIM, DC>(a, k, i, interior, o);
   }
 }
 
-template <typename R, int DIM, int MASK>
-__global__ void __launch_bounds__(256) fused_de_kernel(FusedArgs<R> a) {
+template <typename R, int DIM, int MASK, bool INTERIOR>
+__global__ void __launch_bounds__(256) fused_de_kernel(FusedArgs<R> a, BoxList L) {
   int k[3];
-  fused_coords<DIM>(k);
-  if ((dpresent<DIM>(0) && k[0] >= a.N[0]) || (dpresent<DIM>(1) && k[1] >= a.N[1]) ||
-      (dpresent<DIM>(2) && k[2] >= a.N[2]))
-    return;
-  const bool interior = block_interior<R, DIM>(a);
-  const long long i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
-  de_comp<R, DIM, MASK, 0>(a, k, i, interior);
-  de_comp<R, DIM, MASK, 1>(a, k, i, interior);
-  de_comp<R, DIM, MASK, 2>(a, k, i, interior);
+  if (!box_coords<DIM>(L, k)) return;
+  const int i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
+  de_comp<R, DIM, MASK, 0>(a, k, i, INTERIOR);
+  de_comp<R, DIM, MASK, 1>(a, k, i, INTERIOR);
+  de_comp<R, DIM, MASK, 2>(a, k, i, INTERIOR);
 }
 
 // Integrated E sources: the new D/E/P of each source point, computed from the
@@ -358,13 +330,13 @@ __global__ void fused_src_pre_kernel(FusedArgs<R> a, const SrcPoint *pts, int n,
   int k[3] = {sp.k[0], sp.k[1], sp.k[2]};
   // the general (non-interior) path gives identical values in the interior
   if (dc == 0) {
-    if constexpr (has_comp(MASK, 2, 0)) de_point<R, DIM, MASK, 0>(a, k, sp.i, false, sp.nterm, A, out[j]);
+    if constexpr (has_comp(MASK, 2, 0)) de_point<R, DIM, MASK, 0>(a, k, (int)sp.i, false, sp.nterm, A, out[j]);
   }
   else if (dc == 1) {
-    if constexpr (has_comp(MASK, 2, 1)) de_point<R, DIM, MASK, 1>(a, k, sp.i, false, sp.nterm, A, out[j]);
+    if constexpr (has_comp(MASK, 2, 1)) de_point<R, DIM, MASK, 1>(a, k, (int)sp.i, false, sp.nterm, A, out[j]);
   }
   else {
-    if constexpr (has_comp(MASK, 2, 2)) de_point<R, DIM, MASK, 2>(a, k, sp.i, false, sp.nterm, A, out[j]);
+    if constexpr (has_comp(MASK, 2, 2)) de_point<R, DIM, MASK, 2>(a, k, (int)sp.i, false, sp.nterm, A, out[j]);
   }
 }
 
@@ -375,13 +347,13 @@ __global__ void fused_src_post_kernel(FusedArgs<R> a, const SrcPoint *pts, int n
   const SrcPoint &sp = pts[j];
   int k[3] = {sp.k[0], sp.k[1], sp.k[2]};
   if (dc == 0) {
-    if constexpr (has_comp(MASK, 2, 0)) de_store<R, DIM, 0>(a, k, sp.i, false, in[j]);
+    if constexpr (has_comp(MASK, 2, 0)) de_store<R, DIM, 0>(a, k, (int)sp.i, false, in[j]);
   }
   else if (dc == 1) {
-    if constexpr (has_comp(MASK, 2, 1)) de_store<R, DIM, 1>(a, k, sp.i, false, in[j]);
+    if constexpr (has_comp(MASK, 2, 1)) de_store<R, DIM, 1>(a, k, (int)sp.i, false, in[j]);
   }
   else {
-    if constexpr (has_comp(MASK, 2, 2)) de_store<R, DIM, 2>(a, k, sp.i, false, in[j]);
+    if constexpr (has_comp(MASK, 2, 2)) de_store<R, DIM, 2>(a, k, (int)sp.i, false, in[j]);
   }
 }
 
