@@ -172,25 +172,43 @@ __device__ __forceinline__ void curl_store_aux(const FusedArgs<R> &a, int i, con
 }
 
 // ------------------------------------------------------------ B (+ H) kernel
+// Results of one B component at one point: new B, its auxiliaries and, in the
+// PML slab along its direction, the new H and f_w (update_eh for H,
+// src/step_generic.cpp:692-698 with u == NULL).
+template <typename R> struct BOut {
+  CurlOut<R> c;
+  bool act, wh;
+  R h, fw;
+};
+
 template <typename R, int DIM, int MASK, int DC>
-__device__ __forceinline__ void b_comp(const FusedArgs<R> &a, const int k[3], int i, bool interior) {
+__device__ __forceinline__ void b_compute(const FusedArgs<R> &a, const int k[3], int i, bool interior,
+                                          BOut<R> &o) {
+  o.act = o.wh = false;
   if constexpr (has_comp(MASK, 3, DC)) {
-  if (!interior && !comp_in_range<R, DIM, 3, DC>(a, k)) return;
-  const CurlOut<R> co = curl_point<R, DIM, MASK, 3, DC>(a, k, i, interior);
-  curl_store_aux<R, 3, DC>(a, i, co);
-  const R bn = co.f;
-  a.b[DC][i] = bn;
-  // H = B through the PML f_w ODE inside the slab along DC (update_eh for H,
-  // src/step_generic.cpp:692-698 with u == NULL)
-  if (a.fuse_h && !interior && dpresent<DIM>(DC)) {
-    const int kw = 2 * k[DC];
-    if (fslab(a, DC, kw)) {
-      R *fw = a.fw[1][DC];
-      R fwprev = fw[i], kapwkw = a.tbk(DC, kw), sigwkw = a.tbs(DC, kw);
-      fw[i] = bn;
-      a.h[DC][i] += (kapwkw + sigwkw) * bn - (kapwkw - sigwkw) * fwprev;
+    if (!interior && !comp_in_range<R, DIM, 3, DC>(a, k)) return;
+    o.act = true;
+    o.c = curl_point<R, DIM, MASK, 3, DC>(a, k, i, interior);
+    if (a.fuse_h && !interior && dpresent<DIM>(DC)) {
+      const int kw = 2 * k[DC];
+      if (fslab(a, DC, kw)) {
+        R fwprev = a.fw[1][DC][i], kapwkw = a.tbk(DC, kw), sigwkw = a.tbs(DC, kw);
+        o.fw = o.c.f;
+        o.h = a.h[DC][i] + ((kapwkw + sigwkw) * o.c.f - (kapwkw - sigwkw) * fwprev);
+        o.wh = true;
+      }
     }
   }
+}
+
+template <typename R, int DC>
+__device__ __forceinline__ void b_store(const FusedArgs<R> &a, int i, const BOut<R> &o) {
+  if (!o.act) return;
+  curl_store_aux<R, 3, DC>(a, i, o.c);
+  a.b[DC][i] = o.c.f;
+  if (o.wh) {
+    a.fw[1][DC][i] = o.fw;
+    a.h[DC][i] = o.h;
   }
 }
 
@@ -228,9 +246,15 @@ __global__ void __launch_bounds__(256) fused_b_kernel(FusedArgs<R> a, BoxList L)
   int k[3];
   if (!box_coords<DIM>(L, k)) return;
   const int i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
-  b_comp<R, DIM, MASK, 0>(a, k, i, INTERIOR);
-  b_comp<R, DIM, MASK, 1>(a, k, i, INTERIOR);
-  b_comp<R, DIM, MASK, 2>(a, k, i, INTERIOR);
+  // all loads and arithmetic first, stores last (no store can then alias a
+  // later load, so the loads of all components are in flight together)
+  BOut<R> o0, o1, o2;
+  b_compute<R, DIM, MASK, 0>(a, k, i, INTERIOR, o0);
+  b_compute<R, DIM, MASK, 1>(a, k, i, INTERIOR, o1);
+  b_compute<R, DIM, MASK, 2>(a, k, i, INTERIOR, o2);
+  b_store<R, 0>(a, i, o0);
+  b_store<R, 1>(a, i, o1);
+  b_store<R, 2>(a, i, o2);
 }
 
 // --------------------------------------------------- D, E and poles kernel
@@ -295,13 +319,14 @@ __device__ __forceinline__ void de_store(const FusedArgs<R> &a, const int k[3], 
 }
 
 template <typename R, int DIM, int MASK, int DC>
-__device__ __forceinline__ void de_comp(const FusedArgs<R> &a, const int k[3], int i, bool interior) {
+__device__ __forceinline__ bool de_compute(const FusedArgs<R> &a, const int k[3], int i, bool interior,
+                                           DEOut<R> &o) {
   if constexpr (has_comp(MASK, 2, DC)) {
-      if (!interior && !comp_in_range<R, DIM, 2, DC>(a, k)) return;
-    DEOut<R> o;
+    if (!interior && !comp_in_range<R, DIM, 2, DC>(a, k)) return false;
     de_point<R, DIM, MASK, DC>(a, k, i, interior, 0, (const R *)nullptr, o);
-    de_store<R, DIM, DC>(a, k, i, interior, o);
+    return true;
   }
+  return false;
 }
 
 template <typename R, int DIM, int MASK, bool INTERIOR>
@@ -309,9 +334,13 @@ __global__ void __launch_bounds__(256) fused_de_kernel(FusedArgs<R> a, BoxList L
   int k[3];
   if (!box_coords<DIM>(L, k)) return;
   const int i = k[0] * a.s[0] + k[1] * a.s[1] + k[2] * a.s[2];
-  de_comp<R, DIM, MASK, 0>(a, k, i, INTERIOR);
-  de_comp<R, DIM, MASK, 1>(a, k, i, INTERIOR);
-  de_comp<R, DIM, MASK, 2>(a, k, i, INTERIOR);
+  DEOut<R> o0, o1, o2;
+  const bool a0 = de_compute<R, DIM, MASK, 0>(a, k, i, INTERIOR, o0);
+  const bool a1 = de_compute<R, DIM, MASK, 1>(a, k, i, INTERIOR, o1);
+  const bool a2 = de_compute<R, DIM, MASK, 2>(a, k, i, INTERIOR, o2);
+  if (a0) de_store<R, DIM, 0>(a, k, i, INTERIOR, o0);
+  if (a1) de_store<R, DIM, 1>(a, k, i, INTERIOR, o1);
+  if (a2) de_store<R, DIM, 2>(a, k, i, INTERIOR, o2);
 }
 
 // Integrated E sources: the new D/E/P of each source point, computed from the
