@@ -309,6 +309,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 } // namespace cuda_impl
 } // namespace mfd
 #include "mfd_fused.cuh"
+#include "mfd_k3d.cuh"
 namespace mfd {
 namespace cuda_impl {
 
@@ -730,7 +731,20 @@ public:
   template <int DIM, int MASK>
   void fused_step_t(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
     FusedArgs<R> a = fused_args(p, !has_b_current);
-    if (box_int.n) {
+    const bool cndB = a.cnd[3][0] || a.cnd[3][1] || a.cnd[3][2];
+    const bool cndD = a.cnd[2][0] || a.cnd[2][1] || a.cnd[2][2];
+    IBox ib{};
+    for (int d = 0; d < 3; d++) {
+      ib.lo[d] = box_int.lo[0][d];
+      ib.n[d] = box_int.ext[0][d];
+    }
+    dim3 igrid((ib.n[2] + 31) / 32, (ib.n[1] + 7) / 8, ib.n[0]);
+    if (box_int.n && DIM == 3) {
+      if (cndB) b3_interior_kernel<R, true><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
+      else b3_interior_kernel<R, false><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
+      nlaunch++;
+    }
+    else if (box_int.n) {
       fused_b_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
       nlaunch++;
     }
@@ -762,7 +776,15 @@ public:
             a, d_srcpts[d], nsrcpts[d], d, dip, d_fsrcbuf[d]);
         nlaunch++;
       }
-    if (box_int.n) {
+    if (box_int.n && DIM == 3) {
+      const bool pl = a.npoles > 0;
+      if (cndD && pl) de3_interior_kernel<R, true, true><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
+      else if (cndD) de3_interior_kernel<R, true, false><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
+      else if (pl) de3_interior_kernel<R, false, true><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
+      else de3_interior_kernel<R, false, false><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
+      nlaunch++;
+    }
+    else if (box_int.n) {
       fused_de_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
       nlaunch++;
     }
