@@ -748,7 +748,11 @@ public:
       fused_b_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
       nlaunch++;
     }
-    if (box_bnd.n) {
+    if (box_bnd.n && DIM == 3) {
+      b3_shell_kernel<R><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
+      nlaunch++;
+    }
+    else if (box_bnd.n) {
       fused_b_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
       nlaunch++;
     }
@@ -788,7 +792,11 @@ public:
       fused_de_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
       nlaunch++;
     }
-    if (box_bnd.n) {
+    if (box_bnd.n && DIM == 3) {
+      de3_shell_kernel<R><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
+      nlaunch++;
+    }
+    else if (box_bnd.n) {
       fused_de_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
       nlaunch++;
     }
