@@ -417,22 +417,27 @@ template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
   a.acc[t] = acc;
 }
 
-// flux: out[w] = sum_k Re(E conj H), one block per frequency, double reduction
+// flux: out[w] += sum_k Re(E conj H).  Threads of a warp take consecutive
+// frequencies of one point (coalesced rows of the [npts][nf] sums); the 8 warps
+// of a block stride over points; partial sums meet in shared memory and one
+// double atomic per block and frequency.
 static __global__ void flux_kernel(const double2 *E, const double2 *H, long long npts, int nf, double *out) {
-  int w = blockIdx.x;
+  const int w = blockIdx.x * 32 + threadIdx.x;
   double s = 0;
-  for (long long k = threadIdx.x; k < npts; k += blockDim.x) {
-    double2 e = E[k * nf + w], h = H[k * nf + w];
-    s += e.x * h.x + e.y * h.y;
-  }
-  __shared__ double red[256];
-  red[threadIdx.x] = s;
+  if (w < nf)
+    for (long long k = blockIdx.y * 8 + threadIdx.y; k < npts; k += 8LL * gridDim.y) {
+      const double2 e = E[k * nf + w], h = H[k * nf + w];
+      s += e.x * h.x + e.y * h.y;
+    }
+  __shared__ double red[8][33];
+  red[threadIdx.y][threadIdx.x] = s;
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
+  if (threadIdx.y == 0 && w < nf) {
+    double t = 0;
+    for (int r = 0; r < 8; r++)
+      t += red[r][threadIdx.x];
+    atomicAdd(out + w, t);
   }
-  if (threadIdx.x == 0) out[w] += red[0];
 }
 
 // ---------------------------------------------------------------- backend
@@ -701,6 +706,12 @@ public:
       ghi[d] = p.N[d] - 1;
       ilo[d] = p.T[d][0] + 1;
       ihi[d] = p.N[d] - p.T[d][1] - 1;
+      if (d == p.fastdir && dim > 1) {
+        // whole warps along the unit-stride axis: interior rows start and end
+        // on multiples of 32 points (the shell takes the remainder)
+        ilo[d] = (ilo[d] + 31) / 32 * 32;
+        ihi[d] = (ihi[d] + 1) / 32 * 32 - 1;
+      }
       if (ihi[d] < ilo[d]) ihi[d] = ilo[d] - 1; // empty interior
     }
     box_int = BoxList{};
@@ -1170,8 +1181,10 @@ public:
     double *d_out = d_flux;
     cuda_check(cudaMemsetAsync(d_out, 0, nf * sizeof(double), stream), "memset");
     for (int q = 0; q < npairs; q++) {
-      flux_kernel<<<(unsigned)nf, 256, 0, stream>>>(mons[idE[q]].acc, mons[idH[q]].acc,
-                                                     (long long)p.monitors[idE[q]].npts, (int)nf, d_out);
+      long long np = (long long)p.monitors[idE[q]].npts;
+      unsigned gy = (unsigned)std::min<long long>(std::max<long long>((np + 255) / 256, 1), 512);
+      flux_kernel<<<dim3((unsigned)((nf + 31) / 32), gy), dim3(32, 8), 0, stream>>>(
+          mons[idE[q]].acc, mons[idH[q]].acc, np, (int)nf, d_out);
       nlaunch++;
     }
     cuda_check(cudaMemcpyAsync(out, d_out, nf * sizeof(double), cudaMemcpyDeviceToHost, stream),

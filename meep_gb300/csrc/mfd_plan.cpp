@@ -105,9 +105,10 @@ Plan::Plan(const mfd_grid &grid) : g(grid) {
       ext[d] = 1;
     }
   }
-  // storage: last present direction fastest, padded to a multiple of 8 points
+  // storage: last present direction fastest, each row padded to a multiple of
+  // 32 points so rows start on 128-byte boundaries (FP32)
   fastdir = g.dim == 2 ? 1 : 2;
-  int64_t pitch = (ext[fastdir] + 7) / 8 * 8;
+  int64_t pitch = (ext[fastdir] + 31) / 32 * 32;
   if (g.dim == 3) {
     stride[2] = 1;
     stride[1] = pitch;
