@@ -706,6 +706,7 @@ public:
       if (ext[d] <= 0) return;
     }
     const int FA = dim == 2 ? 1 : 2, MA = dim == 2 ? 0 : (dim == 3 ? 1 : 0), SA = dim == 3 ? 0 : (dim == 2 ? 2 : 1);
+    if (L.n >= 7) throw Error("internal: too many boxes");
     int q = L.n++;
     for (int d = 0; d < 3; d++) {
       L.lo[q][d] = lo[d];
@@ -736,6 +737,7 @@ public:
         ilo[d] = (ilo[d] + 31) / 32 * 32;
         ihi[d] = (ihi[d] + 1) / 32 * 32 - 1;
       }
+      if (ilo[d] > ghi[d] + 1) ilo[d] = ghi[d] + 1;
       if (ihi[d] < ilo[d]) ihi[d] = ilo[d] - 1; // empty interior
     }
     box_int = BoxList{};
@@ -761,6 +763,12 @@ public:
       clo[d] = ilo[d];
       chi_[d] = ihi[d];
     }
+    // every box must lie inside the point range 0..N-1 of each direction
+    for (const BoxList *L : {&box_int, &box_bnd})
+      for (int q = 0; q < L->n; q++)
+        for (int d = 0; d < 3; d++)
+          if (L->lo[q][d] < glo[d] || L->lo[q][d] + L->ext[q][d] - 1 > ghi[d])
+            throw Error("internal: launch box outside the grid");
   }
 
   template <int DIM, int MASK>
