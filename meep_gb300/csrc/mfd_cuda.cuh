@@ -417,50 +417,48 @@ template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
   a.acc[t] = acc;
 }
 
-// flux: sum_k Re(E conj H) per frequency.  Threads of a warp take consecutive
-// frequencies of one point (coalesced rows of the [npts][nf] sums); the 8 warps
-// of a block stride over points.  Sums are carried as double-double (TwoSum),
-// so the result does not depend on the order of summation; block partials go
-// to a buffer and a second kernel adds them in a fixed order (deterministic).
-struct DD {
-  double hi, lo;
-};
-__device__ __forceinline__ DD dd_add(DD a, double b) {
-  const double s = __dadd_rn(a.hi, b);
-  const double bb = __dsub_rn(s, a.hi);
-  const double err = __dadd_rn(__dsub_rn(a.hi, __dsub_rn(s, bb)), __dsub_rn(b, bb));
-  return DD{s, __dadd_rn(a.lo, err)};
-}
-__device__ __forceinline__ DD dd_add(DD a, DD b) { return dd_add(dd_add(a, b.hi), b.lo); }
-
+// flux: sum_k Re(E conj H) per frequency, in double (FP64 units are scarce on
+// this part, so the reduction is a plain deterministic tree, no compensation).
+// Threads of a warp take consecutive frequencies of one point (coalesced rows
+// of the [npts][nf] sums); the 8 warps of a block stride over points; block
+// partials go to a buffer that a second kernel reduces in a fixed order.
 static __global__ void flux_partial_kernel(const double2 *E, const double2 *H, long long npts, int nf,
-                                           DD *partial) {
+                                           double *partial) {
   const int w = blockIdx.x * 32 + threadIdx.x;
-  DD s{0.0, 0.0};
+  double s = 0.0;
   if (w < nf)
     for (long long k = blockIdx.y * 8 + threadIdx.y; k < npts; k += 8LL * gridDim.y) {
       const double2 e = E[k * nf + w], h = H[k * nf + w];
-      s = dd_add(s, __dmul_rn(e.x, h.x));
-      s = dd_add(s, __dmul_rn(e.y, h.y));
+      s += e.x * h.x + e.y * h.y;
     }
-  __shared__ DD red[8][33];
+  __shared__ double red[8][33];
   red[threadIdx.y][threadIdx.x] = s;
   __syncthreads();
   if (threadIdx.y == 0 && w < nf) {
-    DD t = red[0][threadIdx.x];
+    double t = red[0][threadIdx.x];
     for (int r = 1; r < 8; r++)
-      t = dd_add(t, red[r][threadIdx.x]);
+      t += red[r][threadIdx.x];
     partial[(long long)blockIdx.y * nf + w] = t;
   }
 }
 
-static __global__ void flux_final_kernel(const DD *partial, int nparts, int nf, double *out, int accumulate) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nf) return;
-  DD t{accumulate ? out[w] : 0.0, 0.0};
-  for (int q = 0; q < nparts; q++)
-    t = dd_add(t, partial[(long long)q * nf + w]);
-  out[w] = __dadd_rn(t.hi, t.lo);
+// out[w] (+)= sum over the partials of frequency w: 32 frequencies x 8 lanes
+// per block, tree over the lanes
+static __global__ void flux_final_kernel(const double *partial, int nparts, int nf, double *out, int accumulate) {
+  const int w = blockIdx.x * 32 + threadIdx.x;
+  double s = 0.0;
+  if (w < nf)
+    for (int q = threadIdx.y; q < nparts; q += 8)
+      s += partial[(long long)q * nf + w];
+  __shared__ double red[8][33];
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && w < nf) {
+    double t = red[0][threadIdx.x];
+    for (int r = 1; r < 8; r++)
+      t += red[r][threadIdx.x];
+    out[w] = accumulate ? out[w] + t : t;
+  }
 }
 
 // ---------------------------------------------------------------- backend
@@ -512,7 +510,7 @@ public:
   bool has_b_current = false;
   long long nlaunch = 0;
   double *d_flux = nullptr;
-  DD *d_flux_part = nullptr;
+  double *d_flux_part = nullptr;
   size_t flux_cap = 0;
   double ms = 0;
   bool timing = false;
@@ -1209,17 +1207,17 @@ public:
     const int maxparts = 512;
     if (flux_cap < nf) {
       d_flux = dalloc<double>(nf);
-      d_flux_part = dalloc<DD>((size_t)maxparts * nf);
+      d_flux_part = dalloc<double>((size_t)maxparts * nf);
       flux_cap = nf;
     }
     double *d_out = d_flux;
     for (int q = 0; q < npairs; q++) {
       long long np = (long long)p.monitors[idE[q]].npts;
-      int gy = (int)std::min<long long>(std::max<long long>((np + 255) / 256, 1), maxparts);
+      int gy = (int)std::min<long long>(std::max<long long>((np + 1023) / 1024, 1), maxparts);
       flux_partial_kernel<<<dim3((unsigned)((nf + 31) / 32), (unsigned)gy), dim3(32, 8), 0, stream>>>(
           mons[idE[q]].acc, mons[idH[q]].acc, np, (int)nf, d_flux_part);
-      flux_final_kernel<<<(unsigned)((nf + 127) / 128), 128, 0, stream>>>(d_flux_part, gy, (int)nf, d_out,
-                                                                           q > 0);
+      flux_final_kernel<<<(unsigned)((nf + 31) / 32), dim3(32, 8), 0, stream>>>(d_flux_part, gy, (int)nf, d_out,
+                                                                               q > 0);
       nlaunch += 2;
     }
     cuda_check(cudaMemcpyAsync(out, d_out, nf * sizeof(double), cudaMemcpyDeviceToHost, stream),
