@@ -373,12 +373,9 @@ static __global__ void dft_phase_kernel(const double *freq, int nf, double time,
   ph[w] = make_double2(c * sre - s * sim, c * sim + s * sre);
 }
 
-template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  long long total = a.npts * a.nf;
-  if (t >= total) return;
-  long long p = t / a.nf;
-  int w = int(t - p * a.nf);
+// weighted (and centred) field value of monitor point p (update_dft,
+// src/dft.cpp:275-295): weight product in the reference's loop order
+template <typename R> __device__ __forceinline__ R dft_point_value(const Geo &g, const DftArgs<R> &a, long long p) {
   int q[3];
   q[2] = int(p % a.n[2]);
   long long r = p / a.n[2];
@@ -394,27 +391,97 @@ template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
     else if (a.dim == 3) wgt = wz * (wy * (a.dV * wx));
     else wgt = 1.0 * (1.0 * (a.dV * wz));
   }
-  R fv;
   if (a.ad1 >= 0) {
     int k1[3] = {k[0], k[1], k[2]}, k2[3] = {k[0], k[1], k[2]}, k3[3] = {k[0], k[1], k[2]};
     k1[a.ad0]++;
     k2[a.ad1]++;
     k3[a.ad0]++;
     k3[a.ad1]++;
-    fv = R((wgt * 0.25) * (dft_val(g, a, k) + dft_val(g, a, k1) + dft_val(g, a, k2) + dft_val(g, a, k3)));
+    return R((wgt * 0.25) * (dft_val(g, a, k) + dft_val(g, a, k1) + dft_val(g, a, k2) + dft_val(g, a, k3)));
   }
-  else if (a.ad0 >= 0) {
+  if (a.ad0 >= 0) {
     int k1[3] = {k[0], k[1], k[2]};
     k1[a.ad0]++;
-    fv = R((wgt * 0.5) * (dft_val(g, a, k) + dft_val(g, a, k1)));
+    return R((wgt * 0.5) * (dft_val(g, a, k) + dft_val(g, a, k1)));
   }
-  else
-    fv = R(wgt * dft_val(g, a, k));
+  return R(wgt * dft_val(g, a, k));
+}
+
+// direct accumulation, one thread per (point, frequency): the FP64 path
+template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long total = a.npts * a.nf;
+  if (t >= total) return;
+  long long p = t / a.nf;
+  int w = int(t - p * a.nf);
+  const R fv = dft_point_value(g, a, p);
   double2 ph = a.ph[w];
   double2 acc = a.acc[t];
   acc.x += double(fv) * ph.x;
   acc.y += double(fv) * ph.y;
   a.acc[t] = acc;
+}
+
+// Blocked DFT (FP32 path): each sampled step stores the monitor values in one
+// row of a [T][npts] buffer; every T samples the block is contracted against
+// the [T][2 nfreq] phase matrix (phases generated in FP64 from the exact sample
+// times, so nothing drifts between blocks) with FP32 products and FP32 sums of
+// T terms, and the block result is added to the FP64 running sums.
+constexpr int DFT_BLOCK_T = 64;
+
+template <typename R> __global__ void dft_sample_kernel(Geo g, DftArgs<R> a, float *row) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= a.npts) return;
+  row[p] = float(dft_point_value(g, a, p));
+}
+
+// phase matrix B[t][w] = polar(1, 2 pi f_w time_t) * scale, times of the block's
+// samples time_t = (tn0 + t dec) dt (- dt/2 for H and B)
+static __global__ void dft_block_phase_kernel(const double *freq, int nf, int cnt, long long tn0, int dec,
+                                              double dt, int half, double sre, double sim, float2 *B) {
+  int t = blockIdx.y;
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nf || t >= cnt) return;
+  double timeE = (tn0 + (long long)t * dec) * dt;
+  double time = half ? timeE - 0.5 * dt : timeE;
+  double s, c;
+  sincos(2 * kPi * freq[w] * time, &s, &c);
+  B[(long long)t * nf + w] = make_float2(float(c * sre - s * sim), float(c * sim + s * sre));
+}
+
+static __global__ void __launch_bounds__(128) dft_contract_kernel(const float *A, int cnt, long long npts,
+                                                                   const float2 *B, int nf, double2 *acc) {
+  extern __shared__ float2 sB[]; // [cnt][chunk]
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float a[DFT_BLOCK_T];
+#pragma unroll
+  for (int t = 0; t < DFT_BLOCK_T; t++)
+    a[t] = (t < cnt && p < npts) ? A[(long long)t * npts + p] : 0.0f;
+  const int chunk = 64;
+  for (int w0 = 0; w0 < nf; w0 += chunk) {
+    const int wn = min(chunk, nf - w0);
+    __syncthreads();
+    for (int q = threadIdx.x; q < cnt * wn; q += blockDim.x) {
+      const int t = q / wn, w = q - t * wn;
+      sB[t * chunk + w] = B[(long long)t * nf + w0 + w];
+    }
+    __syncthreads();
+    if (p < npts)
+      for (int w = 0; w < wn; w++) {
+        float sr = 0.f, si = 0.f;
+#pragma unroll
+        for (int t = 0; t < DFT_BLOCK_T; t++)
+          if (t < cnt) {
+            const float2 b = sB[t * chunk + w];
+            sr = fmaf(a[t], b.x, sr);
+            si = fmaf(a[t], b.y, si);
+          }
+        double2 v = acc[p * nf + w0 + w];
+        v.x += double(sr);
+        v.y += double(si);
+        acc[p * nf + w0 + w] = v;
+      }
+  }
 }
 
 // flux: sum_k Re(E conj H) per frequency, in double (FP64 units are scarce on
@@ -504,6 +571,11 @@ public:
     double2 *acc = nullptr, *ph = nullptr;
     double *freq = nullptr;
     double *w[3] = {};
+    bool block = false;      // blocked FP32 contraction
+    float *A = nullptr;      // [DFT_BLOCK_T][npts] samples
+    float2 *B = nullptr;     // [DFT_BLOCK_T][nf] phases
+    int cnt = 0;             // samples in the current block
+    long long tn0 = 0;       // step count of the block's first sample
   };
   std::vector<DMon> mons;
   int fused_mask = -1; // component mask of an available fused kernel set, -1 none
@@ -932,7 +1004,29 @@ public:
     dm.freq = dupload(m.freq);
     for (int d = 0; d < 3; d++)
       if (!m.w[d].empty()) dm.w[d] = dupload(m.w[d]);
+    dm.block = sizeof(R) == 4 && !getenv("MFD_DIRECT_DFT");
+    if (dm.block) {
+      dm.A = dalloc<float>((size_t)DFT_BLOCK_T * m.npts);
+      dm.B = dalloc<float2>((size_t)DFT_BLOCK_T * m.freq.size());
+    }
     cuda_check(cudaStreamSynchronize(stream), "monitor sync");
+  }
+
+  // contract the samples of the current block into the running sums
+  void dft_flush(Plan &p, int id) {
+    const Monitor &m = p.monitors[id];
+    DMon &dm = mons[id];
+    if (!dm.block || dm.cnt == 0) return;
+    const int nf = (int)m.freq.size();
+    const int half = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? 1 : 0;
+    dft_block_phase_kernel<<<dim3((nf + 127) / 128, dm.cnt), 128, 0, stream>>>(
+        dm.freq, nf, dm.cnt, dm.tn0, m.decimation, p.dt, half, m.scale.real(), m.scale.imag(), dm.B);
+    const int chunk = 64; // frequencies per shared-memory pass (<= 32 KB)
+    size_t smem = (size_t)dm.cnt * chunk * sizeof(float2);
+    long long np = (long long)m.npts;
+    dft_contract_kernel<<<(unsigned)((np + 127) / 128), 128, smem, stream>>>(dm.A, dm.cnt, np, dm.B, nf, dm.acc);
+    nlaunch += 2;
+    dm.cnt = 0;
   }
 
   Box full_box(const Plan &p, int c) const {
@@ -1082,13 +1176,10 @@ public:
     }
   }
 
-  void dft(Plan &p, int id, double time) {
+  void dft(Plan &p, int id, double time, int64_t tn) {
     const Monitor &m = p.monitors[id];
     DMon &dm = mons[id];
     int nf = (int)m.freq.size();
-    dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(),
-                                                            m.scale.imag(), dm.ph);
-    nlaunch++;
     DftArgs<R> a{};
     a.f = f[m.c];
     a.fb = nullptr;
@@ -1118,6 +1209,17 @@ public:
     a.ph = dm.ph;
     a.nf = nf;
     a.npts = (long long)m.npts;
+    if (dm.block) {
+      if (dm.cnt == 0) dm.tn0 = tn;
+      dft_sample_kernel<R><<<(unsigned)((a.npts + 255) / 256), 256, 0, stream>>>(geo, a,
+                                                                               dm.A + (size_t)dm.cnt * m.npts);
+      nlaunch++;
+      if (++dm.cnt == DFT_BLOCK_T) dft_flush(p, id);
+      return;
+    }
+    dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(), m.scale.imag(),
+                                                            dm.ph);
+    nlaunch++;
     long long total = a.npts * nf;
     int bs = 256;
     long long nb = (total + bs - 1) / bs;
@@ -1153,7 +1255,7 @@ public:
       if (tn % m.decimation != 0) continue;
       double timeE = tn * p.dt;
       double time = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? timeE - 0.5 * p.dt : timeE;
-      dft(p, (int)id, time);
+      dft(p, (int)id, time, tn);
     }
   }
 
@@ -1195,6 +1297,7 @@ public:
   }
 
   void get_dft(Plan &p, int id, double *out) override {
+    dft_flush(p, id);
     const Monitor &m = p.monitors[id];
     size_t n = m.npts * m.freq.size();
     cuda_check(cudaMemcpyAsync(out, mons[id].acc, n * sizeof(double2), cudaMemcpyDeviceToHost, stream),
@@ -1203,6 +1306,10 @@ public:
   }
 
   void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) override {
+    for (int q = 0; q < npairs; q++) {
+      dft_flush(p, idE[q]);
+      dft_flush(p, idH[q]);
+    }
     size_t nf = p.monitors[idE[0]].freq.size();
     const int maxparts = 512;
     if (flux_cap < nf) {
