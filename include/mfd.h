@@ -125,6 +125,26 @@ int mfd_get_dft(mfd_sim *sim, int id, double *out, size_t *npts, size_t *nfreq);
  * src/dft.cpp:542-556. out has nfreq entries. */
 int mfd_flux(mfd_sim *sim, int npairs, const int *idE, const int *idH, double *out);
 
+/* ---- Differentiation: reverse-time adjoint of the leapfrog update ----
+ * Design = the inverse-permittivity diagonal chi1inv of E components `comps`
+ * over the point box lo..hi (inclusive, component-grid indices).
+ * mfd_forward advances n steps like mfd_step and keeps what the adjoint needs:
+ * with checkpoint_every == 0 it records D at the design points for every step;
+ * with checkpoint_every = K > 0 it stores a full-state checkpoint every K steps
+ * and the backward pass recomputes each segment from its checkpoint (sqrt(T)
+ * memory).  mfd_backward takes dJ/dDFT for the listed monitors (per monitor
+ * npts*nfreq*(re,im) = dJ/dRe F + i dJ/dIm F) and returns dJ/dchi1inv for every
+ * design component and box point (ncomp * npts doubles, x slowest).
+ * Replaces the frequency-domain gradient of the reference's adjoint solver
+ * (python/adjoint/optimization_problem.py:262-393, src/meepgeom.cpp:2835-3011)
+ * with the exact gradient of the time-stepped problem.  After mfd_backward the
+ * fields hold an intermediate state; create a new handle for another run.
+ * Not supported with dispersive materials or conductivity. */
+int mfd_design(mfd_sim *sim, int ncomp, const int *comps, const int lo[3], const int hi[3]);
+int mfd_forward(mfd_sim *sim, int nsteps, int checkpoint_every);
+int mfd_backward(mfd_sim *sim, int nmon, const int *mon_ids, const double *const *dft_grad,
+                 double *grad_chi1inv);
+
 /* Number of kernel launches issued by this handle so far (for accounting). */
 int64_t mfd_kernel_launches(const mfd_sim *sim);
 

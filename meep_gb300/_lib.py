@@ -65,6 +65,9 @@ SIGNATURES = [
     ("mfd_get_field", C.c_int, [_P, C.c_int, _DP]),
     ("mfd_get_dft", C.c_int, [_P, C.c_int, _DP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("mfd_flux", C.c_int, [_P, C.c_int, _IP, _IP, _DP]),
+    ("mfd_design", C.c_int, [_P, C.c_int, _IP, _IP, _IP]),
+    ("mfd_forward", C.c_int, [_P, C.c_int, C.c_int]),
+    ("mfd_backward", C.c_int, [_P, C.c_int, _IP, C.POINTER(_DP), _DP]),
     ("mfd_kernel_launches", C.c_int64, [_P]),
     ("mfd_last_step_ms", C.c_double, [_P]),
 ]
@@ -228,6 +231,31 @@ class Sim:
         out = np.zeros(nfreq)
         self.eng.check(self.eng.lib.mfd_flux(self.h, len(idE), idE, idH, _dptr(out)))
         return out
+
+    def design(self, comps, lo, hi):
+        """Declare the design: chi1inv of E components `comps` over the point
+        box lo..hi (inclusive)."""
+        self.design_comps = list(comps)
+        self.design_shape = tuple(int(hi[d]) - int(lo[d]) + 1 for d in range(3))
+        ca = (C.c_int * len(comps))(*comps)
+        self.eng.check(self.eng.lib.mfd_design(self.h, len(comps), ca, (C.c_int * 3)(*lo), (C.c_int * 3)(*hi)))
+
+    def forward(self, n, checkpoint_every=0):
+        self.eng.check(self.eng.lib.mfd_forward(self.h, int(n), int(checkpoint_every)))
+
+    def backward(self, dft_grads):
+        """dft_grads: {monitor id: complex array [npts, nfreq] of dJ/dRe F +
+        i dJ/dIm F}.  Returns dJ/dchi1inv, shape (ncomp, *design box)."""
+        ids = list(dft_grads)
+        keep = []
+        for m in ids:
+            g = np.asarray(dft_grads[m], dtype=np.complex128).reshape(-1)
+            keep.append(np.ascontiguousarray(np.stack([g.real, g.imag], axis=-1).reshape(-1)))
+        ida = (C.c_int * max(1, len(ids)))(*ids)
+        gp = (_DP * max(1, len(ids)))(*[_dptr(k) for k in keep])
+        out = np.zeros(len(self.design_comps) * int(np.prod(self.design_shape)))
+        self.eng.check(self.eng.lib.mfd_backward(self.h, len(ids), ida, gp, _dptr(out)))
+        return out.reshape((len(self.design_comps),) + self.design_shape)
 
     def launches(self):
         return self.eng.lib.mfd_kernel_launches(self.h)

@@ -36,6 +36,31 @@ public:
   // called before a batch of steps / after it (for timing)
   virtual void begin_steps() {}
   virtual void end_steps() {}
+
+  // ---- differentiation: reverse-time (discrete) adjoint of the step ----
+  // Design = E components `comps` over the point box lo..hi of each.
+  virtual void set_design(Plan &p, const std::vector<int> &comps, const int lo[3], const int hi[3]) {
+    (void)p, (void)comps, (void)lo, (void)hi;
+    throw Error("this backend has no adjoint");
+  }
+  // buffer for the design-box D of `nslots` steps; record after a step
+  virtual void alloc_record(Plan &p, int64_t nslots) { (void)p, (void)nslots; }
+  virtual void record_design(Plan &p, int64_t slot) { (void)p, (void)slot; }
+  // full-state checkpoints (all fields and auxiliaries, no DFT sums)
+  virtual int snapshot(Plan &p) {
+    (void)p;
+    return -1;
+  }
+  virtual void restore(Plan &p, int slot) { (void)p, (void)slot; }
+  virtual void set_skip_dft(bool skip) { (void)skip; }
+  // adjoint sweep: begin (zero adjoint fields, upload dJ/dDFT of the listed
+  // monitors), one reversed step s (state s -> s+1, recorded D of step s at
+  // `slot`), end (gradient dJ/dchi1inv per design component and box point)
+  virtual void adjoint_begin(Plan &p, int nmon, const int *ids, const double *const *grads) {
+    (void)p, (void)nmon, (void)ids, (void)grads;
+  }
+  virtual void adjoint_step(Plan &p, int64_t s, int64_t slot) { (void)p, (void)s, (void)slot; }
+  virtual void adjoint_end(Plan &p, double *grad) { (void)p, (void)grad; }
 };
 
 // Defined by whichever backend is linked in.

@@ -2,6 +2,7 @@
 // and the backend; every entry point converts exceptions to a status code and
 // a last-error string, the way the reference's SWIG layer maps meep::abort to
 // a Python exception (python/meep.i:1365-1380).
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -16,6 +17,11 @@ struct mfd_sim {
   std::unique_ptr<Backend> be;
   bool setup_done = false;
   int64_t t = 0;
+  // differentiation state
+  bool design = false;
+  int64_t fwd_t0 = -1, fwd_n = 0;
+  int fwd_K = 0;
+  std::vector<int> snaps;
 };
 
 static thread_local std::string g_last_error;
@@ -195,9 +201,7 @@ int mfd_add_dft(mfd_sim *s, int c, const int lo[3], const int hi[3], const doubl
   MFD_CATCH
 }
 
-int mfd_step(mfd_sim *s, int n) {
-  MFD_TRY
-  need(s && s->plan, "null simulation handle");
+static void ensure_setup(mfd_sim *s) {
   Plan &p = *s->plan;
   if (!s->setup_done) {
     s->be->setup(p);
@@ -205,24 +209,112 @@ int mfd_step(mfd_sim *s, int n) {
       s->be->add_monitor(p, i);
     s->setup_done = true;
   }
-  std::vector<SrcStepValues> vals(p.srcs.size());
+}
+
+// calc_sources at t, t+dt/2 and t+dt (src/step.cpp:64-108)
+static void source_values(Plan &p, int64_t t, std::vector<SrcStepValues> &vals) {
+  vals.resize(p.srcs.size());
+  double time = t * p.dt;
+  for (size_t k = 0; k < p.srcs.size(); k++) {
+    SrcTime &st = p.srcs[k];
+    st.update(time, p.dt);
+    vals[k].cur_b = st.cur_current;
+    st.update(time + 0.5 * p.dt, p.dt);
+    vals[k].cur_d = st.cur_current;
+    st.update(time + p.dt, p.dt);
+    vals[k].dip_e = st.cur_dipole;
+  }
+}
+
+int mfd_step(mfd_sim *s, int n) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  Plan &p = *s->plan;
+  ensure_setup(s);
+  std::vector<SrcStepValues> vals;
   s->be->begin_steps();
   for (int it = 0; it < n; it++) {
-    double time = s->t * p.dt;
-    // calc_sources at t, t+dt/2 and t+dt (src/step.cpp:64-108)
-    for (size_t k = 0; k < p.srcs.size(); k++) {
-      SrcTime &st = p.srcs[k];
-      st.update(time, p.dt);
-      vals[k].cur_b = st.cur_current;
-      st.update(time + 0.5 * p.dt, p.dt);
-      vals[k].cur_d = st.cur_current;
-      st.update(time + p.dt, p.dt);
-      vals[k].dip_e = st.cur_dipole;
-    }
+    source_values(p, s->t, vals);
     s->be->step(p, s->t, vals);
     s->t += 1;
   }
   s->be->end_steps();
+  MFD_CATCH
+}
+
+int mfd_design(mfd_sim *s, int ncomp, const int *comps, const int lo[3], const int hi[3]) {
+  MFD_TRY
+  need(s && s->plan && comps && lo && hi, "null argument");
+  need(ncomp >= 1 && ncomp <= 3, "1 to 3 design components");
+  ensure_setup(s);
+  s->be->set_design(*s->plan, std::vector<int>(comps, comps + ncomp), lo, hi);
+  s->design = true;
+  MFD_CATCH
+}
+
+int mfd_forward(mfd_sim *s, int n, int K) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  need(s->design, "call mfd_design before mfd_forward");
+  need(n >= 1 && K >= 0, "invalid step counts");
+  Plan &p = *s->plan;
+  ensure_setup(s);
+  s->fwd_t0 = s->t;
+  s->fwd_n = n;
+  s->fwd_K = K;
+  s->snaps.clear();
+  if (K == 0) s->be->alloc_record(p, n);
+  std::vector<SrcStepValues> vals;
+  s->be->begin_steps();
+  for (int it = 0; it < n; it++) {
+    if (K > 0 && it % K == 0) s->snaps.push_back(s->be->snapshot(p));
+    source_values(p, s->t, vals);
+    s->be->step(p, s->t, vals);
+    if (K == 0) s->be->record_design(p, it);
+    s->t += 1;
+  }
+  s->be->end_steps();
+  MFD_CATCH
+}
+
+int mfd_backward(mfd_sim *s, int nmon, const int *ids, const double *const *grads, double *grad_out) {
+  MFD_TRY
+  need(s && s->plan && grad_out, "null argument");
+  need(s->fwd_t0 >= 0, "call mfd_forward before mfd_backward");
+  need(nmon >= 0 && (nmon == 0 || (ids && grads)), "invalid monitor gradients");
+  Plan &p = *s->plan;
+  for (int q = 0; q < nmon; q++)
+    need(ids[q] >= 0 && ids[q] < (int)p.monitors.size(), "unknown monitor id");
+  Backend &be = *s->be;
+  be.begin_steps();
+  be.adjoint_begin(p, nmon, ids, grads);
+  const int64_t t0 = s->fwd_t0, n = s->fwd_n;
+  if (s->fwd_K == 0) {
+    for (int64_t st = t0 + n - 1; st >= t0; st--)
+      be.adjoint_step(p, st, st - t0);
+  }
+  else {
+    const int K = s->fwd_K;
+    be.alloc_record(p, K);
+    std::vector<SrcStepValues> vals;
+    for (int seg = (int)s->snaps.size() - 1; seg >= 0; seg--) {
+      const int64_t a = t0 + (int64_t)seg * K;
+      const int64_t len = std::min<int64_t>(K, t0 + n - a);
+      be.restore(p, s->snaps[seg]);
+      be.set_skip_dft(true);
+      for (int64_t it = 0; it < len; it++) {
+        source_values(p, a + it, vals);
+        be.step(p, a + it, vals);
+        be.record_design(p, it);
+      }
+      be.set_skip_dft(false);
+      for (int64_t st = a + len - 1; st >= a; st--)
+        be.adjoint_step(p, st, st - a);
+    }
+  }
+  be.adjoint_end(p, grad_out);
+  be.end_steps();
+  s->fwd_t0 = -1;
   MFD_CATCH
 }
 

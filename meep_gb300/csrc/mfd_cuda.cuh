@@ -310,6 +310,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 } // namespace mfd
 #include "mfd_fused.cuh"
 #include "mfd_k3d.cuh"
+#include "mfd_adjoint.cuh"
 namespace mfd {
 namespace cuda_impl {
 
@@ -1250,7 +1251,7 @@ public:
       update_e(p, dip);
     }
     int64_t tn = t + 1;
-    for (size_t id = 0; id < p.monitors.size(); id++) {
+    for (size_t id = 0; id < p.monitors.size() && !skip_dft; id++) {
       const Monitor &m = p.monitors[id];
       if (tn % m.decimation != 0) continue;
       double timeE = tn * p.dt;
@@ -1273,6 +1274,280 @@ public:
   double last_step_ms() const override { return ms; }
   long long launches() const override { return nlaunch; }
   void synchronize() override { cuda_check(cudaStreamSynchronize(stream), "sync"); }
+
+  // ------------------------------------------------------------ adjoint
+  std::vector<int> dcomps;       // design E components
+  Box dbox{};                    // design point box
+  long long dnpts = 0;
+  R *rec = nullptr;              // [slots][ncomp][dnpts]
+  long long rec_slots = 0;
+  std::vector<std::pair<void *, size_t>> state_list; // (pointer, bytes) of every state array
+  std::vector<char *> snaps;
+  R *lam_f[NC] = {}, *lam_fu[NC] = {}, *lam_fw[NC] = {}, *xbar[NC] = {};
+  double *grad = nullptr;
+  std::vector<double2 *> adj_G; // per monitor (null when the monitor has no gradient)
+  bool skip_dft = false;
+
+  void set_skip_dft(bool s) override { skip_dft = s; }
+
+  void set_design(Plan &p, const std::vector<int> &comps, const int lo[3], const int hi[3]) override {
+    for (int c : comps)
+      if (ctype(c) != MFD_E || !p.have[c]) throw Error("design components must be allocated E components");
+    if (!p.poles.empty()) throw Error("the adjoint does not support dispersive materials yet");
+    for (int c = 0; c < NC; c++)
+      if (!p.cond[c].empty()) throw Error("the adjoint does not support conductivity yet");
+    dcomps = comps;
+    dnpts = 1;
+    for (int d = 0; d < 3; d++) {
+      if (lo[d] < 0 || hi[d] >= p.ext[d] || hi[d] < lo[d]) throw Error("design box out of range");
+      dbox.lo[d] = lo[d];
+      dbox.n[d] = hi[d] - lo[d] + 1;
+      dnpts *= dbox.n[d];
+    }
+    // integrated sources inside the design box would make dE/dchi1inv = D - source
+    for (const SourceGroup &sg : p.sources)
+      for (int64_t di : sg.idx) {
+        int k[3];
+        p.dense_coords(di, k);
+        bool in = true;
+        for (int d = 0; d < 3; d++)
+          in = in && k[d] >= dbox.lo[d] && k[d] < dbox.lo[d] + dbox.n[d];
+        if (in && ctype(sg.c) == MFD_E) throw Error("a source lies inside the design region");
+      }
+  }
+
+  void alloc_record(Plan &p, int64_t nslots) override {
+    (void)p;
+    if (nslots <= rec_slots) return;
+    rec = dalloc<R>((size_t)nslots * dcomps.size() * dnpts);
+    rec_slots = nslots;
+  }
+
+  void record_design(Plan &p, int64_t slot) override {
+    for (size_t q = 0; q < dcomps.size(); q++) {
+      int dc = comp(MFD_D, cdir(dcomps[q]));
+      dim3 grid, block;
+      launch_dims(dbox, grid, block);
+      box_copy_kernel<R><<<grid, block, 0, stream>>>(geo, f[dc], rec + ((size_t)slot * dcomps.size() + q) * dnpts,
+                                                      dbox);
+      nlaunch++;
+    }
+    (void)p;
+  }
+
+  void collect_state(Plan &p) {
+    if (!state_list.empty()) return;
+    size_t bytes = p.nstore * sizeof(R);
+    for (int c = 0; c < NC; c++) {
+      for (R *ptr : {f[c], fu[c], fw[c], fcnd[c]})
+        if (ptr) state_list.push_back({ptr, bytes});
+    }
+    for (auto &pl : poles)
+      for (int d = 0; d < 3; d++)
+        for (R *ptr : {pl.P[d], pl.PP[d]})
+          if (ptr) state_list.push_back({ptr, bytes});
+  }
+
+  int snapshot(Plan &p) override {
+    collect_state(p);
+    size_t tot = 0;
+    for (auto &s_ : state_list)
+      tot += s_.second;
+    char *buf = dalloc<char>(tot);
+    size_t off = 0;
+    for (auto &s_ : state_list) {
+      cuda_check(cudaMemcpyAsync(buf + off, s_.first, s_.second, cudaMemcpyDeviceToDevice, stream), "snapshot");
+      off += s_.second;
+    }
+    snaps.push_back(buf);
+    return (int)snaps.size() - 1;
+  }
+
+  void restore(Plan &p, int slot) override {
+    collect_state(p);
+    size_t off = 0;
+    for (auto &s_ : state_list) {
+      cuda_check(cudaMemcpyAsync(s_.first, snaps[slot] + off, s_.second, cudaMemcpyDeviceToDevice, stream),
+                 "restore");
+      off += s_.second;
+    }
+  }
+
+  void adjoint_begin(Plan &p, int nmon, const int *ids, const double *const *grads) override {
+    for (int c = 0; c < NC; c++) {
+      if (!p.have[c]) continue;
+      if (!lam_f[c]) lam_f[c] = dalloc<R>(p.nstore);
+      cuda_check(cudaMemsetAsync(lam_f[c], 0, p.nstore * sizeof(R), stream), "memset");
+      int t = ctype(c);
+      if ((t == MFD_D || t == MFD_B) && fu[c]) {
+        if (!lam_fu[c]) lam_fu[c] = dalloc<R>(p.nstore);
+        cuda_check(cudaMemsetAsync(lam_fu[c], 0, p.nstore * sizeof(R), stream), "memset");
+      }
+      if ((t == MFD_E || t == MFD_H) && fw[c]) {
+        if (!lam_fw[c]) lam_fw[c] = dalloc<R>(p.nstore);
+        cuda_check(cudaMemsetAsync(lam_fw[c], 0, p.nstore * sizeof(R), stream), "memset");
+      }
+      if ((t == MFD_D || t == MFD_B) && !xbar[c]) xbar[c] = dzeros<R>(p.nstore);
+    }
+    if (!grad) grad = dalloc<double>(std::max<size_t>(1, dcomps.size() * dnpts));
+    cuda_check(cudaMemsetAsync(grad, 0, std::max<size_t>(1, dcomps.size() * dnpts) * sizeof(double), stream),
+               "memset");
+    adj_G.assign(p.monitors.size(), nullptr);
+    for (int q = 0; q < nmon; q++) {
+      const Monitor &m = p.monitors[ids[q]];
+      std::vector<double> h(grads[q], grads[q] + 2 * m.npts * m.freq.size());
+      adj_G[ids[q]] = (double2 *)dupload(h);
+    }
+  }
+
+  AdjCurlArgs<R> adj_args(Plan &p, int c) {
+    const Plan::Curl &cp = p.curl[c];
+    AdjCurlArgs<R> a{};
+    a.lf = lam_f[c];
+    a.lfu = lam_fu[c];
+    a.xbar = xbar[c];
+    a.dsig = cp.dsig;
+    a.dsigu = cp.dsigu;
+    for (int d = 0; d < 3; d++)
+      a.shift[d] = p.shift[c][d];
+    a.c = cp.flip ? -R(p.g.courant) : R(p.g.courant);
+    a.box = full_box(p, c);
+    a.dir = cdir(c);
+    return a;
+  }
+
+  void adj_gather(Plan &p, int srcc, int curl_type) {
+    // adjoint of source component srcc (E for B curls, H for D curls)
+    GatherArgs<R> ga{};
+    int n = 0;
+    for (int c = 0; c < NC; c++) {
+      if (!p.have[c] || ctype(c) != curl_type) continue;
+      const Plan::Curl &cp = p.curl[c];
+      const int stp = curl_type == MFD_B ? 1 : -1;
+      if (cp.g1 == srcc) ga.term[n++] = GatherTerm<R>{xbar[c], cp.d1, +1, stp};
+      if (cp.g2 == srcc) ga.term[n++] = GatherTerm<R>{xbar[c], cp.d2, -1, stp};
+    }
+    if (!n) return;
+    ga.nterm = n;
+    int d = cdir(srcc);
+    if (curl_type == MFD_D) {
+      ga.target = lam_f[comp(MFD_B, d)];
+      ga.target_h = p.pml_dir[d] ? lam_f[srcc] : nullptr;
+      ga.hdir = d;
+    }
+    else {
+      ga.target = lam_f[srcc];
+      ga.target_h = nullptr;
+      ga.hdir = 0;
+    }
+    for (int q = 0; q < 3; q++) {
+      ga.box.lo[q] = 0;
+      ga.box.n[q] = p.ext[q];
+      ga.N[q] = p.N[q];
+    }
+    dim3 grid, block;
+    launch_dims(ga.box, grid, block);
+    adj_gather_kernel<R><<<grid, block, 0, stream>>>(geo, ga);
+    nlaunch++;
+  }
+
+  void adjoint_step(Plan &p, int64_t s, int64_t slot) override {
+    // 1. objective terms of the DFT samples taken after this step
+    const int64_t tn = s + 1;
+    for (size_t id = 0; id < p.monitors.size(); id++) {
+      if (id >= adj_G.size() || !adj_G[id]) continue;
+      const Monitor &m = p.monitors[id];
+      if (tn % m.decimation != 0) continue;
+      DMon &dm = mons[id];
+      const int nf = (int)m.freq.size();
+      double timeE = tn * p.dt;
+      double time = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? timeE - 0.5 * p.dt : timeE;
+      dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(), m.scale.imag(),
+                                                              dm.ph);
+      InjectArgs<R> ia{};
+      ia.lam = lam_f[m.c];
+      ia.lamb = nullptr;
+      if (ctype(m.c) == MFD_H) {
+        int d = cdir(m.c);
+        ia.hdir = d;
+        ia.hshift = p.shift[m.c][d];
+        ia.lamb = lam_f[comp(MFD_B, d)];
+        if (!p.pml_dir[d]) ia.lam = ia.lamb;
+      }
+      for (int d = 0; d < 3; d++) {
+        ia.w[d] = dm.w[d];
+        ia.lo[d] = m.lo[d];
+        ia.n[d] = m.hi[d] - m.lo[d] + 1;
+      }
+      ia.dV = m.dV;
+      ia.include_weights = m.include_weights;
+      ia.dim = p.g.dim;
+      ia.ad0 = ia.ad1 = -1;
+      if (m.centered)
+        for (int d = 0; d < 3; d++)
+          if (p.present[d] && p.shift[m.c][d] == 0) {
+            if (ia.ad0 >= 0) ia.ad1 = d;
+            else ia.ad0 = d;
+          }
+      ia.G = adj_G[id];
+      ia.ph = dm.ph;
+      ia.nf = nf;
+      ia.npts = (long long)m.npts;
+      adj_inject_kernel<R><<<(unsigned)((ia.npts + 255) / 256), 256, 0, stream>>>(geo, ia);
+      nlaunch += 2;
+    }
+    // 2. reverse D/E half step
+    for (int d = 0; d < 3; d++) {
+      int c = comp(MFD_D, d);
+      if (!p.have[c] || p.curl[c].g1 < 0) continue;
+      AdjCurlArgs<R> a = adj_args(p, c);
+      int ec = comp(MFD_E, d);
+      a.le = lam_f[ec];
+      a.lfw = lam_fw[ec];
+      a.chi = chi[ec];
+      a.isB = 0;
+      a.rec = nullptr;
+      for (size_t q = 0; q < dcomps.size(); q++)
+        if (dcomps[q] == ec && rec) {
+          a.rec = rec + ((size_t)slot * dcomps.size() + q) * dnpts;
+          a.grad = grad + q * dnpts;
+          for (int e = 0; e < 3; e++) {
+            a.dlo[e] = dbox.lo[e];
+            a.dn[e] = dbox.n[e];
+          }
+        }
+      dim3 grid, block;
+      launch_dims(a.box, grid, block);
+      adj_de_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+      nlaunch++;
+    }
+    for (int d = 0; d < 3; d++)
+      if (p.have[comp(MFD_H, d)]) adj_gather(p, comp(MFD_H, d), MFD_D);
+    // 3. reverse B half step (H through f_w inside the slab, then the curl)
+    for (int d = 0; d < 3; d++) {
+      int c = comp(MFD_B, d);
+      if (!p.have[c] || p.curl[c].g1 < 0) continue;
+      AdjCurlArgs<R> a = adj_args(p, c);
+      int hc = comp(MFD_H, d);
+      a.le = p.pml_dir[d] ? lam_f[hc] : nullptr;
+      a.lfw = lam_fw[hc];
+      a.isB = 1;
+      dim3 grid, block;
+      launch_dims(a.box, grid, block);
+      adj_bh_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+      nlaunch++;
+    }
+    for (int d = 0; d < 3; d++)
+      if (p.have[comp(MFD_E, d)]) adj_gather(p, comp(MFD_E, d), MFD_B);
+  }
+
+  void adjoint_end(Plan &p, double *out) override {
+    (void)p;
+    size_t n = dcomps.size() * dnpts;
+    cuda_check(cudaMemcpyAsync(out, grad, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "grad");
+    cuda_check(cudaStreamSynchronize(stream), "grad sync");
+    cuda_check(cudaGetLastError(), "adjoint");
+  }
 
   void get_field(Plan &p, int c, double *out) override {
     std::vector<R> h(p.nstore), hb;

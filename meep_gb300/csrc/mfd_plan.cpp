@@ -217,11 +217,15 @@ Plan::Plan(const mfd_grid &grid) : g(grid) {
       s2 = -s2;
     }
     bool flip = false;
+    int d1 = g1 >= 0 ? pderiv : -1, d2 = g2 >= 0 ? mderiv : -1;
     if (g1 < 0) {
       std::swap(g1, g2);
       std::swap(s1, s2);
+      std::swap(d1, d2);
       flip = true;
     }
+    cp.d1 = d1;
+    cp.d2 = d2;
     cp.g1 = g1;
     cp.g2 = g2;
     cp.s1 = s1;

@@ -116,6 +116,7 @@ public:
     int g1 = -1, g2 = -1;
     int64_t s1 = 0, s2 = 0;
     bool flip = false; // dtdx negated (g1 missing, g2 moved into its place)
+    int d1 = -1, d2 = -1; // directions of the strides s1, s2
     int dsig = -1, dsigu = -1;
   } curl[NC];
 

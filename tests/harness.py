@@ -137,3 +137,54 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     out["flux"] = sim.flux([mons[0]], [mons[1]], 5)
     sim.close()
     return out
+
+
+# ---------------------------------------------------------------- adjoint
+def tm2d_design_problem(eng, eps_design, precision=64, steps=600, checkpoint_every=0, grad=True,
+                        nfreq=5, seed=3):
+    """2-D TM problem for gradient tests: 72x56 cells, resolution 10, PML 0.5
+    on all sides, eps=12 guide along x, an eps design block (given) in the
+    middle, Gaussian Ez line source on the left, objective
+    J = sum_w mean_k |DFT Ez(k, w)|^2 over a 9-point line on the right.
+    Returns (J, dJ/deps over the design block or None)."""
+    rng = np.random.default_rng(seed)
+    n = (72, 56, 0)
+    io = (-72, -56, 0)
+    comps = [_lib.comp(_lib.E, _lib.Z), _lib.comp(_lib.D, _lib.Z), _lib.comp(_lib.H, _lib.X),
+             _lib.comp(_lib.B, _lib.X), _lib.comp(_lib.H, _lib.Y), _lib.comp(_lib.B, _lib.Y)]
+    pml = {(d, s): (0.5, 1e-15, 1.0) for d in (0, 1) for s in (0, 1)}
+    sim = _lib.Sim(eng, dim=2, n=n, io=io, a=10.0, courant=0.5, pml=pml, precision=precision,
+                   components=comps)
+    ext = sim.ext
+    eps = np.ones((ext[0], ext[1]))
+    eps[:, 24:32] = 12.0                                  # guide
+    eps += 0.2 * rng.uniform(size=eps.shape)              # weak background texture
+    eps_design = np.asarray(eps_design, dtype=np.float64)
+    lo = (28, 20, 0)
+    hi = (lo[0] + eps_design.shape[0] - 1, lo[1] + eps_design.shape[1] - 1, 0)
+    eps[lo[0]:hi[0] + 1, lo[1]:hi[1] + 1] = eps_design
+    ez = _lib.comp(_lib.E, _lib.Z)
+    sim.set_chi1inv(ez, _lib.Z, 1.0 / eps)
+    src = sim.add_gaussian_src(0.35, 0.2)
+    idx = [14 * ext[1] + j for j in range(24, 33)]
+    sim.add_source_points(ez, src, idx, np.ones(len(idx)) * 10.0)
+    line_lo, line_hi = (56, 24, 0), (56, 32, 0)
+    w = [np.ones(1), np.ones(9), None]
+    freqs = np.linspace(0.3, 0.4, nfreq)
+    mid = sim.add_dft(ez, line_lo, line_hi, w, dV=1.0, include_weights=False, scale=1.0, centered=False,
+                      freqs=freqs, decimation=1)
+    if grad:
+        sim.design([ez], lo, hi)
+        sim.forward(steps, checkpoint_every)
+    else:
+        sim.step(steps)
+    F = sim.get_dft(mid)                                   # [npts, nfreq]
+    J = float(np.sum(np.abs(F) ** 2) / F.shape[0])
+    g = None
+    if grad:
+        G = 2.0 * F / F.shape[0]                           # dJ/dRe F + i dJ/dIm F
+        gchi = sim.backward({mid: G})[0, :, :, 0]
+        chi = 1.0 / eps_design
+        g = -gchi * chi * chi                              # chi = 1/eps
+    sim.close()
+    return J, g
