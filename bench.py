@@ -151,6 +151,48 @@ def cpu_sample(bits=32, steps=4, warmup=1):
         steps, WORKLOAD, bits, warmup, thr)
 
 
+def adjoint_timing():
+    """Reverse-time adjoint on the 2-D design problem (400x240 cells, 100x100
+    design, 3000 steps, checkpoints every 55 steps): wall time of forward +
+    backward over the plain forward run, FP64 and FP32, and the FP64 gradient
+    against central differences at 4 pixels."""
+    import numpy as np
+    from meep_gb300 import _lib
+    from meep_gb300.design import DesignProblem2D
+
+    out = {}
+    rng = np.random.default_rng(2024)
+    for prec in (64, 32):
+        prob = DesignProblem2D(_lib.Engine(), precision=prec)
+        eps = rng.uniform(1.0, 12.0, size=prob.design) if prec == 64 else eps
+        prob.run(eps)  # warm-up
+        t0 = time.perf_counter()
+        F, _ = prob.run(eps)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        F, handle = prob.run(eps, grad=True, checkpoint_every=55)
+        J, dJdF = prob.objective(F)
+        g = prob.backward(handle, dJdF)
+        t_grad = time.perf_counter() - t0
+        entry = {"forward_s": t_fwd, "forward_plus_adjoint_s": t_grad, "grad_over_forward": t_grad / t_fwd}
+        if prec == 64:
+            pix = [(7, 11), (50, 50), (93, 40), (20, 88)]
+            fd = []
+            for (a, b) in pix:
+                ep, em = eps.copy(), eps.copy()
+                ep[a, b] += 1e-4
+                em[a, b] -= 1e-4
+                fd.append((prob.objective(prob.run(ep)[0])[0] - prob.objective(prob.run(em)[0])[0]) / 2e-4)
+            adj = np.array([g[a, b] for (a, b) in pix])
+            fd = np.array(fd)
+            entry["grad_rel_err_vs_fd"] = float(np.abs(adj - fd).max() / np.abs(fd).max())
+            g64 = g
+        else:
+            entry["grad_rel_err_vs_fp64"] = float(np.abs(g - g64).max() / np.abs(g64).max())
+        out["fp%d" % prec] = entry
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,6 +277,10 @@ def main():
             dist.destroy_process_group()
         return 0
     cpu_val, cpu_thr, cpu_desc = cpu_sample(32)
+    try:
+        adj = adjoint_timing()
+    except Exception as e:  # reported, never fatal for the stepping benchmark
+        adj = {"error": str(e)[:200]}
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
@@ -259,6 +305,7 @@ def main():
         "cpu_baseline": {"value": cpu_val, "unit": "Mcell-updates/s", "cores": cpu_thr, "kind": "port",
                          "sample": cpu_desc},
         "clocks": clk.summary(),
+        "adjoint": adj,
     }
     print(json.dumps(line))
     if dist is not None:
