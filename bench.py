@@ -174,7 +174,14 @@ def adjoint_timing():
         J, dJdF = prob.objective(F)
         g = prob.backward(handle, dJdF)
         t_grad = time.perf_counter() - t0
-        entry = {"forward_s": t_fwd, "forward_plus_adjoint_s": t_grad, "grad_over_forward": t_grad / t_fwd}
+        t0 = time.perf_counter()
+        F, handle = prob.run(eps, grad=True, checkpoint_every=0)
+        g_rec = prob.backward(handle, prob.objective(F)[1])
+        t_rec = time.perf_counter() - t0
+        entry = {"forward_s": t_fwd, "forward_plus_adjoint_s": t_grad, "grad_over_forward": t_grad / t_fwd,
+                 "checkpoint_every": 55,
+                 "recorded_design_grad_over_forward": t_rec / t_fwd,
+                 "recorded_vs_checkpointed_rel": float(np.abs(g_rec - g).max() / np.abs(g).max())}
         if prec == 64:
             pix = [(7, 11), (50, 50), (93, 40), (20, 88)]
             fd = []

@@ -132,7 +132,8 @@ int mfd_flux(mfd_sim *sim, int npairs, const int *idE, const int *idH, double *o
  * with checkpoint_every == 0 it records D at the design points for every step;
  * with checkpoint_every = K > 0 it stores a full-state checkpoint every K steps
  * and the backward pass recomputes each segment from its checkpoint (sqrt(T)
- * memory).  mfd_backward takes dJ/dDFT for the listed monitors (per monitor
+ * memory); checkpoint_every = -1 picks recording when it fits a memory budget
+ * (16 GB, or MFD_RECORD_BUDGET_GB) and sqrt(nsteps) checkpoints otherwise.  mfd_backward takes dJ/dDFT for the listed monitors (per monitor
  * npts*nfreq*(re,im) = dJ/dRe F + i dJ/dIm F) and returns dJ/dchi1inv for every
  * design component and box point (ncomp * npts doubles, x slowest).
  * Replaces the frequency-domain gradient of the reference's adjoint solver

@@ -25,6 +25,43 @@
 namespace mfd {
 namespace cuda_impl {
 
+// Gather the curl adjoints Xb of up to two curl components into the adjoint
+// of one source array (E for B curls; H or B for D curls).  For a curl term
+// +G[i+s] - G[i] the adjoint of G receives +Xb at i+s and -Xb at i.
+template <typename R> struct GatherTerm {
+  const R *xb;   // Xb of the curl component (0 outside its updated points)
+  int dir;       // direction of the stride s
+  int sign;      // +1: term G[i+s] - G[i] (s along dir, +1 or -1 point); -1: G[i] - G[i+s]
+  int step;      // +1 or -1: s = step * stride(dir)
+};
+
+template <typename R> struct GatherArgs {
+  R *target;      // lambda array (B, or E)
+  R *target_h;    // for D curls: lambda of H inside the H slab along hdir (null otherwise)
+  int hdir;
+  int nterm;
+  GatherTerm<R> term[4];
+  Box box;        // full point range of the source component
+  int N[3];
+};
+
+// sum of the gathered curl adjoints at point j (k: its indices)
+template <typename R> __device__ __forceinline__ R gather_at(const Geo &g, const GatherArgs<R> &a, const int k[3],
+                                                             long long j) {
+  R acc = R(0);
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    if (t >= a.nterm) break;
+    const GatherTerm<R> &T = a.term[t];
+    // term sign * (G[i+s] - G[i]): at point j the adjoint gets +Xb[j-s] - Xb[j]
+    const int kn = k[T.dir] - T.step;
+    R v = -T.xb[j];
+    if (kn >= 0 && kn <= a.N[T.dir]) v += T.xb[j - T.step * g.stride[T.dir]];
+    acc += T.sign > 0 ? v : -v;
+  }
+  return acc;
+}
+
 template <typename R> struct AdjCurlArgs {
   R *lf, *lfu, *xbar;
   int dsig, dsigu;
@@ -40,6 +77,9 @@ template <typename R> struct AdjCurlArgs {
   const R *rec;       // recorded D at the design points for this step, or null
   double *grad;       // dJ/dchi1inv accumulator
   int dlo[3], dn[3];
+  // curl adjoints of the other half step, gathered into the E (or H/B)
+  // adjoint at this point before it is used
+  GatherArgs<R> gat;
 };
 
 template <typename R>
@@ -86,7 +126,9 @@ __global__ void __launch_bounds__(256) adj_de_kernel(Geo g, Tables<R> tb, AdjCur
   int k[3];
   if (!box_point(g, a.box, k)) return;
   const long long i = lin(g, k);
-  const R le = a.le[i];
+  // lambda of E: objective terms already added, plus the curl adjoints of the
+  // B half step that read E
+  const R le = a.le[i] + gather_at(g, a.gat, k, i);
   R lam = a.lf[i];
   const int pw = a.shift[a.dir] + 2 * k[a.dir];
   R gsrc;
@@ -95,8 +137,9 @@ __global__ void __launch_bounds__(256) adj_de_kernel(Geo g, Tables<R> tb, AdjCur
     const R kk = tb.kap[a.dir][pw], ss = tb.sig[a.dir][pw];
     const R lfw = a.lfw[i] + (kk + ss) * le;
     a.lfw[i] = -(kk - ss) * le;
+    a.le[i] = le; // lambda of E_old
     lam += a.chi[i] * lfw;
-    gsrc = lfw; // lambda of E_old stays le
+    gsrc = lfw;
   }
   else {
     // E' = chi (D' - P - sources)
@@ -120,37 +163,22 @@ __global__ void __launch_bounds__(256) adj_bh_kernel(Geo g, Tables<R> tb, AdjCur
   int k[3];
   if (!box_point(g, a.box, k)) return;
   const long long i = lin(g, k);
+  // curl adjoints of the D half step that read H (inside the H slab) or B
+  const R gsum = gather_at(g, a.gat, k, i);
   R lam = a.lf[i];
   const int pw = 2 * k[a.dir];
   if (a.le && slab(g, a.dir, pw)) {
     // H' = H + (k+s) B' - (k-s) fw, fw' = B'
     const R kk = tb.kap[a.dir][pw], ss = tb.sig[a.dir][pw];
-    const R lh = a.le[i];
+    const R lh = a.le[i] + gsum;
+    a.le[i] = lh;
     lam += (kk + ss) * lh + a.lfw[i];
     a.lfw[i] = -(kk - ss) * lh;
   }
+  else
+    lam += gsum;
   adj_curl_core(g, tb, a, k, i, lam);
 }
-
-// Gather the curl adjoints Xb of up to two curl components into the adjoint
-// of one source array (E for B curls; H or B for D curls).  For a curl term
-// +G[i+s] - G[i] the adjoint of G receives +Xb at i+s and -Xb at i.
-template <typename R> struct GatherTerm {
-  const R *xb;   // Xb of the curl component (0 outside its updated points)
-  int dir;       // direction of the stride s
-  int sign;      // +1: term G[i+s] - G[i] (s along dir, +1 or -1 point); -1: G[i] - G[i+s]
-  int step;      // +1 or -1: s = step * stride(dir)
-};
-
-template <typename R> struct GatherArgs {
-  R *target;      // lambda array (B, or E)
-  R *target_h;    // for D curls: lambda of H inside the H slab along hdir (null otherwise)
-  int hdir;
-  int nterm;
-  GatherTerm<R> term[4];
-  Box box;        // full point range of the source component
-  int N[3];
-};
 
 template <typename R> __global__ void __launch_bounds__(256) adj_gather_kernel(Geo g, GatherArgs<R> a) {
   int k[3];

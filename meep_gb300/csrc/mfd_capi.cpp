@@ -3,6 +3,8 @@
 // a last-error string, the way the reference's SWIG layer maps meep::abort to
 // a Python exception (python/meep.i:1365-1380).
 #include <algorithm>
+#include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -19,6 +21,7 @@ struct mfd_sim {
   int64_t t = 0;
   // differentiation state
   bool design = false;
+  int64_t design_points = 0;
   int64_t fwd_t0 = -1, fwd_n = 0;
   int fwd_K = 0;
   std::vector<int> snaps;
@@ -249,6 +252,7 @@ int mfd_design(mfd_sim *s, int ncomp, const int *comps, const int lo[3], const i
   ensure_setup(s);
   s->be->set_design(*s->plan, std::vector<int>(comps, comps + ncomp), lo, hi);
   s->design = true;
+  s->design_points = (int64_t)ncomp * (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
   MFD_CATCH
 }
 
@@ -256,9 +260,17 @@ int mfd_forward(mfd_sim *s, int n, int K) {
   MFD_TRY
   need(s && s->plan, "null simulation handle");
   need(s->design, "call mfd_design before mfd_forward");
-  need(n >= 1 && K >= 0, "invalid step counts");
+  need(n >= 1 && K >= -1, "invalid step counts");
   Plan &p = *s->plan;
   ensure_setup(s);
+  if (K < 0) {
+    // automatic: record the design-point D of every step when that fits the
+    // budget (no recomputation), else checkpoints every ceil(sqrt(n)) steps
+    double budget = 16e9;
+    if (const char *e = getenv("MFD_RECORD_BUDGET_GB")) budget = atof(e) * 1e9;
+    double need_bytes = (double)s->design_points * n * (p.g.precision / 8);
+    K = need_bytes <= budget ? 0 : (int)std::ceil(std::sqrt((double)n));
+  }
   s->fwd_t0 = s->t;
   s->fwd_n = n;
   s->fwd_K = K;

@@ -1387,7 +1387,8 @@ public:
         if (!lam_fw[c]) lam_fw[c] = dalloc<R>(p.nstore);
         cuda_check(cudaMemsetAsync(lam_fw[c], 0, p.nstore * sizeof(R), stream), "memset");
       }
-      if ((t == MFD_D || t == MFD_B) && !xbar[c]) xbar[c] = dzeros<R>(p.nstore);
+      if ((t == MFD_D || t == MFD_B) && !xbar[c]) xbar[c] = dalloc<R>(p.nstore);
+      if (xbar[c]) cuda_check(cudaMemsetAsync(xbar[c], 0, p.nstore * sizeof(R), stream), "memset");
     }
     if (!grad) grad = dalloc<double>(std::max<size_t>(1, dcomps.size() * dnpts));
     cuda_check(cudaMemsetAsync(grad, 0, std::max<size_t>(1, dcomps.size() * dnpts) * sizeof(double), stream),
@@ -1416,8 +1417,9 @@ public:
     return a;
   }
 
-  void adj_gather(Plan &p, int srcc, int curl_type) {
-    // adjoint of source component srcc (E for B curls, H for D curls)
+  // gather description for the adjoint of source component srcc (E for B
+  // curls, H for D curls)
+  GatherArgs<R> gather_args(Plan &p, int srcc, int curl_type) {
     GatherArgs<R> ga{};
     int n = 0;
     for (int c = 0; c < NC; c++) {
@@ -1427,28 +1429,13 @@ public:
       if (cp.g1 == srcc) ga.term[n++] = GatherTerm<R>{xbar[c], cp.d1, +1, stp};
       if (cp.g2 == srcc) ga.term[n++] = GatherTerm<R>{xbar[c], cp.d2, -1, stp};
     }
-    if (!n) return;
     ga.nterm = n;
-    int d = cdir(srcc);
-    if (curl_type == MFD_D) {
-      ga.target = lam_f[comp(MFD_B, d)];
-      ga.target_h = p.pml_dir[d] ? lam_f[srcc] : nullptr;
-      ga.hdir = d;
-    }
-    else {
-      ga.target = lam_f[srcc];
-      ga.target_h = nullptr;
-      ga.hdir = 0;
-    }
     for (int q = 0; q < 3; q++) {
       ga.box.lo[q] = 0;
       ga.box.n[q] = p.ext[q];
       ga.N[q] = p.N[q];
     }
-    dim3 grid, block;
-    launch_dims(ga.box, grid, block);
-    adj_gather_kernel<R><<<grid, block, 0, stream>>>(geo, ga);
-    nlaunch++;
+    return ga;
   }
 
   void adjoint_step(Plan &p, int64_t s, int64_t slot) override {
@@ -1506,6 +1493,7 @@ public:
       a.lfw = lam_fw[ec];
       a.chi = chi[ec];
       a.isB = 0;
+      a.gat = gather_args(p, ec, MFD_B);
       a.rec = nullptr;
       for (size_t q = 0; q < dcomps.size(); q++)
         if (dcomps[q] == ec && rec) {
@@ -1521,8 +1509,6 @@ public:
       adj_de_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
       nlaunch++;
     }
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_H, d)]) adj_gather(p, comp(MFD_H, d), MFD_D);
     // 3. reverse B half step (H through f_w inside the slab, then the curl)
     for (int d = 0; d < 3; d++) {
       int c = comp(MFD_B, d);
@@ -1532,13 +1518,12 @@ public:
       a.le = p.pml_dir[d] ? lam_f[hc] : nullptr;
       a.lfw = lam_fw[hc];
       a.isB = 1;
+      a.gat = gather_args(p, hc, MFD_D);
       dim3 grid, block;
       launch_dims(a.box, grid, block);
       adj_bh_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
       nlaunch++;
     }
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_E, d)]) adj_gather(p, comp(MFD_E, d), MFD_B);
   }
 
   void adjoint_end(Plan &p, double *out) override {
