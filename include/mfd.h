@@ -146,6 +146,26 @@ int mfd_forward(mfd_sim *sim, int nsteps, int checkpoint_every);
 int mfd_backward(mfd_sim *sim, int nmon, const int *mon_ids, const double *const *dft_grad,
                  double *grad_chi1inv);
 
+/* Allocation-free flux reduction.  No counterpart in the reference: it is the
+ * reduction of mfd_flux (sum_k Re(E conj H) per frequency) for callers that
+ * must not allocate device memory when they call it -- code recording a CUDA
+ * graph, hosts whose device memory belongs to another allocator, loops that
+ * cannot take the device synchronisation of cudaMalloc/cudaFree.  Inputs are
+ * device pointers to two DFT sum arrays laid out as this engine keeps them
+ * (npts * nfreq complex doubles, point-major, i.e. mfd_get_dft's layout), the
+ * output a device pointer to nfreq doubles; `stream` is a cudaStream_t (NULL
+ * = default stream).  Scratch is a fixed 2 MiB file-scope device array
+ * (MFD_NOALLOC_MAX_PARTS rows of MFD_NOALLOC_MAX_FREQ doubles) shared by every
+ * call on a device: nfreq above MFD_NOALLOC_MAX_FREQ is rejected, and calls
+ * that overlap on the GPU race on it.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) with that device current; make it
+ * before any stream capture.  Errors: mfd_noalloc_last_error(). */
+#define MFD_NOALLOC_MAX_FREQ 1024
+#define MFD_NOALLOC_MAX_PARTS 256
+int mfd_flux_noalloc(const double *dft_E, const double *dft_H, int64_t npts, int nfreq, double *flux_out,
+                     void *stream);
+const char *mfd_noalloc_last_error(void);
+
 /* Number of kernel launches issued by this handle so far (for accounting). */
 int64_t mfd_kernel_launches(const mfd_sim *sim);
 

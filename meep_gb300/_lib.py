@@ -68,9 +68,15 @@ SIGNATURES = [
     ("mfd_design", C.c_int, [_P, C.c_int, _IP, _IP, _IP]),
     ("mfd_forward", C.c_int, [_P, C.c_int, C.c_int]),
     ("mfd_backward", C.c_int, [_P, C.c_int, _IP, C.POINTER(_DP), _DP]),
+    ("mfd_flux_noalloc", C.c_int, [_P, _P, C.c_int64, C.c_int, _P, _P]),
+    ("mfd_noalloc_last_error", C.c_char_p, []),
     ("mfd_kernel_launches", C.c_int64, [_P]),
     ("mfd_last_step_ms", C.c_double, [_P]),
 ]
+
+
+# entry points that take device pointers; only the CUDA library exports them
+DEVICE_ONLY = ("mfd_flux_noalloc", "mfd_noalloc_last_error")
 
 
 class Engine:
@@ -88,6 +94,8 @@ class Engine:
         self.path = path
         self.lib = C.CDLL(path, mode=C.RTLD_LOCAL)
         for name, res, args in SIGNATURES:
+            if name in DEVICE_ONLY and not hasattr(self.lib, name):
+                continue  # the CPU oracle library has no device-pointer entries
             fn = getattr(self.lib, name)
             fn.restype = res
             fn.argtypes = args

@@ -69,6 +69,8 @@ def build_engine(force=False, verbose=False):
                              "-o", os.path.join(objdir, "mfd_cuda_f64.o")])
     jobs.append(cu_common + ["-c", os.path.join(CSRC, "mfd_cuda_f32.cu"),
                              "-o", os.path.join(objdir, "mfd_cuda_f32.o")])
+    jobs.append(cu_common + ["-c", os.path.join(CSRC, "mfd_noalloc.cu"),
+                             "-o", os.path.join(objdir, "mfd_noalloc.o")])
     for src in ("mfd_plan.cpp", "mfd_capi.cpp"):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"] + INC +
                     ["-c", os.path.join(CSRC, src), "-o", os.path.join(objdir, src.replace(".cpp", ".o"))])
@@ -77,8 +79,8 @@ def build_engine(force=False, verbose=False):
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    objs = [os.path.join(objdir, f) for f in ("mfd_cuda_f64.o", "mfd_cuda_f32.o", "mfd_plan.o",
-                                               "mfd_capi.o")]
+    objs = [os.path.join(objdir, f) for f in ("mfd_cuda_f64.o", "mfd_cuda_f32.o", "mfd_noalloc.o",
+                                               "mfd_plan.o", "mfd_capi.o")]
     _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
     api = os.path.join(CSRC, "meep_api.cpp")
     links = []
