@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "mfd_backend.hpp"
@@ -310,6 +311,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 } // namespace mfd
 #include "mfd_fused.cuh"
 #include "mfd_k3d.cuh"
+#include "mfd_q3d.cuh"
 #include "mfd_adjoint.cuh"
 namespace mfd {
 namespace cuda_impl {
@@ -770,6 +772,74 @@ public:
   BoxList box_int{}, box_bnd{};
   dim3 fblock{32, 8, 1};
 
+  // 3-D decomposition: rows (x, y interior, all z; z slabs inside the rows),
+  // x slabs (all y, all z), y slabs (interior x, all z).  The FP32 B update
+  // splits the rows into the core (quads) and the z ends of the rows.
+  Band band_rows{}, band_x{}, band_y{}, band_zend{};
+  QCore qcore{};
+
+  static Span span_run(int lo, int hi) {
+    Span s{};
+    s.n = std::max(0, hi - lo + 1);
+    s.split = s.n;
+    s.a0 = lo;
+    return s;
+  }
+  // points 0..n-1 outside the run lo..hi
+  static Span span_outside(int n, int lo, int hi) {
+    Span s{};
+    s.split = lo;
+    s.n = lo + (n - 1 - hi);
+    s.a0 = 0;
+    s.a1 = hi + 1 - lo;
+    return s;
+  }
+  // short z spans (the z ends of the rows) take whole blocks of several rows
+  // so no lane idles; long spans take warps of 32 consecutive z points
+  static void band_shape(const Band &b, dim3 &g, dim3 &blk) {
+    g = blk = dim3(0, 0, 0);
+    if (b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0) return;
+    if (b.s[2].n <= 64) {
+      blk = dim3((unsigned)b.s[2].n, (unsigned)std::max(1, 256 / b.s[2].n), 1);
+      g = dim3(1, (unsigned)((b.s[1].n + blk.y - 1) / blk.y), (unsigned)b.s[0].n);
+      return;
+    }
+    blk = dim3(32, 8, 1);
+    g = dim3((unsigned)((b.s[2].n + 31) / 32), (unsigned)((b.s[1].n + 7) / 8), (unsigned)b.s[0].n);
+  }
+
+  template <bool FX, bool FY> void launch_b_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp) {
+    dim3 g, blk;
+    band_shape(bd, g, blk);
+    if (g.x == 0) return;
+    if (cnd && zp) b3_band_kernel<R, true, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
+    else if (cnd) b3_band_kernel<R, true, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
+    else if (zp) b3_band_kernel<R, false, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
+    else b3_band_kernel<R, false, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
+    nlaunch++;
+  }
+  template <bool FX, bool FY, bool POLES>
+  void launch_de_band_p(const Band &bd, const dim3 &g, const dim3 &blk, const FusedArgs<R> &a, bool cnd, bool zp) {
+    if (cnd && zp) de3_band_kernel<R, true, POLES, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
+    else if (cnd) de3_band_kernel<R, true, POLES, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
+    else if (zp) de3_band_kernel<R, false, POLES, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
+    else de3_band_kernel<R, false, POLES, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
+  }
+  template <bool FX, bool FY> void launch_de_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp) {
+    dim3 g, blk;
+    band_shape(bd, g, blk);
+    if (g.x == 0) return;
+    if (a.npoles > 0) launch_de_band_p<FX, FY, true>(bd, g, blk, a, cnd, zp);
+    else launch_de_band_p<FX, FY, false>(bd, g, blk, a, cnd, zp);
+    nlaunch++;
+  }
+
+  dim3 core_grid() const {
+    const int nz = qcore.zend - qcore.lo[2];
+    if (qcore.n[0] <= 0 || qcore.n[1] <= 0 || nz <= 0) return dim3(0, 0, 0);
+    return dim3((unsigned)((nz / 4 + 31) / 32), (unsigned)((qcore.n[1] + 7) / 8), (unsigned)qcore.n[0]);
+  }
+
   static void add_box(BoxList &L, const int lo[3], const int hi[3], int dim, dim3 blk) {
     int ext[3];
     for (int d = 0; d < 3; d++) {
@@ -813,6 +883,29 @@ public:
     }
     box_int = BoxList{};
     box_bnd = BoxList{};
+    if (dim == 3) {
+      int xlo = p.T[0][0] + 1, xhi = p.N[0] - p.T[0][1] - 1, ylo = p.T[1][0] + 1, yhi = p.N[1] - p.T[1][1] - 1;
+      xlo = std::min(xlo, p.N[0]);
+      ylo = std::min(ylo, p.N[1]);
+      xhi = std::max(xhi, xlo - 1);
+      yhi = std::max(yhi, ylo - 1);
+      band_rows = Band{{span_run(xlo, xhi), span_run(ylo, yhi), span_run(0, p.N[2] - 1)}};
+      band_x = Band{{span_outside(p.N[0], xlo, xhi), span_run(0, p.N[1] - 1), span_run(0, p.N[2] - 1)}};
+      band_y = Band{{span_run(xlo, xhi), span_outside(p.N[1], ylo, yhi), span_run(0, p.N[2] - 1)}};
+      // the B core: z interior (no slab, off the low wall) rounded inwards to quads
+      qcore = QCore{};
+      qcore.lo[0] = xlo;
+      qcore.lo[1] = ylo;
+      qcore.n[0] = xhi - xlo + 1;
+      qcore.n[1] = yhi - ylo + 1;
+      qcore.lo[2] = (std::max(p.T[2][0] + 1, 1) + 3) / 4 * 4;
+      qcore.zend = std::max((p.N[2] - p.T[2][1]) / 4 * 4, qcore.lo[2]);
+      band_zend = Band{{span_run(xlo, xhi), span_run(ylo, yhi),
+                        qcore.zend > qcore.lo[2] ? span_outside(p.N[2], qcore.lo[2], qcore.zend - 1)
+                                                 : span_run(0, p.N[2] - 1)}};
+      check_bands(p);
+      return;
+    }
     add_box(box_int, ilo, ihi, dim, fblock);
     // shell around the interior: slabs peeled off direction by direction
     int lo[3], hi[3], clo[3], chi_[3];
@@ -834,12 +927,62 @@ public:
       clo[d] = ilo[d];
       chi_[d] = ihi[d];
     }
-    // every box must lie inside the point range 0..N-1 of each direction
+    check_boxes(glo, ghi);
+  }
+
+  // every box must lie inside the point range 0..N-1 of each direction, and
+  // the boxes must cover it exactly once
+  // the 3-D launches must cover points 0..N-1 of every direction exactly once
+  // and stay inside them (rows, x slabs, y slabs)
+  void check_bands(const Plan &p) const {
+    std::vector<unsigned char> seen((size_t)p.N[0] * p.N[1] * p.N[2], 0);
+    auto mark = [&](int k0, int k1, int k2) {
+      if (k0 < 0 || k0 >= p.N[0] || k1 < 0 || k1 >= p.N[1] || k2 < 0 || k2 >= p.N[2])
+        throw Error("internal: launch band outside the grid");
+      seen[((size_t)k0 * p.N[1] + k1) * p.N[2] + k2]++;
+    };
+    auto kof = [](const Span &s, int t) { return t + (t < s.split ? s.a0 : s.a1); };
+    auto band = [&](const Band &b) {
+      for (int t0 = 0; t0 < b.s[0].n; t0++)
+        for (int t1 = 0; t1 < b.s[1].n; t1++)
+          for (int t2 = 0; t2 < b.s[2].n; t2++)
+            mark(kof(b.s[0], t0), kof(b.s[1], t1), kof(b.s[2], t2));
+    };
+    band(band_x);
+    band(band_y);
+    band(band_rows);
+    for (unsigned char v : seen)
+      if (v != 1) throw Error("internal: launch bands do not tile the grid");
+    // the FP32 B update: core + z ends instead of the rows
+    std::fill(seen.begin(), seen.end(), 0);
+    band(band_x);
+    band(band_y);
+    band(band_zend);
+    for (int t0 = 0; t0 < qcore.n[0]; t0++)
+      for (int t1 = 0; t1 < qcore.n[1]; t1++)
+        for (int k2 = qcore.lo[2]; k2 < qcore.zend; k2++)
+          mark(qcore.lo[0] + t0, qcore.lo[1] + t1, k2);
+    if (qcore.zend > qcore.lo[2] && (qcore.lo[2] % 4 || qcore.zend % 4 || qcore.lo[2] < 1 || qcore.zend > p.N[2]))
+      throw Error("internal: quad core not aligned");
+    for (unsigned char v : seen)
+      if (v != 1) throw Error("internal: launch bands do not tile the grid");
+  }
+
+  void check_boxes(const int glo[3], const int ghi[3]) const {
+    long long total = 1, covered = 0;
+    for (int d = 0; d < 3; d++)
+      total *= ghi[d] - glo[d] + 1;
     for (const BoxList *L : {&box_int, &box_bnd})
-      for (int q = 0; q < L->n; q++)
-        for (int d = 0; d < 3; d++)
+      for (int q = 0; q < L->n; q++) {
+        long long v = 1;
+        for (int d = 0; d < 3; d++) {
           if (L->lo[q][d] < glo[d] || L->lo[q][d] + L->ext[q][d] - 1 > ghi[d])
             throw Error("internal: launch box outside the grid");
+          v *= L->ext[q][d];
+        }
+        covered += v;
+      }
+    if (covered != total) throw Error("internal: launch boxes do not tile the grid");
   }
 
   template <int DIM, int MASK>
@@ -847,28 +990,32 @@ public:
     FusedArgs<R> a = fused_args(p, !has_b_current);
     const bool cndB = a.cnd[3][0] || a.cnd[3][1] || a.cnd[3][2];
     const bool cndD = a.cnd[2][0] || a.cnd[2][1] || a.cnd[2][2];
-    IBox ib{};
-    for (int d = 0; d < 3; d++) {
-      ib.lo[d] = box_int.lo[0][d];
-      ib.n[d] = box_int.ext[0][d];
+    const bool zp = a.pml[2] != 0;
+    constexpr bool F32 = std::is_same<R, float>::value;
+    if constexpr (DIM == 3) {
+      if constexpr (F32) {
+        const dim3 g = core_grid();
+        if (g.x) {
+          if (cndB) b3q_core_kernel<true><<<g, dim3(32, 8, 1), 0, stream>>>(a, qcore);
+          else b3q_core_kernel<false><<<g, dim3(32, 8, 1), 0, stream>>>(a, qcore);
+          nlaunch++;
+        }
+        launch_b_band<false, false>(band_zend, a, cndB, zp);
+      }
+      else
+        launch_b_band<false, false>(band_rows, a, cndB, zp);
+      launch_b_band<true, true>(band_x, a, cndB, zp);
+      launch_b_band<false, true>(band_y, a, cndB, zp);
     }
-    dim3 igrid((ib.n[2] + 31) / 32, (ib.n[1] + 7) / 8, ib.n[0]);
-    if (box_int.n && DIM == 3) {
-      if (cndB) b3_interior_kernel<R, true><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
-      else b3_interior_kernel<R, false><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
-      nlaunch++;
-    }
-    else if (box_int.n) {
-      fused_b_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
-      nlaunch++;
-    }
-    if (box_bnd.n && DIM == 3) {
-      b3_shell_kernel<R><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
-      nlaunch++;
-    }
-    else if (box_bnd.n) {
-      fused_b_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
-      nlaunch++;
+    else {
+      if (box_int.n) {
+        fused_b_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
+        nlaunch++;
+      }
+      if (box_bnd.n) {
+        fused_b_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
+        nlaunch++;
+      }
     }
     if (has_b_current) {
       step_current(p, MFD_B, curb);
@@ -894,25 +1041,20 @@ public:
             a, d_srcpts[d], nsrcpts[d], d, dip, d_fsrcbuf[d]);
         nlaunch++;
       }
-    if (box_int.n && DIM == 3) {
-      const bool pl = a.npoles > 0;
-      if (cndD && pl) de3_interior_kernel<R, true, true><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
-      else if (cndD) de3_interior_kernel<R, true, false><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
-      else if (pl) de3_interior_kernel<R, false, true><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
-      else de3_interior_kernel<R, false, false><<<igrid, dim3(32, 8, 1), 0, stream>>>(a, ib);
-      nlaunch++;
+    if constexpr (DIM == 3) {
+      launch_de_band<false, false>(band_rows, a, cndD, zp);
+      launch_de_band<true, true>(band_x, a, cndD, zp);
+      launch_de_band<false, true>(band_y, a, cndD, zp);
     }
-    else if (box_int.n) {
-      fused_de_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
-      nlaunch++;
-    }
-    if (box_bnd.n && DIM == 3) {
-      de3_shell_kernel<R><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
-      nlaunch++;
-    }
-    else if (box_bnd.n) {
-      fused_de_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
-      nlaunch++;
+    else {
+      if (box_int.n) {
+        fused_de_kernel<R, DIM, MASK, true><<<box_int.blk0[box_int.n], fblock, 0, stream>>>(a, box_int);
+        nlaunch++;
+      }
+      if (box_bnd.n) {
+        fused_de_kernel<R, DIM, MASK, false><<<box_bnd.blk0[box_bnd.n], fblock, 0, stream>>>(a, box_bnd);
+        nlaunch++;
+      }
     }
     for (int d = 0; d < 3; d++)
       if (nsrcpts[d]) {

@@ -1,133 +1,29 @@
-// Hand-written 3-D interior kernels.  The interior box holds only points of
-// the reference's interior chunk (no PML slab, no metal wall, H == B), so the
-// updates are the plain branches of step_curl (src/step_generic.cpp:94-113)
-// and step_update_EDHB (src/step_generic.cpp:769-777) plus the Lorentzian
-// recurrence (src/susceptibility.cpp:249-255), with the operands spelled out:
-//   B -= dtdx * curl E     (forward differences, strides +)
-//   D -= dtdx * curl' H    (backward differences, strides negated)
-//   E  = chi1inv * (D - sum P);  P, P_prev <- Lorentz/Drude update with W = E
-// Grid: blockIdx.x,y tile z (32) and y (8), blockIdx.z is the x plane.
+// Hand-written 3-D one-point kernels over bands of the grid.  A band is a
+// box whose x, y and z ranges are either a contiguous run or the two slabs
+// outside an interior run; the launch maps blockIdx.z to x, blockIdx.y and
+// threadIdx.y to y, blockIdx.x and threadIdx.x to z (unit stride), so every
+// warp is a run of consecutive z points of one row.
+//
+// The per-point code takes the general branches of step_curl /
+// step_update_EDHB; each component's branch is chosen from the chunk region
+// of its own Yee position, exactly as the reference picks dsig / dsigu /
+// dsigw per chunk (src/step_db.cpp:54-60, src/update_eh.cpp:159-160).  The
+// band kernels are templated on which directions can hold PML slab points:
+// for the others the flags are compile-time "interior" and their branches
+// vanish.
 #pragma once
 
 namespace mfd {
 namespace cuda_impl {
 
-struct IBox {
-  int lo[3], n[3];
+// k = t + (t < split ? a0 : a1) for t < n: a contiguous run (split = n) or
+// the two slabs around an interior run
+struct Span {
+  int n, split, a0, a1;
 };
-
-template <typename R, bool CND>
-__global__ void __launch_bounds__(256) b3_interior_kernel(const FusedArgs<R> a, const IBox b) {
-  const int k2 = b.lo[2] + blockIdx.x * 32 + threadIdx.x;
-  const int k1 = b.lo[1] + blockIdx.y * 8 + threadIdx.y;
-  const int k0 = b.lo[0] + blockIdx.z;
-  if (k2 >= b.lo[2] + b.n[2] || k1 >= b.lo[1] + b.n[1]) return;
-  const int sx = a.s[0], sy = a.s[1];
-  const int i = k0 * sx + k1 * sy + k2;
-  const R *__restrict__ Ex = a.e[0];
-  const R *__restrict__ Ey = a.e[1];
-  const R *__restrict__ Ez = a.e[2];
-  const R ex = Ex[i], exy = Ex[i + sy], exz = Ex[i + 1];
-  const R ey = Ey[i], eyx = Ey[i + sx], eyz = Ey[i + 1];
-  const R ez = Ez[i], ezx = Ez[i + sx], ezy = Ez[i + sy];
-  const R bx = a.b[0][i], by = a.b[1][i], bz = a.b[2][i];
-  const R Xx = (ezy - ez) + ey - eyz;
-  const R Xy = (exz - ex) + ez - ezx;
-  const R Xz = (eyx - ey) + ex - exy;
-  const R dtdx = a.dtdx;
-  R nbx, nby, nbz;
-  if (CND) {
-    const R one = R(1);
-    nbx = a.cnd[3][0] ? ((one - a.dt2 * a.cnd[3][0][i]) * bx - dtdx * Xx) * a.cndinv[3][0][i] : bx - dtdx * Xx;
-    nby = a.cnd[3][1] ? ((one - a.dt2 * a.cnd[3][1][i]) * by - dtdx * Xy) * a.cndinv[3][1][i] : by - dtdx * Xy;
-    nbz = a.cnd[3][2] ? ((one - a.dt2 * a.cnd[3][2][i]) * bz - dtdx * Xz) * a.cndinv[3][2][i] : bz - dtdx * Xz;
-  }
-  else {
-    nbx = bx - dtdx * Xx;
-    nby = by - dtdx * Xy;
-    nbz = bz - dtdx * Xz;
-  }
-  a.b[0][i] = nbx;
-  a.b[1][i] = nby;
-  a.b[2][i] = nbz;
-}
-
-template <typename R>
-__device__ __forceinline__ R e_from_d(const FusedArgs<R> &a, int dc, int i, R dn, int npoles) {
-  R gs = dn;
-  for (int q = 0; q < npoles; q++)
-    if (a.P[q][dc]) gs -= a.P[q][dc][i];
-  const R e = gs * a.chi[dc][i];
-  for (int q = 0; q < npoles; q++)
-    if (a.P[q][dc]) {
-      const R pcur = a.P[q][dc][i];
-      a.P[q][dc][i] = a.pg1inv[q] * (pcur * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][dc][i] +
-                                     a.pw0[q] * (a.ps[q][dc][i] * e));
-      a.PP[q][dc][i] = pcur;
-    }
-  return e;
-}
-
-template <typename R, bool CND, bool POLES>
-__global__ void __launch_bounds__(256) de3_interior_kernel(const FusedArgs<R> a, const IBox b) {
-  const int k2 = b.lo[2] + blockIdx.x * 32 + threadIdx.x;
-  const int k1 = b.lo[1] + blockIdx.y * 8 + threadIdx.y;
-  const int k0 = b.lo[0] + blockIdx.z;
-  if (k2 >= b.lo[2] + b.n[2] || k1 >= b.lo[1] + b.n[1]) return;
-  const int sx = a.s[0], sy = a.s[1];
-  const int i = k0 * sx + k1 * sy + k2;
-  const R *__restrict__ Hx = a.b[0]; // H == B in the interior chunk
-  const R *__restrict__ Hy = a.b[1];
-  const R *__restrict__ Hz = a.b[2];
-  const R hx = Hx[i], hxy = Hx[i - sy], hxz = Hx[i - 1];
-  const R hy = Hy[i], hyx = Hy[i - sx], hyz = Hy[i - 1];
-  const R hz = Hz[i], hzx = Hz[i - sx], hzy = Hz[i - sy];
-  const R dx = a.d[0][i], dy = a.d[1][i], dz = a.d[2][i];
-  const R cx = a.chi[0][i], cy = a.chi[1][i], cz = a.chi[2][i];
-  const R Xx = (hzy - hz) + hy - hyz;
-  const R Xy = (hxz - hx) + hz - hzx;
-  const R Xz = (hyx - hy) + hx - hxy;
-  const R dtdx = a.dtdx;
-  R ndx, ndy, ndz;
-  if (CND) {
-    const R one = R(1);
-    ndx = a.cnd[2][0] ? ((one - a.dt2 * a.cnd[2][0][i]) * dx - dtdx * Xx) * a.cndinv[2][0][i] : dx - dtdx * Xx;
-    ndy = a.cnd[2][1] ? ((one - a.dt2 * a.cnd[2][1][i]) * dy - dtdx * Xy) * a.cndinv[2][1][i] : dy - dtdx * Xy;
-    ndz = a.cnd[2][2] ? ((one - a.dt2 * a.cnd[2][2][i]) * dz - dtdx * Xz) * a.cndinv[2][2][i] : dz - dtdx * Xz;
-  }
-  else {
-    ndx = dx - dtdx * Xx;
-    ndy = dy - dtdx * Xy;
-    ndz = dz - dtdx * Xz;
-  }
-  a.d[0][i] = ndx;
-  a.d[1][i] = ndy;
-  a.d[2][i] = ndz;
-  if (POLES) {
-    a.e[0][i] = e_from_d(a, 0, i, ndx, a.npoles);
-    a.e[1][i] = e_from_d(a, 1, i, ndy, a.npoles);
-    a.e[2][i] = e_from_d(a, 2, i, ndz, a.npoles);
-  }
-  else {
-    a.e[0][i] = ndx * cx;
-    a.e[1][i] = ndy * cy;
-    a.e[2][i] = ndz * cz;
-  }
-}
-
-} // namespace cuda_impl
-} // namespace mfd
-
-namespace mfd {
-namespace cuda_impl {
-
-// ------------------------------------------------------------ PML shell
-// Points of the shell (PML slabs, metal walls, chunk boundaries) take the
-// general branches of step_curl / step_update_EDHB.  Each component's branch
-// is chosen from the chunk region of its own Yee position, exactly as the
-// reference picks dsig / dsigu / dsigw per chunk (src/step_db.cpp:54-60,
-// src/update_eh.cpp:159-160).  Loads of every component are issued before any
-// store.
+struct Band {
+  Span s[3];
+};
 
 template <typename R> struct CurlRes {
   R f, fu, fc;
@@ -192,14 +88,35 @@ template <typename R> struct ShellFlags {
   bool s0[3], s1[3];
 };
 
-template <typename R> __device__ __forceinline__ void shell_flags(const FusedArgs<R> &a, const int k[3], ShellFlags<R> &f) {
+// flags of the directions that can hold slab points (FX, FY, FZ); the others
+// are interior: middle chunk region, no slab
+template <typename R, bool FX, bool FY, bool FZ>
+__device__ __forceinline__ void band_flags(const FusedArgs<R> &a, const int k[3], ShellFlags<R> &f) {
+  constexpr bool fl[3] = {FX, FY, FZ};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    f.r0[d] = fregion(a, d, 2 * k[d]);
-    f.r1[d] = fregion(a, d, 2 * k[d] + 1);
-    f.s0[d] = a.pml[d] && f.r0[d] != 1;
-    f.s1[d] = a.pml[d] && f.r1[d] != 1;
+    if (fl[d]) {
+      f.r0[d] = fregion(a, d, 2 * k[d]);
+      f.r1[d] = fregion(a, d, 2 * k[d] + 1);
+      f.s0[d] = a.pml[d] && f.r0[d] != 1;
+      f.s1[d] = a.pml[d] && f.r1[d] != 1;
+    }
+    else {
+      f.r0[d] = f.r1[d] = 1;
+      f.s0[d] = f.s1[d] = false;
+    }
   }
+}
+
+// point of this thread; false past the end of the band
+__device__ __forceinline__ bool band_coords(const Band &bd, int k[3]) {
+  const int t[3] = {(int)blockIdx.z, (int)(blockIdx.y * blockDim.y + threadIdx.y),
+                    (int)(blockIdx.x * blockDim.x + threadIdx.x)};
+  if (t[1] >= bd.s[1].n || t[2] >= bd.s[2].n) return false;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    k[d] = t[d] + (t[d] < bd.s[d].split ? bd.s[d].a0 : bd.s[d].a1);
+  return true;
 }
 
 // does the chunk holding this component position carry a conductivity array
@@ -207,14 +124,14 @@ __device__ __forceinline__ bool chunk_has(unsigned mask, int rx, int ry, int rz)
   return (mask >> (rx * 9 + ry * 3 + rz)) & 1u;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) b3_shell_kernel(const FusedArgs<R> a, const BoxList L) {
-  int k[3];
-  if (!box_coords<3>(L, k)) return;
+// B -= dtdx * curl E with PML / conductivity branches, then H inside the
+// slab along its own direction (update_eh through f_w)
+template <typename R, bool CND, bool FX, bool FY, bool FZ>
+__device__ __forceinline__ void b3_point(const FusedArgs<R> &a, const int k[3]) {
   const int sx = a.s[0], sy = a.s[1];
   const int i = k[0] * sx + k[1] * sy + k[2];
   ShellFlags<R> F;
-  shell_flags(a, k, F);
+  band_flags<R, FX, FY, FZ>(a, k, F);
   // the low wall point (k = 0) of a component with shift 0 is not advanced
   const bool vx = k[0] >= 1, vy = k[1] >= 1, vz = k[2] >= 1;
   const R *Ex = a.e[0], *Ey = a.e[1], *Ez = a.e[2];
@@ -228,7 +145,7 @@ __global__ void __launch_bounds__(256) b3_shell_kernel(const FusedArgs<R> a, con
   const R dtdx = a.dtdx, dt2 = a.dt2;
   const int p0x = 2 * k[0], p1x = p0x + 1, p0y = 2 * k[1], p1y = p0y + 1, p0z = 2 * k[2], p1z = p0z + 1;
   // Bx at (0,1,1): dsig = Y, dsigu = Z
-  bool hcx = a.cnd[3][0] != nullptr, hcy = a.cnd[3][1] != nullptr, hcz = a.cnd[3][2] != nullptr;
+  bool hcx = CND && a.cnd[3][0] != nullptr, hcy = CND && a.cnd[3][1] != nullptr, hcz = CND && a.cnd[3][2] != nullptr;
   if (hcx && F.s1[1]) hcx = chunk_has(a.cond_chunks[3][0], F.r0[0], F.r1[1], F.r1[2]);
   if (hcy && F.s1[2]) hcy = chunk_has(a.cond_chunks[3][1], F.r1[0], F.r0[1], F.r1[2]);
   if (hcz && F.s1[0]) hcz = chunk_has(a.cond_chunks[3][2], F.r1[0], F.r1[1], F.r0[2]);
@@ -295,15 +212,24 @@ __global__ void __launch_bounds__(256) b3_shell_kernel(const FusedArgs<R> a, con
 template <typename R> struct EShell {
   R e, fw;
   bool wfw;
+  R pn[MAX_POLES], pc[MAX_POLES]; // new and current P of each pole
 };
 
-template <typename R>
+// everything loaded and computed, nothing stored (so the loads of all three
+// components are in flight together)
+template <typename R, bool POLES>
 __device__ __forceinline__ EShell<R> e_general(const FusedArgs<R> &a, int dc, int i, R dn, bool slabw, int pw) {
-  R gs = dn;
-  for (int q = 0; q < a.npoles; q++)
-    if (a.P[q][dc]) gs -= a.P[q][dc][i];
-  const R us = a.chi[dc][i];
   EShell<R> o;
+  R gs = dn;
+  if (POLES) {
+#pragma unroll
+    for (int q = 0; q < MAX_POLES; q++)
+      if (q < a.npoles && a.P[q][dc]) {
+        o.pc[q] = a.P[q][dc][i];
+        gs -= o.pc[q];
+      }
+  }
+  const R us = a.chi[dc][i];
   R W;
   if (slabw) {
     const R fwprev = a.fw[0][dc][i], kk = a.kap[dc][pw], ss = a.sig[dc][pw];
@@ -319,24 +245,36 @@ __device__ __forceinline__ EShell<R> e_general(const FusedArgs<R> &a, int dc, in
     o.wfw = false;
     W = o.e;
   }
-  for (int q = 0; q < a.npoles; q++)
-    if (a.P[q][dc]) {
-      const R pcur = a.P[q][dc][i];
-      a.P[q][dc][i] = a.pg1inv[q] * (pcur * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][dc][i] +
-                                     a.pw0[q] * (a.ps[q][dc][i] * W));
-      a.PP[q][dc][i] = pcur;
-    }
+  if (POLES) {
+#pragma unroll
+    for (int q = 0; q < MAX_POLES; q++)
+      if (q < a.npoles && a.P[q][dc])
+        o.pn[q] = a.pg1inv[q] * (o.pc[q] * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][dc][i] +
+                                 a.pw0[q] * (a.ps[q][dc][i] * W));
+  }
   return o;
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) de3_shell_kernel(const FusedArgs<R> a, const BoxList L) {
-  int k[3];
-  if (!box_coords<3>(L, k)) return;
+template <typename R, bool POLES>
+__device__ __forceinline__ void e_store(const FusedArgs<R> &a, int dc, int i, const EShell<R> &o) {
+  a.e[dc][i] = o.e;
+  if (o.wfw) a.fw[0][dc][i] = o.fw;
+  if (POLES) {
+#pragma unroll
+    for (int q = 0; q < MAX_POLES; q++)
+      if (q < a.npoles && a.P[q][dc]) {
+        a.P[q][dc][i] = o.pn[q];
+        a.PP[q][dc][i] = o.pc[q];
+      }
+  }
+}
+
+template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
+__device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3]) {
   const int sx = a.s[0], sy = a.s[1];
   const int i = k[0] * sx + k[1] * sy + k[2];
   ShellFlags<R> F;
-  shell_flags(a, k, F);
+  band_flags<R, FX, FY, FZ>(a, k, F);
   // D components sit at shift 1 along their own direction, 0 elsewhere:
   // Dx (1,0,0) needs k_y, k_z >= 1; Dy needs k_x, k_z >= 1; Dz needs k_x, k_y >= 1
   const bool vx = k[1] >= 1 && k[2] >= 1, vy = k[0] >= 1 && k[2] >= 1, vz = k[0] >= 1 && k[1] >= 1;
@@ -358,7 +296,7 @@ __global__ void __launch_bounds__(256) de3_shell_kernel(const FusedArgs<R> a, co
   const R Xz = (hyx - hy) + hx - hxy;
   const R dtdx = a.dtdx, dt2 = a.dt2;
   const int p0x = 2 * k[0], p1x = p0x + 1, p0y = 2 * k[1], p1y = p0y + 1, p0z = 2 * k[2], p1z = p0z + 1;
-  bool hcx = a.cnd[2][0] != nullptr, hcy = a.cnd[2][1] != nullptr, hcz = a.cnd[2][2] != nullptr;
+  bool hcx = CND && a.cnd[2][0] != nullptr, hcy = CND && a.cnd[2][1] != nullptr, hcz = CND && a.cnd[2][2] != nullptr;
   // Dx (1,0,0): dsig = Y (shift 0), dsigu = Z (shift 0)
   if (hcx && F.s0[1]) hcx = chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]);
   // Dy (0,1,0): dsig = Z, dsigu = X
@@ -374,31 +312,68 @@ __global__ void __launch_bounds__(256) de3_shell_kernel(const FusedArgs<R> a, co
   const CurlRes<R> cz = curl_general(dz, Xz, dtdx, dt2, F.s0[0], F.s0[1], hcz, a.sig[0], a.kap[0], a.siginv[0], p0x,
                                      a.sig[1], a.kap[1], a.siginv[1], p0y, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2],
                                      a.cndinv[2][2], i);
-  // E components share the D positions: f_w slab along their own direction at shift 1
+  // E components share the D positions: f_w slab along their own direction at
+  // shift 1.  Without poles all loads go first, then the stores; with poles
+  // (four more arrays per pole and component) one component after the other
+  // keeps the registers, and so the occupancy, in bounds.
+  EShell<R> ox, oy, oz;
+  if constexpr (POLES) {
+    if (vx) {
+      ox = e_general<R, POLES>(a, 0, i, cx.f, F.s1[0], p1x);
+      a.d[0][i] = cx.f;
+      if (cx.wfu) a.fu[2][0][i] = cx.fu;
+      if (cx.wfc) a.fcnd[2][0][i] = cx.fc;
+      e_store<R, POLES>(a, 0, i, ox);
+    }
+    if (vy) {
+      oy = e_general<R, POLES>(a, 1, i, cy.f, F.s1[1], p1y);
+      a.d[1][i] = cy.f;
+      if (cy.wfu) a.fu[2][1][i] = cy.fu;
+      if (cy.wfc) a.fcnd[2][1][i] = cy.fc;
+      e_store<R, POLES>(a, 1, i, oy);
+    }
+    if (vz) {
+      oz = e_general<R, POLES>(a, 2, i, cz.f, F.s1[2], p1z);
+      a.d[2][i] = cz.f;
+      if (cz.wfu) a.fu[2][2][i] = cz.fu;
+      if (cz.wfc) a.fcnd[2][2][i] = cz.fc;
+      e_store<R, POLES>(a, 2, i, oz);
+    }
+    return;
+  }
+  if (vx) ox = e_general<R, POLES>(a, 0, i, cx.f, F.s1[0], p1x);
+  if (vy) oy = e_general<R, POLES>(a, 1, i, cy.f, F.s1[1], p1y);
+  if (vz) oz = e_general<R, POLES>(a, 2, i, cz.f, F.s1[2], p1z);
   if (vx) {
-    const EShell<R> ox = e_general(a, 0, i, cx.f, F.s1[0], p1x);
     a.d[0][i] = cx.f;
     if (cx.wfu) a.fu[2][0][i] = cx.fu;
     if (cx.wfc) a.fcnd[2][0][i] = cx.fc;
-    a.e[0][i] = ox.e;
-    if (ox.wfw) a.fw[0][0][i] = ox.fw;
+    e_store<R, POLES>(a, 0, i, ox);
   }
   if (vy) {
-    const EShell<R> oy = e_general(a, 1, i, cy.f, F.s1[1], p1y);
     a.d[1][i] = cy.f;
     if (cy.wfu) a.fu[2][1][i] = cy.fu;
     if (cy.wfc) a.fcnd[2][1][i] = cy.fc;
-    a.e[1][i] = oy.e;
-    if (oy.wfw) a.fw[0][1][i] = oy.fw;
+    e_store<R, POLES>(a, 1, i, oy);
   }
   if (vz) {
-    const EShell<R> oz = e_general(a, 2, i, cz.f, F.s1[2], p1z);
     a.d[2][i] = cz.f;
     if (cz.wfu) a.fu[2][2][i] = cz.fu;
     if (cz.wfc) a.fcnd[2][2][i] = cz.fc;
-    a.e[2][i] = oz.e;
-    if (oz.wfw) a.fw[0][2][i] = oz.fw;
+    e_store<R, POLES>(a, 2, i, oz);
   }
+}
+
+template <typename R, bool CND, bool FX, bool FY, bool FZ>
+__global__ void __launch_bounds__(256) b3_band_kernel(const FusedArgs<R> a, const Band bd) {
+  int k[3];
+  if (band_coords(bd, k)) b3_point<R, CND, FX, FY, FZ>(a, k);
+}
+
+template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
+__global__ void __launch_bounds__(256) de3_band_kernel(const FusedArgs<R> a, const Band bd) {
+  int k[3];
+  if (band_coords(bd, k)) de3_point<R, CND, POLES, FX, FY, FZ>(a, k);
 }
 
 } // namespace cuda_impl

@@ -70,14 +70,15 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
-                   nsrc=3, steps=60):
+                   nsrc=3, steps=60, n=None):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
     arrays on a small grid with PML; integrated E sources at random points and
     a current source; two DFT monitors.  Returns dict of field arrays and DFT
-    sums after `steps` steps."""
+    sums after `steps` steps; `n` overrides the random grid size."""
     rng = np.random.default_rng(seed)
+    nrand = n
     if dim == 2:
         n = (int(rng.integers(28, 40)), int(rng.integers(24, 36)), 0)
         comps = [_lib.comp(_lib.E, _lib.Z), _lib.comp(_lib.D, _lib.Z), _lib.comp(_lib.H, _lib.X),
@@ -85,6 +86,8 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     else:
         n = (int(rng.integers(18, 24)), int(rng.integers(16, 22)), int(rng.integers(14, 20)))
         comps = [_lib.comp(t, d) for t in range(4) for d in range(3)]
+    if nrand is not None:
+        n = tuple(nrand)
     io = [-(n[d] - n[d] % 2) for d in range(3)]
     a = 10.0
     pmlspec = {}

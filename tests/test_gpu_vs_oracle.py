@@ -10,9 +10,9 @@ from meep_gb300 import _lib
 pytestmark = pytest.mark.gpu
 
 
-def _run(lib, seed, dim, prec):
+def _run(lib, seed, dim, prec, **kw):
     eng = _lib.Engine(lib)
-    return random_problem(lambda **kw: _lib.Sim(eng, **kw), seed, dim, precision=prec)
+    return random_problem(lambda **k: _lib.Sim(eng, **k), seed, dim, precision=prec, **kw)
 
 
 @pytest.mark.parametrize("dim", [2, 3])
@@ -30,3 +30,17 @@ def test_fp32_close(dim, engine_lib, oracle_lib):
     o = _run(oracle_lib, 7, dim, 64)
     for k in o:
         assert relerr(g[k], o[k]) <= 1e-3, (k, relerr(g[k], o[k]))
+
+
+# FP32 engine against the FP32 oracle (same arithmetic, rounding differs only
+# by fused multiply-adds): a wrong branch at any PML, wall, conductivity or
+# pole point shows up as an O(1) error.  The long-z grids span several warps
+# of four-point quads along the unit-stride axis, with rows whose length is
+# not a multiple of four.
+@pytest.mark.parametrize("seed,n", [(11, None), (12, None), (13, (18, 16, 141)), (14, (16, 17, 262)),
+                                    (15, (13, 11, 130))])
+def test_fp32_matches_fp32_oracle(seed, n, engine_lib, oracle_lib):
+    g = _run(engine_lib, seed, 3, 32, n=n)
+    o = _run(oracle_lib, seed, 3, 32, n=n)
+    for k in o:
+        assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
