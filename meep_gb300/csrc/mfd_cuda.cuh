@@ -540,6 +540,11 @@ public:
     cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
     cuda_check(cudaEventCreate(&ev0), "event");
     cuda_check(cudaEventCreate(&ev1), "event");
+    for (int q = 0; q < NSIDE; q++) {
+      cuda_check(cudaStreamCreateWithFlags(&side[q], cudaStreamNonBlocking), "stream");
+      cuda_check(cudaEventCreateWithFlags(&side_ev[q], cudaEventDisableTiming), "event");
+    }
+    cuda_check(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming), "event");
     (void)p;
   }
   ~CudaBackend() override {
@@ -547,11 +552,33 @@ public:
       cudaFree(ptr);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
+    for (int q = 0; q < NSIDE; q++) {
+      cudaEventDestroy(side_ev[q]);
+      cudaStreamDestroy(side[q]);
+    }
+    cudaEventDestroy(fork_ev);
     cudaStreamDestroy(stream);
   }
 
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // side streams: the launches of one half-step touch disjoint points, so
+  // they run side by side (filling each other's tail waves) and join the main
+  // stream before the next half-step
+  static constexpr int NSIDE = 3;
+  cudaStream_t side[NSIDE] = {};
+  cudaEvent_t side_ev[NSIDE] = {}, fork_ev = nullptr;
+  void fork() {
+    cuda_check(cudaEventRecord(fork_ev, stream), "event record");
+    for (int q = 0; q < NSIDE; q++)
+      cuda_check(cudaStreamWaitEvent(side[q], fork_ev, 0), "stream wait");
+  }
+  void join() {
+    for (int q = 0; q < NSIDE; q++) {
+      cuda_check(cudaEventRecord(side_ev[q], side[q]), "event record");
+      cuda_check(cudaStreamWaitEvent(stream, side_ev[q], 0), "stream wait");
+    }
+  }
   std::vector<void *> allocs;
   Geo geo{};
   Tables<R> tb{};
@@ -808,29 +835,32 @@ public:
     g = dim3((unsigned)((b.s[2].n + 31) / 32), (unsigned)((b.s[1].n + 7) / 8), (unsigned)b.s[0].n);
   }
 
-  template <bool FX, bool FY> void launch_b_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp) {
+  template <bool FX, bool FY>
+  void launch_b_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
     dim3 g, blk;
     band_shape(bd, g, blk);
     if (g.x == 0) return;
-    if (cnd && zp) b3_band_kernel<R, true, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
-    else if (cnd) b3_band_kernel<R, true, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
-    else if (zp) b3_band_kernel<R, false, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
-    else b3_band_kernel<R, false, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
+    if (cnd && zp) b3_band_kernel<R, true, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else if (cnd) b3_band_kernel<R, true, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    else if (zp) b3_band_kernel<R, false, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else b3_band_kernel<R, false, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
     nlaunch++;
   }
   template <bool FX, bool FY, bool POLES>
-  void launch_de_band_p(const Band &bd, const dim3 &g, const dim3 &blk, const FusedArgs<R> &a, bool cnd, bool zp) {
-    if (cnd && zp) de3_band_kernel<R, true, POLES, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
-    else if (cnd) de3_band_kernel<R, true, POLES, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
-    else if (zp) de3_band_kernel<R, false, POLES, FX, FY, true><<<g, blk, 0, stream>>>(a, bd);
-    else de3_band_kernel<R, false, POLES, FX, FY, false><<<g, blk, 0, stream>>>(a, bd);
+  void launch_de_band_p(const Band &bd, const dim3 &g, const dim3 &blk, const FusedArgs<R> &a, bool cnd, bool zp,
+                        cudaStream_t st) {
+    if (cnd && zp) de3_band_kernel<R, true, POLES, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else if (cnd) de3_band_kernel<R, true, POLES, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    else if (zp) de3_band_kernel<R, false, POLES, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else de3_band_kernel<R, false, POLES, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
   }
-  template <bool FX, bool FY> void launch_de_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp) {
+  template <bool FX, bool FY>
+  void launch_de_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
     dim3 g, blk;
     band_shape(bd, g, blk);
     if (g.x == 0) return;
-    if (a.npoles > 0) launch_de_band_p<FX, FY, true>(bd, g, blk, a, cnd, zp);
-    else launch_de_band_p<FX, FY, false>(bd, g, blk, a, cnd, zp);
+    if (a.npoles > 0) launch_de_band_p<FX, FY, true>(bd, g, blk, a, cnd, zp, st);
+    else launch_de_band_p<FX, FY, false>(bd, g, blk, a, cnd, zp, st);
     nlaunch++;
   }
 
@@ -993,6 +1023,7 @@ public:
     const bool zp = a.pml[2] != 0;
     constexpr bool F32 = std::is_same<R, float>::value;
     if constexpr (DIM == 3) {
+      fork();
       if constexpr (F32) {
         const dim3 g = core_grid();
         if (g.x) {
@@ -1000,12 +1031,13 @@ public:
           else b3q_core_kernel<false><<<g, dim3(32, 8, 1), 0, stream>>>(a, qcore);
           nlaunch++;
         }
-        launch_b_band<false, false>(band_zend, a, cndB, zp);
+        launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
       }
       else
-        launch_b_band<false, false>(band_rows, a, cndB, zp);
-      launch_b_band<true, true>(band_x, a, cndB, zp);
-      launch_b_band<false, true>(band_y, a, cndB, zp);
+        launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
+      launch_b_band<true, true>(band_x, a, cndB, zp, side[0]);
+      launch_b_band<false, true>(band_y, a, cndB, zp, side[1]);
+      join();
     }
     else {
       if (box_int.n) {
@@ -1042,9 +1074,11 @@ public:
         nlaunch++;
       }
     if constexpr (DIM == 3) {
-      launch_de_band<false, false>(band_rows, a, cndD, zp);
-      launch_de_band<true, true>(band_x, a, cndD, zp);
-      launch_de_band<false, true>(band_y, a, cndD, zp);
+      fork();
+      launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
+      launch_de_band<true, true>(band_x, a, cndD, zp, side[0]);
+      launch_de_band<false, true>(band_y, a, cndD, zp, side[1]);
+      join();
     }
     else {
       if (box_int.n) {
