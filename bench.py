@@ -93,7 +93,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
 
     def __exit__(self, *a):
         if self.proc:
@@ -103,10 +103,14 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
+    def summary(self, window=None):
+        """Median SM clock and active throttle reasons over the samples taken
+        inside `window` (wall-clock seconds of the timed region)."""
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ts, ln in self.lines:
+            if window and not (window[0] <= ts <= window[1] + 0.15):
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -203,7 +207,7 @@ def adjoint_timing():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     args = ap.parse_args()
@@ -249,10 +253,13 @@ def main():
         dist.barrier()
 
     e2e_steps = max(10, args.steps // 4)
-    total = max(FULL_STEPS, args.warmup + args.steps + e2e_steps)
     with ClockSampler(local) as clk:
-        r32 = run_driver(exe32, args.warmup, args.steps, e2e_steps, total)
-    r64 = run_driver(exe64, args.warmup, args.steps, e2e_steps, total)
+        r32 = run_driver(exe32, args.warmup, args.steps, e2e_steps, 0)
+    r64 = run_driver(exe64, args.warmup, args.steps, 0, 0)
+    # the configuration's flux comparison: FULL_STEPS steps from t = 0
+    total = FULL_STEPS
+    f32 = run_driver(exe32, 0, 0, 0, total)
+    f64 = run_driver(exe64, 0, 0, 0, total)
 
     cells = r32["cells"]
     t32 = r32["device_ms"] * 1e-3
@@ -265,7 +272,7 @@ def main():
     value = world * cells * args.steps / t32 / 1e6
     value64 = world * cells * args.steps / t64 / 1e6
     e2e = world * cells * e2e_steps / (r32["e2e_ms"] * 1e-3) / 1e6
-    flux32, flux64 = r32["flux"], r64["flux"]
+    flux32, flux64 = f32["flux"], f64["flux"]
     m = max(abs(x) for x in flux64) or 1.0
     flux_err = max(abs(a - b) for a, b in zip(flux32, flux64)) / m
 
@@ -311,7 +318,7 @@ def main():
                      "algorithmic_bytes_per_step": alg},
         "cpu_baseline": {"value": cpu_val, "unit": "Mcell-updates/s", "cores": cpu_thr, "kind": "port",
                          "sample": cpu_desc},
-        "clocks": clk.summary(),
+        "clocks": clk.summary(r32.get("timed_wall")),
         "adjoint": adj,
     }
     print(json.dumps(line))

@@ -54,9 +54,17 @@ int main(int argc, char **argv) {
   // device-resident timing: one batched call of `steps` steps
   double device_ms = 0;
   long long l0 = f.kernel_launches();
+  // wall-clock bounds of the timed region (seconds since the epoch), so that
+  // clock samples taken by an outside sampler can be matched to it
+  double wall0 = 0, wall1 = 0;
+  auto epoch_s = [] {
+    return std::chrono::duration<double>(std::chrono::system_clock::now().time_since_epoch()).count();
+  };
   if (steps > 0) {
+    wall0 = epoch_s();
     meep::step_n(f, steps);
     device_ms = f.last_step_ms();
+    wall1 = epoch_s();
   }
   long long launches = f.kernel_launches() - l0;
   // end-to-end through the public API: step + flux spectrum to host
@@ -93,8 +101,8 @@ int main(int argc, char **argv) {
   printf("{\"workload\": \"%s\", \"cells\": %.0f, \"realnum_bytes\": %d, \"warmup\": %d, "
          "\"steps\": %d, \"e2e_steps\": %d, \"device_ms\": %.6f, \"e2e_ms\": %.6f, "
          "\"launches\": %lld, \"nfreq\": %d, \"setup_s\": %.3f, \"checksum\": %.17g, \"t\": %d, "
-         "\"flux\": %s}\n",
+         "\"timed_wall\": [%.6f, %.6f], \"flux\": %s}\n",
          name.c_str(), wl->cells(), (int)sizeof(meep::realnum), warm, steps, e2e_steps, device_ms,
-         e2e_ms, launches, wl->nfreq, setup_s, checksum, f.t, flux.c_str());
+         e2e_ms, launches, wl->nfreq, setup_s, checksum, f.t, wall0, wall1, flux.c_str());
   return 0;
 }
