@@ -565,7 +565,7 @@ public:
   // side streams: the launches of one half-step touch disjoint points, so
   // they run side by side (filling each other's tail waves) and join the main
   // stream before the next half-step
-  static constexpr int NSIDE = 3;
+  static constexpr int NSIDE = 6;
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t side_ev[NSIDE] = {}, fork_ev = nullptr;
   void fork() {
@@ -802,7 +802,9 @@ public:
   // 3-D decomposition: rows (x, y interior, all z; z slabs inside the rows),
   // x slabs (all y, all z), y slabs (interior x, all z).  The FP32 B update
   // splits the rows into the core (quads) and the z ends of the rows.
-  Band band_rows{}, band_x{}, band_y{}, band_zend{};
+  // slabs split by how many directions can hold slab points: faces (one) run
+  // the lean single-flag code, edges and corners the general code
+  Band band_rows{}, band_zend{}, band_xface{}, band_yface{}, band_xyedge{}, band_xzedge{}, band_yzedge{};
   QCore qcore{};
 
   static Span span_run(int lo, int hi) {
@@ -835,8 +837,11 @@ public:
     g = dim3((unsigned)((b.s[2].n + 31) / 32), (unsigned)((b.s[1].n + 7) / 8), (unsigned)b.s[0].n);
   }
 
-  template <bool FX, bool FY>
-  void launch_b_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
+  // ZCAN: the band can hold z slab points (the z flags are computed when the
+  // grid has a z PML)
+  template <bool FX, bool FY, bool ZCAN = true>
+  void launch_b_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp_, cudaStream_t st) {
+    const bool zp = ZCAN && zp_;
     dim3 g, blk;
     band_shape(bd, g, blk);
     if (g.x == 0) return;
@@ -854,8 +859,11 @@ public:
     else if (zp) de3_band_kernel<R, false, POLES, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
     else de3_band_kernel<R, false, POLES, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
   }
-  template <bool FX, bool FY>
-  void launch_de_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
+  // ZCAN: the band can hold z slab points (the z flags are computed when the
+  // grid has a z PML)
+  template <bool FX, bool FY, bool ZCAN = true>
+  void launch_de_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp_, cudaStream_t st) {
+    const bool zp = ZCAN && zp_;
     dim3 g, blk;
     band_shape(bd, g, blk);
     if (g.x == 0) return;
@@ -920,8 +928,16 @@ public:
       xhi = std::max(xhi, xlo - 1);
       yhi = std::max(yhi, ylo - 1);
       band_rows = Band{{span_run(xlo, xhi), span_run(ylo, yhi), span_run(0, p.N[2] - 1)}};
-      band_x = Band{{span_outside(p.N[0], xlo, xhi), span_run(0, p.N[1] - 1), span_run(0, p.N[2] - 1)}};
-      band_y = Band{{span_run(xlo, xhi), span_outside(p.N[1], ylo, yhi), span_run(0, p.N[2] - 1)}};
+      int zlo = std::min(p.T[2][0] + 1, p.N[2]), zhi = p.N[2] - p.T[2][1] - 1;
+      zhi = std::max(zhi, zlo - 1);
+      const Span sxr = span_run(xlo, xhi), sxo = span_outside(p.N[0], xlo, xhi);
+      const Span syr = span_run(ylo, yhi), syo = span_outside(p.N[1], ylo, yhi);
+      const Span szr = span_run(zlo, zhi), szo = span_outside(p.N[2], zlo, zhi), sza = span_run(0, p.N[2] - 1);
+      band_xface = Band{{sxo, syr, szr}};
+      band_yface = Band{{sxr, syo, szr}};
+      band_xyedge = Band{{sxo, syo, sza}};
+      band_xzedge = Band{{sxo, syr, szo}};
+      band_yzedge = Band{{sxr, syo, szo}};
       // the B core: z interior (no slab, off the low wall) rounded inwards to quads
       qcore = QCore{};
       qcore.lo[0] = xlo;
@@ -978,15 +994,20 @@ public:
           for (int t2 = 0; t2 < b.s[2].n; t2++)
             mark(kof(b.s[0], t0), kof(b.s[1], t1), kof(b.s[2], t2));
     };
-    band(band_x);
-    band(band_y);
+    auto slabs = [&] {
+      band(band_xface);
+      band(band_yface);
+      band(band_xyedge);
+      band(band_xzedge);
+      band(band_yzedge);
+    };
+    slabs();
     band(band_rows);
     for (unsigned char v : seen)
       if (v != 1) throw Error("internal: launch bands do not tile the grid");
     // the FP32 B update: core + z ends instead of the rows
     std::fill(seen.begin(), seen.end(), 0);
-    band(band_x);
-    band(band_y);
+    slabs();
     band(band_zend);
     for (int t0 = 0; t0 < qcore.n[0]; t0++)
       for (int t1 = 0; t1 < qcore.n[1]; t1++)
@@ -1035,8 +1056,11 @@ public:
       }
       else
         launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
-      launch_b_band<true, true>(band_x, a, cndB, zp, side[0]);
-      launch_b_band<false, true>(band_y, a, cndB, zp, side[1]);
+      launch_b_band<true, false, false>(band_xface, a, cndB, zp, side[0]);
+      launch_b_band<false, true, false>(band_yface, a, cndB, zp, side[1]);
+      launch_b_band<true, true>(band_xyedge, a, cndB, zp, side[3]);
+      launch_b_band<true, false>(band_xzedge, a, cndB, zp, side[4]);
+      launch_b_band<false, true>(band_yzedge, a, cndB, zp, side[5]);
       join();
     }
     else {
@@ -1076,8 +1100,11 @@ public:
     if constexpr (DIM == 3) {
       fork();
       launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
-      launch_de_band<true, true>(band_x, a, cndD, zp, side[0]);
-      launch_de_band<false, true>(band_y, a, cndD, zp, side[1]);
+      launch_de_band<true, false, false>(band_xface, a, cndD, zp, side[0]);
+      launch_de_band<false, true, false>(band_yface, a, cndD, zp, side[1]);
+      launch_de_band<true, true>(band_xyedge, a, cndD, zp, side[3]);
+      launch_de_band<true, false>(band_xzedge, a, cndD, zp, side[4]);
+      launch_de_band<false, true>(band_yzedge, a, cndD, zp, side[5]);
       join();
     }
     else {
