@@ -204,6 +204,51 @@ def adjoint_timing():
     return out
 
 
+def adjoint3d_timing():
+    """Reverse-time adjoint on the 3-D design workload (192x192x128 cells,
+    64x64x16 design voxels on an eps = 2.1 slab, flux objective over a 128x128
+    plane at 20 frequencies, 2000 steps) in FP32 fields with FP64 DFT sums and
+    sqrt(T) checkpoints (every 45 steps): wall time of forward + backward over
+    the plain forward run, device memory held by the forward state and the
+    checkpoints, and the gradient against FP64 central differences at 2
+    voxels."""
+    import numpy as np
+    from meep_gb300 import _lib
+    from meep_gb300.design import DesignProblem3D
+
+    try:
+        import torch
+        mem = lambda: torch.cuda.mem_get_info()[0]
+    except Exception:
+        mem = None
+    prob = DesignProblem3D(_lib.Engine())
+    rng = np.random.default_rng(2025)
+    eps = rng.uniform(1.0, 12.0, size=prob.design_shape)
+    prob.run(eps)  # warm-up
+    t0 = time.perf_counter()
+    prob.run(eps)
+    t_fwd = time.perf_counter() - t0
+    free0 = mem() if mem else None
+    t0 = time.perf_counter()
+    J, F, handle = prob.run(eps, grad=True, checkpoint_every=45)
+    free1 = mem() if mem else None
+    g = prob.backward(handle, F)
+    t_grad = time.perf_counter() - t0
+    vox = [(5, 60, 3), (32, 31, 8)]
+    fd = []
+    for v in vox:
+        ep, em = eps.copy(), eps.copy()
+        ep[v] += 1e-4
+        em[v] -= 1e-4
+        fd.append((prob.run(ep, precision=64)[0] - prob.run(em, precision=64)[0]) / 2e-4)
+    adj = np.array([g[v] for v in vox])
+    fd = np.array(fd)
+    return {"forward_s": t_fwd, "forward_plus_adjoint_s": t_grad, "grad_over_forward": t_grad / t_fwd,
+            "checkpoint_every": 45, "steps": prob.steps,
+            "device_gb_forward_state_and_checkpoints": (free0 - free1) / 1e9 if mem else None,
+            "grad_rel_err_fp32_vs_fd64": float(np.abs(adj - fd).max() / np.abs(fd).max())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -295,6 +340,10 @@ def main():
         adj = adjoint_timing()
     except Exception as e:  # reported, never fatal for the stepping benchmark
         adj = {"error": str(e)[:200]}
+    try:
+        adj["design3d_fp32"] = adjoint3d_timing()
+    except Exception as e:
+        adj["design3d_fp32"] = {"error": str(e)[:200]}
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,

@@ -8,6 +8,8 @@ source in the input guide and DFT monitors of Ez on an output line.
 needs (design-point D per step, or full checkpoints every K steps) and
 `backward()` returns dJ/deps over the design block for dJ/dDFT.
 
+`DesignProblem3D` is the 3-D counterpart with a flux objective.
+
 `DesignDFT` is the torch.autograd.Function mapping the design permittivity to
 the complex DFT of the output line, so objectives can be written in torch.
 """
@@ -99,6 +101,97 @@ class DesignProblem2D:
         """sum over frequencies of the mean over the line of |F|^2, and dJ/dF."""
         n = F.shape[0]
         return float(np.sum(np.abs(F) ** 2) / n), 2.0 * F / n
+
+
+class DesignProblem3D:
+    """Synthetic 3-D design problem: an eps block on a slab under a dipole,
+    objective = flux through a plane above it, summed over frequencies.
+
+    Default sizes: 192x192x128 cells at resolution 20, 16-cell PML (0.8
+    units) on every face, an eps=2.1 slab 10 cells thick across the cell, a
+    64x64x16-voxel design block (eps per voxel) on top of it, a Gaussian Ex
+    dipole (fcen 0.25, df 0.1) below the slab, and Ex, Ey, Hx, Hy DFT
+    monitors at 20 frequencies on a 128x128 z-normal plane above the block;
+    2000 steps.  The objective is J = sum_w Flux_z(w), Flux_z = sum over the
+    plane of Re(Ex conj Hy - Ey conj Hx).  The design variable is eps of each
+    voxel, applied to the inverse permittivity of Ex, Ey and Ez at the point
+    of the same index.
+    """
+
+    def __init__(self, engine=None, n=(192, 192, 128), res=20.0, dpml_cells=16, slab=(40, 50), design=(64, 64, 16),
+                 plane_z=90, plane=128, src_z=30, fcen=0.25, df=0.1, nfreq=20, steps=2000, precision=32):
+        self.eng = engine or _lib.Engine()
+        self.n, self.res = tuple(n), res
+        self.dpml = dpml_cells / res
+        self.steps, self.precision = steps, precision
+        self.fcen, self.df = fcen, df
+        self.freqs = np.linspace(fcen - df / 2, fcen + df / 2, nfreq)
+        self.comps = [_lib.comp(t, d) for t in range(4) for d in range(3)]
+        self.ecomps = [_lib.comp(_lib.E, d) for d in range(3)]
+        self.ext = tuple(x + 1 for x in self.n)
+        cx, cy = self.n[0] // 2, self.n[1] // 2
+        self.lo = (cx - design[0] // 2, cy - design[1] // 2, slab[1])
+        self.hi = (self.lo[0] + design[0] - 1, self.lo[1] + design[1] - 1, slab[1] + design[2] - 1)
+        eps = np.ones(self.ext)
+        eps[:, :, slab[0]:slab[1]] = 2.1
+        self.eps_bg = eps
+        self.src = (cx, cy, src_z)
+        self.plane_lo = (cx - plane // 2, cy - plane // 2, plane_z)
+        self.plane_hi = (self.plane_lo[0] + plane - 1, self.plane_lo[1] + plane - 1, plane_z)
+        self.design_shape = design
+
+    def _sim(self, eps_design, precision):
+        pml = {(d, s): (self.dpml, 1e-15, 1.0) for d in range(3) for s in (0, 1)}
+        sim = _lib.Sim(self.eng, dim=3, n=self.n, io=tuple(-x for x in self.n), a=self.res, courant=0.5, pml=pml,
+                       precision=precision, components=self.comps)
+        eps = self.eps_bg.copy()
+        eps[self.lo[0]:self.hi[0] + 1, self.lo[1]:self.hi[1] + 1, self.lo[2]:self.hi[2] + 1] = eps_design
+        inv = 1.0 / eps
+        for d, c in enumerate(self.ecomps):
+            sim.set_chi1inv(c, d, inv)
+        src = sim.add_gaussian_src(self.fcen, self.df)
+        e1, e2 = self.ext[1], self.ext[2]
+        sim.add_source_points(self.ecomps[0], src, [(self.src[0] * e1 + self.src[1]) * e2 + self.src[2]], [1.0])
+        npl = self.plane_hi[0] - self.plane_lo[0] + 1
+        w = [np.ones(npl), np.ones(npl), np.ones(1)]
+        mons = {}
+        for name, c, sc in (("ex", _lib.comp(_lib.E, _lib.X), 1.0), ("ey", _lib.comp(_lib.E, _lib.Y), -1.0),
+                            ("hx", _lib.comp(_lib.H, _lib.X), 1.0), ("hy", _lib.comp(_lib.H, _lib.Y), 1.0)):
+            mons[name] = sim.add_dft(c, self.plane_lo, self.plane_hi, w, dV=1.0, include_weights=False, scale=sc,
+                                     centered=False, freqs=self.freqs, decimation=1)
+        return sim, mons
+
+    @staticmethod
+    def objective(F):
+        """J = sum_w Flux(w) and dJ/dF for F = {ex, ey, hx, hy} DFT arrays (the
+        Ey monitor carries the flux sign in its scale)."""
+        J = float(np.sum((F["ex"] * np.conj(F["hy"])).real + (F["ey"] * np.conj(F["hx"])).real))
+        return J, {"ex": F["hy"], "hy": F["ex"], "ey": F["hx"], "hx": F["ey"]}
+
+    def run(self, eps_design, grad=False, checkpoint_every=-1, precision=None):
+        """Forward run.  Returns (J, F, handle); handle goes to backward()."""
+        prec = precision or self.precision
+        eps_design = np.asarray(eps_design, dtype=np.float64)
+        sim, mons = self._sim(eps_design, prec)
+        if grad:
+            sim.design(self.ecomps, self.lo, self.hi)
+            sim.forward(self.steps, checkpoint_every)
+        else:
+            sim.step(self.steps)
+        F = {k: sim.get_dft(m) for k, m in mons.items()}
+        J, _ = self.objective(F)
+        if not grad:
+            sim.close()
+            return J, F, None
+        return J, F, (sim, mons, eps_design)
+
+    def backward(self, handle, F):
+        """dJ/deps over the design block for the flux objective."""
+        sim, mons, eps_design = handle
+        _, g = self.objective(F)
+        gchi = sim.backward({mons[k]: g[k] for k in g})
+        sim.close()
+        return -gchi.sum(axis=0) / (eps_design * eps_design)  # chi1inv = 1/eps on Ex, Ey, Ez
 
 
 try:
