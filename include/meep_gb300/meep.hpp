@@ -476,6 +476,7 @@ public:
   virtual int kind() const = 0;
   virtual std::complex<double> frequency() const = 0;
   virtual double get_fwidth() const = 0;
+  virtual double last_time() const { return 0.0; }
   // parameters forwarded to the engine (see mfd_add_*_src)
   double p[6] = {0, 0, 0, 0, 0, 0};
 };
@@ -488,7 +489,7 @@ public:
   int kind() const override { return 0; }
   std::complex<double> frequency() const override { return freq; }
   double get_fwidth() const override { return fwidth; }
-  double last_time() const { return float(peak_time + cutoff); }
+  double last_time() const override { return float(peak_time + cutoff); }
   double freq, fwidth, width, peak_time, cutoff;
   bool explicit_window;
 };
@@ -501,6 +502,7 @@ public:
   int kind() const override { return 1; }
   std::complex<double> frequency() const override { return freq; }
   double get_fwidth() const override { return 0.0; }
+  double last_time() const override { return end_time; }
   std::complex<double> freq;
   double width, start_time, end_time, slowness;
 };
@@ -566,6 +568,8 @@ public:
   void use_real_fields();
   void step();
   double time() const { return t * dt; }
+  // latest time any source is still on (src/bands.cpp:35-41)
+  double last_source_time() const;
   double round_time() const { return float(t * dt); }
   double last_step_ms() const;
   long long kernel_launches() const;

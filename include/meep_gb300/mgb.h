@@ -1,0 +1,92 @@
+/* C interface of the meep:: drop-in for the Python Simulation front end.
+ *
+ * The reference's Python layer (python/simulation.py, python/geom.py,
+ * python/source.py) drives its C++ core through SWIG: it builds a grid_volume
+ * and a structure from a libctl geometry (src/meepgeom.cpp), adds volume
+ * sources, DFT flux and DFT field monitors, and steps the fields.  These
+ * entry points expose the same C++ calls of this repository's drop-in
+ * (include/meep_gb300/meep.hpp) to ctypes, with the geometry evaluated in C++
+ * (blocks, spheres, cylinders; later objects take precedence, as in libctl).
+ * All functions return 0 on success and -1 on error; mgb_last_error() then
+ * holds "meep: ...".
+ */
+#ifndef MGB_H_
+#define MGB_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGB_MAX_SUS 8
+
+typedef struct mgb_sim mgb_sim;
+
+typedef struct {
+  int kind; /* 0 block (axis-aligned), 1 sphere, 2 cylinder */
+  double center[3];
+  double size[3];  /* block edge lengths */
+  double radius;   /* sphere, cylinder */
+  double height;   /* cylinder */
+  double axis[3];  /* cylinder axis (unit vector) */
+  int material;    /* index into the medium table */
+} mgb_object;
+
+typedef struct {
+  double eps[3];    /* epsilon_diag */
+  double d_cond[3]; /* D_conductivity_diag */
+  int nsus;
+  int sus[MGB_MAX_SUS];          /* indices into the susceptibility table */
+  double sigma[MGB_MAX_SUS][3];  /* sigma_diag of each */
+} mgb_medium;
+
+typedef struct {
+  double frequency, gamma;
+  int drude;
+} mgb_susceptibility;
+
+/* grid and structure: vol1d/vol2d/vol3d(cell, resolution) centred on the
+ * origin; pml: npml rows of (thickness, direction or -1 for all, side
+ * (0 high, 1 low) or -1 for both, R_asymptotic, mean_stretch).  Real fields,
+ * metallic cell walls (k_point = False). */
+int mgb_create(int dim, const double cell[3], double resolution, double courant, int npml, const double *pml,
+               int nmed, const mgb_medium *media, int default_medium, int nobj, const mgb_object *objects,
+               int nsus, const mgb_susceptibility *sus, mgb_sim **out);
+void mgb_destroy(mgb_sim *s);
+const char *mgb_last_error(void);
+
+/* sources: kind 0 gaussian_src_time(p0 = frequency, p1 = width, p2 = start
+ * time, p3 = end time); kind 1 continuous_src_time(p0 = frequency, p1 =
+ * width, p2 = start time, p3 = end time, p4 = slowness).  Added with
+ * fields::add_volume_source(component, src, volume(center, size), amp). */
+int mgb_add_source(mgb_sim *s, int component, int kind, const double *params, int is_integrated,
+                   const double center[3], const double size[3], double amp_re, double amp_im);
+double mgb_last_source_time(const mgb_sim *s);
+
+/* flux: nreg rows of (center[3], size[3], direction or -1 for the normal of
+ * the region, weight); freqs[nfreq]; returns a handle */
+int mgb_add_flux(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                 int *handle);
+int mgb_flux(mgb_sim *s, int handle, double *out);
+/* DFT fields of ncomp components over volume(center, size) */
+int mgb_add_dft_fields(mgb_sim *s, int ncomp, const int *components, const double center[3],
+                       const double size[3], int nfreq, const double *freqs, int yee_grid, int decimation,
+                       int *handle);
+/* shape[3] (points per direction, 1 for absent ones) of component c of a DFT
+ * fields handle; out (may be NULL) receives shape product complex values of
+ * frequency ifreq, interleaved re/im, last direction fastest */
+int mgb_dft_fields_array(mgb_sim *s, int handle, int component, int ifreq, double *out, int shape[3]);
+
+int mgb_step(mgb_sim *s, int n);
+int mgb_time(const mgb_sim *s, double *time, double *round_time, double *dt, int *t);
+/* fields::get_field at n points (interpolated as the reference does) */
+int mgb_get_field_points(mgb_sim *s, int component, int n, const double *xyz, double *re, double *im);
+/* component c at every Yee point of the cell, x slowest (n = prod(N_d + 1)
+ * values; out NULL returns the count in *n) */
+int mgb_yee_array(mgb_sim *s, int component, double *out, long long *n);
+/* epsilon of the material at n points (no averaging) */
+int mgb_get_epsilon_points(mgb_sim *s, int n, const double *xyz, double *eps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

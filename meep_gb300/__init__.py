@@ -3,10 +3,17 @@
 The compute path is the CUDA engine in meep_gb300/lib/libmfd.so (C ABI:
 include/mfd.h); the C++ drop-in for meep::structure / meep::fields is
 include/meep_gb300/meep.hpp over meep_gb300/lib/libmeep_gb300.so.  This package
-binds the C ABI for Python (`Engine`, `Sim`).  There is no CPU fallback:
+binds the C ABI for Python (`Engine`, `Sim`) and carries the reference's
+Python `Simulation` interface for the stepping path (meep_gb300.simulation,
+re-exported here: `import meep_gb300 as mp; mp.Simulation(...)`).  There is no CPU fallback:
 loading raises if the CUDA library has not been built.
 """
 from ._lib import PRODUCT_LIB, Engine, MeepError, Sim, comp  # noqa: F401
+from .simulation import (  # noqa: F401
+    ALL, AUTOMATIC, Block, Bx, By, Bz, ContinuousSource, Cylinder, DrudeSusceptibility, Dx, Dy, Dz, Ex, Ey, Ez,
+    FluxRegion, GaussianSource, High, Hx, Hy, Hz, LorentzianSusceptibility, Low, Medium, PML, Simulation, Source,
+    Sphere, Vector3, Volume, X, Y, Z, after_time, air, at_beginning, at_end, at_every, get_flux_freqs, get_fluxes,
+    inf, vacuum)
 
 __all__ = ["Engine", "Sim", "MeepError", "comp", "PRODUCT_LIB", "engine"]
 

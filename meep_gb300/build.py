@@ -48,7 +48,8 @@ def _newer(target, sources):
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files += [os.path.join(ROOT, "include", "mfd.h"), os.path.join(ROOT, "include", "meep_gb300", "meep.hpp")]
+    files += [os.path.join(ROOT, "include", "mfd.h"), os.path.join(ROOT, "include", "meep_gb300", "meep.hpp"),
+              os.path.join(ROOT, "include", "meep_gb300", "mgb.h")]
     return files
 
 
@@ -82,11 +83,11 @@ def build_engine(force=False, verbose=False):
     objs = [os.path.join(objdir, f) for f in ("mfd_cuda_f64.o", "mfd_cuda_f32.o", "mfd_noalloc.o",
                                                "mfd_plan.o", "mfd_capi.o")]
     _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
-    api = os.path.join(CSRC, "meep_api.cpp")
+    api = [os.path.join(CSRC, "meep_api.cpp"), os.path.join(CSRC, "meep_pyshim.cpp")]
     links = []
     for name, flag in (("libmeep_gb300.so", []), ("libmeep_gb300_single.so", ["-DMEEP_SINGLE=1"])):
         links.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"] + flag + INC +
-                      ["-o", os.path.join(LIB, name), api, "-L" + LIB, "-lmfd", "-Wl,-rpath," + LIB])
+                     ["-o", os.path.join(LIB, name)] + api + ["-L" + LIB, "-lmfd", "-Wl,-rpath," + LIB])
     with ThreadPoolExecutor(max_workers=2) as ex:
         list(ex.map(_run, links))
     return so

@@ -995,6 +995,13 @@ void fields::sync_dfts() {
 
 void sync_dfts(fields &f) { f.sync_dfts(); }
 
+double fields::last_source_time() const {
+  double t = 0;
+  for (const auto &src : d->srcs)
+    t = std::max(t, src->last_time());
+  return t;
+}
+
 /* ------------------------------------------------------- fields: step */
 void fields::step() {
   ensure_engine(*this);

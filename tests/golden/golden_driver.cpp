@@ -235,6 +235,186 @@ static void case_known(Writer &w) {
   }
 }
 
+/* Scripts of the reference's Python interface, restated as the C++ calls its
+   Python layer makes (python/simulation.py: _create_grid_volume +
+   center_origin, PML boundary_region, geometry as a material_function with
+   the last containing object winning, one polarization per distinct
+   susceptibility, Source.add_source -> add_volume_source with
+   gaussian_src_time(f, w, start, start + 2 w cutoff) and is_integrated,
+   _add_fluxish_stuff -> add_dft_flux(volume_list prepended per region),
+   add_dft_fields, _run_until / _run_sources_until stopping on round_time).
+   tests/test_simulation_api.py runs the same scripts through the package's
+   Simulation class. */
+struct PyObj {
+  int kind; // 0 block, 1 sphere, 2 cylinder (axis z, infinite height)
+  double c[3], s[3], r;
+  int mat;
+};
+struct PyMed {
+  double eps[3], cond;
+  double sig[2]; // sigma of susceptibility 0 and 1
+};
+class PyGeom : public material_function {
+public:
+  int dim = 2;
+  std::vector<PyObj> objs;
+  std::vector<PyMed> meds;
+  const PyMed &at(const vec &r) const {
+    double p[3] = {r.x(), r.y(), dim == 3 ? r.z() : 0.0};
+    for (size_t q = objs.size(); q-- > 0;) {
+      const PyObj &o = objs[q];
+      double d[3] = {p[0] - o.c[0], p[1] - o.c[1], p[2] - o.c[2]};
+      bool in;
+      if (o.kind == 0) in = std::fabs(d[0]) <= 0.5 * o.s[0] && std::fabs(d[1]) <= 0.5 * o.s[1] &&
+                            std::fabs(d[2]) <= 0.5 * o.s[2];
+      else if (o.kind == 1) in = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] <= o.r * o.r;
+      else in = d[0] * d[0] + d[1] * d[1] <= o.r * o.r;
+      if (in) return meds[o.mat];
+    }
+    return meds[0];
+  }
+  virtual double chi1p1(field_type ft, const vec &r) { return ft == H_stuff ? 1.0 : at(r).eps[0]; }
+  virtual void eff_chi1inv_row(component c, double row[3], const volume &v, double, int) {
+    row[0] = row[1] = row[2] = 0.0;
+    int d = component_direction(c) % 3;
+    row[d] = type(c) == H_stuff ? 1.0 : 1.0 / at(v.center()).eps[d];
+  }
+  virtual bool has_conductivity(component c) {
+    if (!is_D(c)) return false;
+    for (const PyMed &m : meds)
+      if (m.cond != 0) return true;
+    return false;
+  }
+  virtual double conductivity(component c, const vec &r) { return is_D(c) ? at(r).cond : 0.0; }
+};
+class PySigma : public material_function {
+public:
+  const PyGeom *g;
+  int q;
+  PySigma(const PyGeom *geo, int k) : g(geo), q(k) {}
+  virtual void sigma_row(component c, double row[3], const vec &r) {
+    row[0] = row[1] = row[2] = 0.0;
+    row[component_direction(c) % 3] = g->at(r).sig[q];
+  }
+};
+
+// numpy.linspace(a, b, n): a + i * ((b - a) / (n - 1)), last element b
+static std::vector<double> np_linspace(double a, double b, int n) {
+  std::vector<double> v(n);
+  double step = (b - a) / (n - 1);
+  for (int i = 0; i < n; i++)
+    v[i] = i * step + a;
+  v[n - 1] = b;
+  return v;
+}
+
+static void py_run_until(fields &f, double until) {
+  double t0 = f.round_time();
+  while (!(f.round_time() >= t0 + until))
+    f.step();
+}
+
+static void py_run_until_after_sources(fields &f, double T) {
+  double ts = f.last_source_time();
+  py_run_until(f, (ts - f.round_time()) + T);
+}
+
+/* Script:
+     geometry = [mp.Block(mp.Vector3(mp.inf, 1, mp.inf), material=mp.Medium(epsilon=12)),
+                 mp.Cylinder(0.8, center=mp.Vector3(3, 1.5), material=mp.Medium(index=2)),
+                 mp.Sphere(0.6, center=mp.Vector3(-2, -1.7),
+                           material=mp.Medium(epsilon=6, D_conductivity=0.05))]
+     sim = mp.Simulation(cell_size=mp.Vector3(16, 8), resolution=10, geometry=geometry,
+                         boundary_layers=[mp.PML(1.0)], eps_averaging=False,
+                         sources=[mp.Source(mp.GaussianSource(0.15, fwidth=0.1), component=mp.Ez,
+                                            center=mp.Vector3(-6), size=mp.Vector3(y=1))])
+     tran = sim.add_flux([0.1, 0.125, 0.15, 0.175, 0.2],
+                         mp.FluxRegion(center=mp.Vector3(6), size=mp.Vector3(y=2)))
+     box = sim.add_flux(0.15, 0.05, 3, mp.FluxRegion(center=mp.Vector3(4), size=mp.Vector3(y=3)),
+                        mp.FluxRegion(center=mp.Vector3(2), size=mp.Vector3(y=3), weight=-1))
+     dft = sim.add_dft_fields([mp.Ez], [0.12, 0.15], center=mp.Vector3(5), size=mp.Vector3(1, 2))
+     sim.run(until_after_sources=30) */
+static void case_py_tm2d(Writer &w) {
+  const double inf = 1.0e20;
+  grid_volume gv = vol2d(16, 8, 10);
+  gv.center_origin();
+  PyGeom g;
+  g.dim = 2;
+  g.meds = {{{1, 1, 1}, 0, {0, 0}}, {{12, 12, 12}, 0, {0, 0}}, {{4, 4, 4}, 0, {0, 0}}, {{6, 6, 6}, 0.05, {0, 0}}};
+  g.objs = {{0, {0, 0, 0}, {inf, 1, inf}, 0, 1}, {2, {3, 1.5, 0}, {0, 0, 0}, 0.8, 2},
+            {1, {-2, -1.7, 0}, {0, 0, 0}, 0.6, 3}};
+  structure s(gv, g, pml(1.0), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.1);
+  gaussian_src_time src(0.15, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, volume(vec(-6, -0.5), vec(-6, 0.5)), complex<double>(1.0, 0.0));
+  std::vector<double> fr1 = {0.1, 0.125, 0.15, 0.175, 0.2};
+  volume_list r1(volume(vec(6, -1), vec(6, 1)), Sx, 1.0);
+  dft_flux tran = f.add_dft_flux(&r1, fr1.data(), fr1.size(), true, true, 0);
+  std::vector<double> fr2 = np_linspace(0.15 - 0.5 * 0.05, 0.15 + 0.5 * 0.05, 3);
+  volume_list *b1 = new volume_list(volume(vec(4, -1.5), vec(4, 1.5)), Sx, 1.0, nullptr);
+  volume_list b2(volume(vec(2, -1.5), vec(2, 1.5)), Sx, -1.0, b1);
+  dft_flux box = f.add_dft_flux(&b2, fr2.data(), fr2.size(), true, true, 0);
+  component cs[1] = {Ez};
+  std::vector<double> fr3 = {0.12, 0.15};
+  dft_fields dft = f.add_dft_fields(cs, 1, volume(vec(4.5, -1), vec(5.5, 1)), fr3.data(), fr3.size(), true, 0);
+  py_run_until_after_sources(f, 30);
+  sync_dfts(f);
+  double *F = tran.flux();
+  w.rec("flux_tran", std::vector<double>(F, F + fr1.size()));
+  delete[] F;
+  F = box.flux();
+  w.rec("flux_box", std::vector<double>(F, F + fr2.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ez", global_field(f, gv, Ez));
+  w.rec("Hy", global_field(f, gv, Hy));
+  w.rec("dft_Ez", dump_dft_chunks(dft.chunks, Ez, gv));
+}
+
+/* Script:
+     mat = mp.Medium(epsilon=2, E_susceptibilities=[
+         mp.LorentzianSusceptibility(frequency=1.1, gamma=0.1, sigma=0.5),
+         mp.DrudeSusceptibility(frequency=0.8, gamma=0.05, sigma=0.3)])
+     geometry = [mp.Block(mp.Vector3(1.2, 1.2, 1.2), material=mat),
+                 mp.Sphere(0.4, center=mp.Vector3(0.6), material=mp.Medium(epsilon_diag=mp.Vector3(2, 3, 4)))]
+     sim = mp.Simulation(cell_size=mp.Vector3(3, 3, 3), resolution=10, geometry=geometry,
+                         boundary_layers=[mp.PML(0.5)], eps_averaging=False,
+                         sources=[mp.Source(mp.GaussianSource(0.8, fwidth=0.5, is_integrated=True),
+                                            component=mp.Ex, center=mp.Vector3(-0.7, 0.1))])
+     flux = sim.add_flux(0.8, 0.4, 4, mp.FluxRegion(center=mp.Vector3(z=0.9), size=mp.Vector3(2, 2)))
+     sim.run(until=8) */
+static void case_py_disp3d(Writer &w) {
+  grid_volume gv = vol3d(3, 3, 3, 10);
+  gv.center_origin();
+  PyGeom g;
+  g.dim = 3;
+  g.meds = {{{1, 1, 1}, 0, {0, 0}}, {{2, 2, 2}, 0, {0.5, 0.3}}, {{2, 3, 4}, 0, {0, 0}}};
+  g.objs = {{0, {0, 0, 0}, {1.2, 1.2, 1.2}, 0, 1}, {1, {0.6, 0, 0}, {0, 0, 0}, 0.4, 2}};
+  structure s(gv, g, pml(0.5), identity(), 0, 0.5, false);
+  PySigma s0(&g, 0), s1(&g, 1);
+  s.add_susceptibility(s0, E_stuff, lorentzian_susceptibility(1.1, 0.1));
+  s.add_susceptibility(s1, E_stuff, lorentzian_susceptibility(0.8, 0.05, true));
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.5);
+  gaussian_src_time src(0.8, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = true;
+  f.add_volume_source(Ex, src, volume(vec(-0.7, 0.1, 0), vec(-0.7, 0.1, 0)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = np_linspace(0.8 - 0.5 * 0.4, 0.8 + 0.5 * 0.4, 4);
+  volume_list r(volume(vec(-1, -1, 0.9), vec(1, 1, 0.9)), Sz, 1.0);
+  dft_flux flux = f.add_dft_flux(&r, fr.data(), fr.size(), true, true, 0);
+  py_run_until(f, 8);
+  double *F = flux.flux();
+  w.rec("flux", std::vector<double>(F, F + fr.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ex", global_field(f, gv, Ex));
+  w.rec("Hy", global_field(f, gv, Hy));
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -260,6 +440,10 @@ int main(int argc, char **argv) {
     case_disp3d(w, 20, 18, 16, 20.0, 0.25, steps > 0 ? steps : 600, 7, true, 1);
   else if (cs == "known")
     case_known(w);
+  else if (cs == "py_tm2d")
+    case_py_tm2d(w);
+  else if (cs == "py_disp3d")
+    case_py_disp3d(w);
   else {
     fprintf(stderr, "unknown case %s\n", cs.c_str());
     return 2;

@@ -1,0 +1,129 @@
+"""The Python Simulation front end (meep_gb300.Simulation) on scripts of the
+reference's Python interface, against fixtures written by the reference core
+for the same scripts (tests/golden/golden_driver.cpp, cases py_tm2d and
+py_disp3d, which restate the C++ calls the reference's Python layer makes).
+
+CPU: the front end over the meep:: drop-in on the CPU oracle.
+GPU: the same over the CUDA engine (FP64 and FP32)."""
+import os
+
+import numpy as np
+import pytest
+
+from harness import golden, relerr
+import meep_gb300 as mp
+from meep_gb300.simulation import PRODUCT_LIB
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SINGLE_LIB = os.path.join(ROOT, "meep_gb300", "lib", "libmeep_gb300_single.so")
+
+
+def script_tm2d(lib):
+    geometry = [mp.Block(mp.Vector3(mp.inf, 1, mp.inf), material=mp.Medium(epsilon=12)),
+                mp.Cylinder(0.8, center=mp.Vector3(3, 1.5), material=mp.Medium(index=2)),
+                mp.Sphere(0.6, center=mp.Vector3(-2, -1.7), material=mp.Medium(epsilon=6, D_conductivity=0.05))]
+    sim = mp.Simulation(cell_size=mp.Vector3(16, 8), resolution=10, geometry=geometry,
+                        boundary_layers=[mp.PML(1.0)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(0.15, fwidth=0.1), component=mp.Ez,
+                                           center=mp.Vector3(-6), size=mp.Vector3(y=1))], _library=lib)
+    tran = sim.add_flux([0.1, 0.125, 0.15, 0.175, 0.2], mp.FluxRegion(center=mp.Vector3(6), size=mp.Vector3(y=2)))
+    box = sim.add_flux(0.15, 0.05, 3, mp.FluxRegion(center=mp.Vector3(4), size=mp.Vector3(y=3)),
+                       mp.FluxRegion(center=mp.Vector3(2), size=mp.Vector3(y=3), weight=-1))
+    dft = sim.add_dft_fields([mp.Ez], [0.12, 0.15], center=mp.Vector3(5), size=mp.Vector3(1, 2))
+    sim.run(until_after_sources=30)
+    return {"flux_tran": mp.get_fluxes(tran), "flux_box": mp.get_fluxes(box), "t": sim.meep_time(),
+            "Ez": sim.get_yee_array(mp.Ez).reshape(-1), "Hy": sim.get_yee_array(mp.Hy).reshape(-1),
+            "dft_Ez": [sim.get_dft_array(dft, mp.Ez, i) for i in range(2)]}
+
+
+def script_disp3d(lib):
+    mat = mp.Medium(epsilon=2, E_susceptibilities=[
+        mp.LorentzianSusceptibility(frequency=1.1, gamma=0.1, sigma=0.5),
+        mp.DrudeSusceptibility(frequency=0.8, gamma=0.05, sigma=0.3)])
+    geometry = [mp.Block(mp.Vector3(1.2, 1.2, 1.2), material=mat),
+                mp.Sphere(0.4, center=mp.Vector3(0.6), material=mp.Medium(epsilon_diag=mp.Vector3(2, 3, 4)))]
+    sim = mp.Simulation(cell_size=mp.Vector3(3, 3, 3), resolution=10, geometry=geometry,
+                        boundary_layers=[mp.PML(0.5)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(0.8, fwidth=0.5, is_integrated=True), component=mp.Ex,
+                                           center=mp.Vector3(-0.7, 0.1))], _library=lib)
+    flux = sim.add_flux(0.8, 0.4, 4, mp.FluxRegion(center=mp.Vector3(z=0.9), size=mp.Vector3(2, 2)))
+    sim.run(until=8)
+    return {"flux": mp.get_fluxes(flux), "t": sim.meep_time(), "Ex": sim.get_yee_array(mp.Ex).reshape(-1),
+            "Hy": sim.get_yee_array(mp.Hy).reshape(-1)}
+
+
+def _dft_from_fixture(rec, nd, nf):
+    rows = np.asarray(rec).reshape(-1, nd + 2 * nf)
+    return [rows[:, nd + 2 * w] + 1j * rows[:, nd + 2 * w + 1] for w in range(nf)]
+
+
+def _compare(out, ref, tol):
+    for k, v in ref.items():
+        if k == "realnum_bytes":
+            continue
+        if k == "dft_Ez":
+            for w, r in enumerate(_dft_from_fixture(v, 2, 2)):
+                o = np.asarray(out[k][w]).reshape(-1)
+                assert relerr(np.concatenate([o.real, o.imag]), np.concatenate([r.real, r.imag])) <= tol, (k, w)
+            continue
+        o = np.asarray(out[k], dtype=np.float64).reshape(-1)
+        assert relerr(o, np.asarray(v).reshape(-1)) <= tol, (k, relerr(o, np.asarray(v).reshape(-1)))
+
+
+@pytest.fixture(scope="module")
+def oracle_meep_lib(oracle_lib):
+    return os.path.join(os.path.dirname(oracle_lib), "liboracle_meep.so")
+
+
+def test_script_tm2d_on_oracle(oracle_meep_lib):
+    _compare(script_tm2d(oracle_meep_lib), golden("py_tm2d"), 1e-10)
+
+
+def test_script_disp3d_on_oracle(oracle_meep_lib):
+    _compare(script_disp3d(oracle_meep_lib), golden("py_disp3d"), 1e-10)
+
+
+def test_run_until_step_count(oracle_meep_lib):
+    """run(until=T) stops at the first step with round_time() >= T, as the
+    reference's _run_until does; a second run continues from there."""
+    sim = mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, eps_averaging=False,
+                        sources=[mp.Source(mp.ContinuousSource(0.5), component=mp.Ez, center=mp.Vector3())],
+                        _library=oracle_meep_lib)
+    sim.run(until=3)
+    assert sim.timestep() == 60
+    sim.run(until=0.26)
+    assert sim.timestep() == 66
+    calls = []
+    sim.run(mp.at_every(0.5, lambda s: calls.append(s.meep_time())), until=2)
+    assert sim.timestep() == 106 and len(calls) == 5
+
+
+def test_unsupported_options_raise(oracle_meep_lib):
+    with pytest.raises(NotImplementedError, match="eps_averaging"):
+        mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, _library=oracle_meep_lib)
+    with pytest.raises(NotImplementedError, match="k_point"):
+        mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, eps_averaging=False, k_point=mp.Vector3(),
+                      _library=oracle_meep_lib)
+    with pytest.raises(NotImplementedError, match="material functions"):
+        mp.Block(mp.Vector3(1, 1), material=lambda p: mp.Medium(epsilon=2))
+
+
+@pytest.mark.gpu
+def test_script_tm2d_on_gpu(engine_lib):
+    _compare(script_tm2d(PRODUCT_LIB), golden("py_tm2d"), 1e-10)
+
+
+@pytest.mark.gpu
+def test_script_disp3d_on_gpu(engine_lib):
+    _compare(script_disp3d(PRODUCT_LIB), golden("py_disp3d"), 1e-10)
+
+
+@pytest.mark.gpu
+def test_scripts_fp32_on_gpu(engine_lib):
+    for script, case in ((script_tm2d, "py_tm2d"), (script_disp3d, "py_disp3d")):
+        out = script(SINGLE_LIB)
+        ref64, ref32 = golden(case), golden(case, "f32")
+        for k in ("Ez", "Hy", "Ex", "flux", "flux_tran"):
+            if k in ref64:
+                bound = max(3 * relerr(ref32[k], ref64[k]), 1e-5)
+                assert relerr(np.reshape(out[k], -1), ref64[k]) <= bound, (case, k)
