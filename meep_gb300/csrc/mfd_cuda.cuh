@@ -312,6 +312,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 #include "mfd_fused.cuh"
 #include "mfd_k3d.cuh"
 #include "mfd_q3d.cuh"
+#include "mfd_dft_tc.cuh"
 #include "mfd_adjoint.cuh"
 namespace mfd {
 namespace cuda_impl {
@@ -602,12 +603,21 @@ public:
     double *freq = nullptr;
     double *w[3] = {};
     bool block = false;      // blocked FP32 contraction
+    bool tc = false;         // ... on the tensor cores (3xTF32 tcgen05)
     float *A = nullptr;      // [DFT_BLOCK_T][npts] samples
     float2 *B = nullptr;     // [DFT_BLOCK_T][nf] phases
     int cnt = 0;             // samples in the current block
     long long tn0 = 0;       // step count of the block's first sample
   };
   std::vector<DMon> mons;
+  int *d_tc_err = nullptr; // set by the tensor-core contraction when a wait ran out
+  void check_tc() {
+    if (!d_tc_err) return;
+    int e = 0;
+    cuda_check(cudaMemcpyAsync(&e, d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, stream), "error flag");
+    cuda_check(cudaStreamSynchronize(stream), "error flag sync");
+    if (e) throw Error("tensor-core DFT contraction: an MMA completion wait timed out");
+  }
   int fused_mask = -1; // component mask of an available fused kernel set, -1 none
   bool has_b_current = false;
   long long nlaunch = 0;
@@ -1209,6 +1219,14 @@ public:
     for (int d = 0; d < 3; d++)
       if (!m.w[d].empty()) dm.w[d] = dupload(m.w[d]);
     dm.block = sizeof(R) == 4 && !getenv("MFD_DIRECT_DFT");
+    // the block contraction on the tensor cores unless MFD_DFT_CUDA_CORES is
+    // set (the CUDA-core kernel stays as the cross-check)
+    dm.tc = dm.block && !getenv("MFD_DFT_CUDA_CORES");
+    if (dm.tc && !d_tc_err) {
+      d_tc_err = dzeros<int>(1);
+      cuda_check(cudaFuncSetAttribute(dft_contract_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM),
+                 "tensor-core DFT shared memory");
+    }
     if (dm.block) {
       dm.A = dalloc<float>((size_t)DFT_BLOCK_T * m.npts);
       dm.B = dalloc<float2>((size_t)DFT_BLOCK_T * m.freq.size());
@@ -1228,7 +1246,11 @@ public:
     const int chunk = 64; // frequencies per shared-memory pass (<= 32 KB)
     size_t smem = (size_t)dm.cnt * chunk * sizeof(float2);
     long long np = (long long)m.npts;
-    dft_contract_kernel<<<(unsigned)((np + 127) / 128), 128, smem, stream>>>(dm.A, dm.cnt, np, dm.B, nf, dm.acc);
+    if (dm.tc)
+      dft_contract_tc_kernel<<<(unsigned)((np + TC_M - 1) / TC_M), 128, TC_SMEM, stream>>>(dm.A, dm.cnt, np, dm.B, nf,
+                                                                                          dm.acc, d_tc_err);
+    else
+      dft_contract_kernel<<<(unsigned)((np + 127) / 128), 128, smem, stream>>>(dm.A, dm.cnt, np, dm.B, nf, dm.acc);
     nlaunch += 2;
     dm.cnt = 0;
   }
@@ -1473,6 +1495,7 @@ public:
     cuda_check(cudaEventElapsedTime(&fms, ev0, ev1), "elapsed");
     ms = fms;
     cuda_check(cudaGetLastError(), "kernel launch");
+    check_tc();
   }
   double last_step_ms() const override { return ms; }
   long long launches() const override { return nlaunch; }
@@ -1766,6 +1789,7 @@ public:
     cuda_check(cudaMemcpyAsync(out, mons[id].acc, n * sizeof(double2), cudaMemcpyDeviceToHost, stream),
                "download dft");
     cuda_check(cudaStreamSynchronize(stream), "download sync");
+    check_tc();
   }
 
   void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) override {
@@ -1793,6 +1817,7 @@ public:
     cuda_check(cudaMemcpyAsync(out, d_out, nf * sizeof(double), cudaMemcpyDeviceToHost, stream),
                "download flux");
     cuda_check(cudaStreamSynchronize(stream), "flux sync");
+    check_tc();
   }
 };
 
