@@ -566,6 +566,8 @@ public:
   ~fields();
 
   void use_real_fields();
+  void use_bloch(direction d, double k);
+  void use_bloch(const vec &k);
   void step();
   double time() const { return t * dt; }
   // latest time any source is still on (src/bands.cpp:35-41)

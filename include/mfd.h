@@ -146,6 +146,16 @@ int mfd_forward(mfd_sim *sim, int nsteps, int checkpoint_every);
 int mfd_backward(mfd_sim *sim, int nmon, const int *mon_ids, const double *const *dft_grad,
                  double *grad_chi1inv);
 
+/* Bloch-periodic boundaries (replaces fields::use_bloch, src/boundaries.cpp:
+ * 90-109): directions with periodic[d] != 0 get the Bloch wavevector k[d]
+ * (units of 2 pi / a); the other directions keep metallic walls.  A nonzero
+ * k makes the fields complex (fields::use_real_fields then aborts in the
+ * reference); mfd_get_field returns the real part, mfd_get_field_im the
+ * imaginary part.  Before the first step; not with PML in the same
+ * direction. */
+int mfd_set_bloch(mfd_sim *s, const int periodic[3], const double k[3]);
+int mfd_get_field_im(mfd_sim *s, int c, double *out);
+
 /* Allocation-free flux reduction.  No counterpart in the reference: it is the
  * reduction of mfd_flux (sum_k Re(E conj H) per frequency) for callers that
  * must not allocate device memory when they call it -- code recording a CUDA

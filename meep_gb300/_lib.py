@@ -68,6 +68,8 @@ SIGNATURES = [
     ("mfd_design", C.c_int, [_P, C.c_int, _IP, _IP, _IP]),
     ("mfd_forward", C.c_int, [_P, C.c_int, C.c_int]),
     ("mfd_backward", C.c_int, [_P, C.c_int, _IP, C.POINTER(_DP), _DP]),
+    ("mfd_set_bloch", C.c_int, [_P, C.POINTER(C.c_int), _DP]),
+    ("mfd_get_field_im", C.c_int, [_P, C.c_int, _DP]),
     ("mfd_flux_noalloc", C.c_int, [_P, _P, C.c_int64, C.c_int, _P, _P]),
     ("mfd_noalloc_last_error", C.c_char_p, []),
     ("mfd_kernel_launches", C.c_int64, [_P]),
@@ -223,6 +225,18 @@ class Sim:
     def get_field(self, c):
         out = np.zeros(self.ndense)
         self.eng.check(self.eng.lib.mfd_get_field(self.h, c, _dptr(out)))
+        return out.reshape(self.ext)
+
+    def set_bloch(self, periodic, k):
+        """Bloch-periodic boundaries: periodic[d] != 0 with wavevector k[d]
+        (units of 2 pi / a); a nonzero k makes the fields complex."""
+        per = (C.c_int * 3)(*[int(bool(x)) for x in periodic])
+        kk = np.ascontiguousarray(np.asarray(k, dtype=np.float64))
+        self.eng.check(self.eng.lib.mfd_set_bloch(self.h, per, _dptr(kk)))
+
+    def get_field_im(self, c):
+        out = np.zeros(self.ndense)
+        self.eng.check(self.eng.lib.mfd_get_field_im(self.h, c, _dptr(out)))
         return out.reshape(self.ext)
 
     def get_dft(self, mid):

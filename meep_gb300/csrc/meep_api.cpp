@@ -463,9 +463,19 @@ struct fields::impl {
   std::vector<std::unique_ptr<dft_chunk>> chunks; // owned dft chunks
   std::vector<dft_flux *> fluxes;
   bool real_fields = false;
-  // cache of downloaded fields for get_field
+  // Bloch-periodic boundaries (use_bloch): periodic directions, k, and
+  // eikna = exp(2 pi i k L) as the engine computes it
+  int periodic[3] = {0, 0, 0};
+  double kvec[3] = {0, 0, 0};
+  std::complex<double> eikna[3] = {{1, 0}, {1, 0}, {1, 0}};
+  bool complex_fields() const {
+    for (int q = 0; q < 3; q++)
+      if (periodic[q] && kvec[q] != 0.0) return true;
+    return false;
+  }
+  // cache of downloaded fields for get_field (real and imaginary parts)
   int64_t cache_t[20];
-  std::vector<double> cache[20];
+  std::vector<double> cache[20], cache_im[20];
   impl() {
     for (int i = 0; i < 20; i++)
       cache_t[i] = -1;
@@ -485,7 +495,28 @@ fields::fields(structure *s_, double m, double beta, bool zcyl, int tdb, int teh
 
 fields::~fields() {}
 
-void fields::use_real_fields() { d->real_fields = true; }
+void fields::use_real_fields() {
+  if (d->complex_fields()) meep::abort("Can't use real fields with bloch boundary conditions!\n");
+  d->real_fields = true;
+}
+
+// fields::use_bloch (src/boundaries.cpp:90-117): periodic boundaries along d
+// with Bloch wavevector k (units of 2 pi / a); a nonzero k needs complex
+// fields
+void fields::use_bloch(direction dd, double k) {
+  if (d->sim) meep::abort("use_bloch must be called before the first step");
+  if (dd > Z) meep::abort("use_bloch along a non-Cartesian direction is not supported");
+  d->periodic[dd] = 1;
+  d->kvec[dd] = k;
+  const double L = gv.num_direction(dd);
+  if (k * L == 0.5 * a) d->eikna[dd] = -1.0;
+  else d->eikna[dd] = std::exp(std::complex<double>(0.0, 1.0) * std::complex<double>(k, 0.0) * ((2 * pi / a) * L));
+  if (d->real_fields && k != 0.0) meep::abort("Can't use real fields with bloch boundary conditions!\n");
+}
+
+void fields::use_bloch(const vec &k) {
+  LOOP_OVER_DIRECTIONS(gv.dim, dd) use_bloch(dd, k.in_direction(dd));
+}
 
 static bool is_like(ndim dim, component c1, component c2) {
   if (dim != D2) return true;
@@ -534,6 +565,7 @@ static void ensure_engine(fields &f) {
   g.precision = sizeof(realnum) == 8 ? 64 : 32;
   g.components = I.components;
   chk(mfd_create(&g, &I.sim));
+  if (I.periodic[0] || I.periodic[1] || I.periodic[2]) chk(mfd_set_bloch(I.sim, I.periodic, I.kvec));
   structure::impl &S = *f.s->d;
   for (int dc = 0; dc < 3; dc++)
     for (int q = 0; q < 3; q++)
@@ -1027,15 +1059,37 @@ std::vector<double> fields::get_field_array(component c) {
   return out;
 }
 
-std::complex<double> fields::get_field(component c, const ivec &iloc, bool parallel) {
+std::complex<double> fields::get_field(component c, const ivec &iloc_, bool parallel) {
   (void)parallel;
   if (c >= Dielectric) meep::abort("get_field of a non-field component is not supported");
+  ivec iloc = iloc_;
+  std::complex<double> phase = 1.0;
+  // points outside the cell along a periodic direction are translated into it
+  // with the Bloch phase (fields::locate_point_in_user_volume,
+  // src/boundaries.cpp:207-229)
+  if (!gv.owns(iloc))
+    LOOP_OVER_DIRECTIONS(gv.dim, dd) {
+      if (dd > Z || !d->periodic[dd]) continue;
+      const int L = 2 * gv.num_direction(dd), lo = gv.little_corner().in_direction(dd);
+      while (iloc.in_direction(dd) <= lo) {
+        iloc.set_direction(dd, iloc.in_direction(dd) + L);
+        phase *= std::conj(d->eikna[dd]);
+      }
+      while (iloc.in_direction(dd) - L > lo) {
+        iloc.set_direction(dd, iloc.in_direction(dd) - L);
+        phase *= d->eikna[dd];
+      }
+    }
   if (!gv.owns(iloc)) return 0.0;
   int mc = mfd_comp(c);
   if (!((d->components >> mc) & 1)) return 0.0;
   ensure_engine(*this);
   if (d->cache_t[mc] != t) {
     d->cache[mc] = get_field_array(c);
+    if (d->complex_fields()) {
+      d->cache_im[mc].assign(d->cache[mc].size(), 0.0);
+      chk(mfd_get_field_im(d->sim, mc, d->cache_im[mc].data()));
+    }
     d->cache_t[mc] = t;
   }
   Dense dn(gv);
@@ -1044,7 +1098,8 @@ std::complex<double> fields::get_field(component c, const ivec &iloc, bool paral
   // points not on this component's grid are not owned by it
   ivec back = dn.iloc(gv, c, k);
   if (back != iloc) return 0.0;
-  return d->cache[mc][dn.index(k)];
+  const double im = d->complex_fields() ? d->cache_im[mc][dn.index(k)] : 0.0;
+  return phase * std::complex<double>(d->cache[mc][dn.index(k)], im);
 }
 
 static int my_round(double x) { return int(std::floor(std::fabs(x) + 0.5) * (x < 0 ? -1 : 1)); }

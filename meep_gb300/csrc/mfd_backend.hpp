@@ -28,6 +28,8 @@ public:
   // One full step from step count t to t+1, then the DFT updates at t+1.
   virtual void step(Plan &p, int64_t t, const std::vector<SrcStepValues> &vals) = 0;
   virtual void get_field(Plan &p, int c, double *out_dense) = 0;
+  // imaginary part of a complex (Bloch) field
+  virtual void get_field_im(Plan &p, int c, double *out_dense) = 0;
   virtual void get_dft(Plan &p, int id, double *out) = 0;
   virtual void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) = 0;
   virtual void synchronize() {}

@@ -260,6 +260,7 @@ int mfd_forward(mfd_sim *s, int n, int K) {
   MFD_TRY
   need(s && s->plan, "null simulation handle");
   need(s->design, "call mfd_design before mfd_forward");
+  need(!s->plan->complex_fields, "the adjoint does not support complex (Bloch) fields");
   need(n >= 1 && K >= -1, "invalid step counts");
   Plan &p = *s->plan;
   ensure_setup(s);
@@ -354,6 +355,28 @@ int mfd_get_field(mfd_sim *s, int c, double *out) {
     s->setup_done = true;
   }
   s->be->get_field(p, c, out);
+  MFD_CATCH
+}
+
+int mfd_get_field_im(mfd_sim *s, int c, double *out) {
+  MFD_TRY
+  check_comp(s, c);
+  need(out != nullptr, "null output");
+  Plan &p = *s->plan;
+  if (!p.have[c] || !p.complex_fields) {
+    std::memset(out, 0, sizeof(double) * p.ndense);
+    return 0;
+  }
+  ensure_setup(s);
+  s->be->get_field_im(p, c, out);
+  MFD_CATCH
+}
+
+int mfd_set_bloch(mfd_sim *s, const int periodic[3], const double k[3]) {
+  MFD_TRY
+  need(s && s->plan && periodic && k, "null argument");
+  need(!s->setup_done, "boundaries must be set before the first step");
+  s->plan->set_bloch(periodic, k);
   MFD_CATCH
 }
 

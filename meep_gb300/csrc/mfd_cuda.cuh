@@ -347,6 +347,7 @@ __global__ void src_current_kernel(R *f, const R *cndinv, const CurPoint *pts, i
 // ------------------------------------------------------------------ DFT
 template <typename R> struct DftArgs {
   const R *f, *fb;   // component array; fb = B array for H components (else null)
+  const R *fim, *fbim; // imaginary parts of complex (Bloch) fields, else null
   int hdir;          // direction of the H component (H/B selection)
   int hshift;        // shift of the component along hdir
   const double *w[3];
@@ -421,9 +422,39 @@ template <typename R> __global__ void dft_kernel(Geo g, DftArgs<R> a) {
   const R fv = dft_point_value(g, a, p);
   double2 ph = a.ph[w];
   double2 acc = a.acc[t];
-  acc.x += double(fv) * ph.x;
-  acc.y += double(fv) * ph.y;
+  if (a.fim) {
+    // complex fields: acc += phase * (f_re + i f_im) (src/dft.cpp:296-299)
+    DftArgs<R> ai = a;
+    ai.f = a.fim;
+    ai.fb = a.fbim;
+    const double fr = double(fv), fi = double(dft_point_value(g, ai, p));
+    acc.x += ph.x * fr - ph.y * fi;
+    acc.y += ph.x * fi + ph.y * fr;
+  }
+  else {
+    acc.x += double(fv) * ph.x;
+    acc.y += double(fv) * ph.y;
+  }
   a.acc[t] = acc;
+}
+
+// Bloch-periodic ghost plane along direction d: dst = phase * src for the two
+// parts (complex<realnum> product, src/step.cpp:186-192); im may be null for
+// real fields (phase then +-1)
+template <typename R>
+__global__ void ghost_plane_kernel(R *re, R *im, long long dst, long long src, int n1, int n2, long long s1,
+                                   long long s2, R pr, R pi) {
+  const int j2 = blockIdx.x * blockDim.x + threadIdx.x, j1 = blockIdx.y;
+  if (j2 >= n2 || j1 >= n1) return;
+  const long long o = j1 * s1 + j2 * s2;
+  const R vr = re[src + o];
+  if (im) {
+    const R vi = im[src + o];
+    re[dst + o] = pr * vr - pi * vi;
+    im[dst + o] = pr * vi + pi * vr;
+  }
+  else
+    re[dst + o] = pr * vr;
 }
 
 // Blocked DFT (FP32 path): each sampled step stores the monitor values in one
@@ -587,9 +618,57 @@ public:
     *cndinv[NC] = {};
   struct DPole {
     R *P[3] = {}, *PP[3] = {}, *s[3] = {};
+    R *Pim[3] = {}, *PPim[3] = {}; // imaginary parts (complex fields)
     R gamma1inv, gamma1, w0, w0d;
   };
   std::vector<DPole> poles;
+  // complex (Bloch) fields: the imaginary parts of every state array; the
+  // kernels run once per part with these swapped into f, fu, fw, fcnd, P
+  bool cplx = false;
+  R *fim[NC] = {}, *fuim[NC] = {}, *fwim[NC] = {}, *fcndim[NC] = {};
+  void swap_parts() {
+    for (int c = 0; c < NC; c++) {
+      std::swap(f[c], fim[c]);
+      std::swap(fu[c], fuim[c]);
+      std::swap(fw[c], fwim[c]);
+      std::swap(fcnd[c], fcndim[c]);
+    }
+    for (DPole &dp : poles)
+      for (int d = 0; d < 3; d++) {
+        std::swap(dp.P[d], dp.Pim[d]);
+        std::swap(dp.PP[d], dp.PPim[d]);
+      }
+  }
+  // source values for the imaginary part: Re(amp * (-i v)) = Im(amp * v)
+  static DipoleVals imag_part(const DipoleVals &v) {
+    DipoleVals o = v;
+    for (int k = 0; k < 16; k++) {
+      o.re[k] = v.im[k];
+      o.im[k] = -v.re[k];
+    }
+    return o;
+  }
+  // Bloch-periodic ghost planes of the components of field types t0, t1
+  void ghost_copy(const Plan &p, int t0, int t1) {
+    for (int d = 0; d < 3; d++) {
+      if (!p.periodic[d]) continue;
+      int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+      if (o1 > o2) std::swap(o1, o2);
+      for (int c = 0; c < NC; c++) {
+        if (!f[c] || (ctype(c) != t0 && ctype(c) != t1)) continue;
+        const bool s0 = p.shift[c][d] == 0;
+        const std::complex<double> ph = s0 ? std::conj(p.eikna[d]) : p.eikna[d];
+        const long long dst = s0 ? 0 : (long long)p.N[d] * p.stride[d];
+        const long long src = s0 ? (long long)p.N[d] * p.stride[d] : 0;
+        const int n1 = p.ext[o1], n2 = p.ext[o2];
+        const dim3 grid((unsigned)((n2 + 127) / 128), (unsigned)n1);
+        ghost_plane_kernel<R><<<grid, 128, 0, stream>>>(f[c], cplx ? fim[c] : nullptr, dst, src, n1, n2,
+                                                        (long long)p.stride[o1], (long long)p.stride[o2],
+                                                        R(ph.real()), R(ph.imag()));
+        nlaunch++;
+      }
+    }
+  }
   // sources
   SrcPoint *d_srcpts[3] = {};
   int nsrcpts[3] = {};
@@ -735,6 +814,21 @@ public:
       }
       poles.push_back(dp);
     }
+    cplx = p.complex_fields;
+    if (cplx) {
+      for (int c = 0; c < NC; c++) {
+        if (f[c]) fim[c] = dzeros<R>(p.nstore);
+        if (fu[c]) fuim[c] = dzeros<R>(p.nstore);
+        if (fw[c]) fwim[c] = dzeros<R>(p.nstore);
+        if (fcnd[c]) fcndim[c] = dzeros<R>(p.nstore);
+      }
+      for (DPole &dp : poles)
+        for (int d = 0; d < 3; d++)
+          if (dp.P[d]) {
+            dp.Pim[d] = dzeros<R>(p.nstore);
+            dp.PPim[d] = dzeros<R>(p.nstore);
+          }
+    }
     setup_sources(p);
     int mask = 0;
     for (int c = 0; c < NC; c++)
@@ -745,6 +839,7 @@ public:
     for (int d = 0; d < 3; d++)
       has_b_current = has_b_current || ncur[comp(MFD_B, d)] > 0;
     if (getenv("MFD_GENERIC_KERNELS")) fused_mask = -1;
+    if (p.any_periodic()) fused_mask = -1; // Bloch boundaries: the per-component kernels
     if (fused_mask >= 0) plan_boxes(p);
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
   }
@@ -1218,7 +1313,7 @@ public:
     dm.freq = dupload(m.freq);
     for (int d = 0; d < 3; d++)
       if (!m.w[d].empty()) dm.w[d] = dupload(m.w[d]);
-    dm.block = sizeof(R) == 4 && !getenv("MFD_DIRECT_DFT");
+    dm.block = sizeof(R) == 4 && !getenv("MFD_DIRECT_DFT") && !p.complex_fields;
     // the block contraction on the tensor cores unless MFD_DFT_CUDA_CORES is
     // set (the CUDA-core kernel stays as the cross-check)
     dm.tc = dm.block && !getenv("MFD_DFT_CUDA_CORES");
@@ -1409,12 +1504,18 @@ public:
     DftArgs<R> a{};
     a.f = f[m.c];
     a.fb = nullptr;
+    a.fim = cplx ? fim[m.c] : nullptr;
+    a.fbim = nullptr;
     if (ctype(m.c) == MFD_H) {
       int d = cdir(m.c);
       a.hdir = d;
       a.hshift = p.shift[m.c][d];
       a.fb = f[comp(MFD_B, d)];
       if (!p.pml_dir[d]) a.f = a.fb;
+      if (cplx) {
+        a.fbim = fim[comp(MFD_B, d)];
+        if (!p.pml_dir[d]) a.fim = a.fbim;
+      }
     }
     for (int d = 0; d < 3; d++) {
       a.w[d] = dm.w[d];
@@ -1465,15 +1566,28 @@ public:
     }
     if (fused_mask >= 0) fused_step(p, curb, curd, dip);
     else {
-      for (int d = 0; d < 3; d++)
-        if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
-      step_current(p, MFD_B, curb);
-      for (int d = 0; d < 3; d++)
-        if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
-      for (int d = 0; d < 3; d++)
-        if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
-      step_current(p, MFD_D, curd);
-      update_e(p, dip);
+      // per part (real, then imaginary for complex fields): the B half-step,
+      // its boundaries; then the D/E half-step, its boundaries
+      const int nparts = cplx ? 2 : 1;
+      for (int part = 0; part < nparts; part++) {
+        if (part) swap_parts();
+        for (int d = 0; d < 3; d++)
+          if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
+        step_current(p, MFD_B, part ? imag_part(curb) : curb);
+        for (int d = 0; d < 3; d++)
+          if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
+        if (part) swap_parts();
+      }
+      ghost_copy(p, MFD_B, MFD_H);
+      for (int part = 0; part < nparts; part++) {
+        if (part) swap_parts();
+        for (int d = 0; d < 3; d++)
+          if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
+        step_current(p, MFD_D, part ? imag_part(curd) : curd);
+        update_e(p, part ? imag_part(dip) : dip);
+        if (part) swap_parts();
+      }
+      ghost_copy(p, MFD_D, MFD_E);
     }
     int64_t tn = t + 1;
     for (size_t id = 0; id < p.monitors.size() && !skip_dft; id++) {
@@ -1758,6 +1872,21 @@ public:
     cuda_check(cudaMemcpyAsync(out, grad, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "grad");
     cuda_check(cudaStreamSynchronize(stream), "grad sync");
     cuda_check(cudaGetLastError(), "adjoint");
+  }
+
+  void get_field_im(Plan &p, int c, double *out) override {
+    if (!cplx) {
+      std::fill(out, out + p.ndense, 0.0);
+      return;
+    }
+    swap_parts();
+    try {
+      get_field(p, c, out);
+    } catch (...) {
+      swap_parts();
+      throw;
+    }
+    swap_parts();
   }
 
   void get_field(Plan &p, int c, double *out) override {

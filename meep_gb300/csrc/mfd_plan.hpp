@@ -111,6 +111,16 @@ public:
   int shift[NC][3] = {};
   int klo[NC][3] = {}, khi[NC][3] = {}; // updated (owned, not on a metal wall) range
 
+  // Bloch-periodic directions (fields::use_bloch, src/boundaries.cpp:90-109):
+  // the not-owned points (position 0 of shift-0 components, 2N+1 of shift-1
+  // components) hold the field of the opposite side times conj(eikna) /
+  // eikna, eikna = exp(2 pi i k L); the shift-0 high-wall points are owned
+  bool periodic[3] = {false, false, false};
+  std::complex<double> eikna[3] = {{1, 0}, {1, 0}, {1, 0}};
+  bool complex_fields = false; // a periodic direction with k != 0
+  void set_bloch(const int per[3], const double k[3]);
+  bool any_periodic() const { return periodic[0] || periodic[1] || periodic[2]; }
+
   // curl plan (D, B components): f -= dtdx (g1[i+s1]-g1[i] + g2[i]-g2[i+s2])
   struct Curl {
     int g1 = -1, g2 = -1;

@@ -46,6 +46,61 @@ public:
   bool have_H_sep[NC] = {};
   double ms = 0;
 
+  // complex (Bloch) fields: imaginary parts of every state array, swapped in
+  // for the second pass of each half-step; `part` selects Re or Im of the
+  // complex source amplitudes
+  bool cplx = false;
+  int part = 0;
+  std::vector<R> f_im[NC], fu_im[NC], fw_im[NC], fcnd_im[NC], fmp_im[NC];
+  std::vector<std::vector<R>> P_im, PP_im; // [pole * 3 + d]
+  void swap_parts() {
+    for (int c = 0; c < NC; c++) {
+      f[c].swap(f_im[c]);
+      fu[c].swap(fu_im[c]);
+      fw[c].swap(fw_im[c]);
+      fcnd[c].swap(fcnd_im[c]);
+      fmp[c].swap(fmp_im[c]);
+    }
+    for (size_t q = 0; q < poles.size(); q++)
+      for (int d = 0; d < 3; d++) {
+        poles[q].P[d].swap(P_im[q * 3 + d]);
+        poles[q].PP[d].swap(PP_im[q * 3 + d]);
+      }
+    part ^= 1;
+  }
+  double src_part(const std::complex<double> &A) const { return part ? A.imag() : A.real(); }
+
+  // not-owned points of Bloch-periodic directions: position 0 of shift-0
+  // components = conj(eikna) x position 2N, position 2N+1 of shift-1
+  // components = eikna x position 1 (src/boundaries.cpp:207-229,
+  // src/step.cpp:172-222); product in complex<realnum>
+  void ghost_copy(const Plan &p, int t0, int t1) {
+    for (int d = 0; d < 3; d++) {
+      if (!p.periodic[d]) continue;
+      int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+      if (o1 > o2) std::swap(o1, o2);
+      for (int c = 0; c < NC; c++) {
+        if (f[c].empty() || (ctype(c) != t0 && ctype(c) != t1)) continue;
+        const bool s0 = p.shift[c][d] == 0;
+        const std::complex<double> ph = s0 ? std::conj(p.eikna[d]) : p.eikna[d];
+        const std::complex<R> phr(R(ph.real()), R(ph.imag()));
+        const int64_t dst = s0 ? 0 : (int64_t)p.N[d] * p.stride[d];
+        const int64_t src = s0 ? (int64_t)p.N[d] * p.stride[d] : 0;
+        for (int j1 = 0; j1 < p.ext[o1]; j1++)
+          for (int j2 = 0; j2 < p.ext[o2]; j2++) {
+            const int64_t o = j1 * p.stride[o1] + j2 * p.stride[o2];
+            if (cplx) {
+              const std::complex<R> v = phr * std::complex<R>(f[c][src + o], f_im[c][src + o]);
+              f[c][dst + o] = v.real();
+              f_im[c][dst + o] = v.imag();
+            }
+            else
+              f[c][dst + o] = phr.real() * f[c][src + o];
+          }
+      }
+    }
+  }
+
   int64_t idx(const Plan &p, int k0, int k1, int k2) const {
     return k0 * p.stride[0] + k1 * p.stride[1] + k2 * p.stride[2];
   }
@@ -133,6 +188,21 @@ public:
       }
       (void)anyP;
       poles.push_back(std::move(pd));
+    }
+    cplx = p.complex_fields;
+    if (cplx) {
+      for (int c = 0; c < NC; c++) {
+        f_im[c].assign(f[c].size(), R(0));
+        fu_im[c].assign(fu[c].size(), R(0));
+        fw_im[c].assign(fw[c].size(), R(0));
+        fcnd_im[c].assign(fcnd[c].size(), R(0));
+        fmp_im[c].assign(fmp[c].size(), R(0));
+      }
+      for (const PoleData &pd : poles)
+        for (int d = 0; d < 3; d++) {
+          P_im.emplace_back(pd.P[d].size(), R(0));
+          PP_im.emplace_back(pd.PP[d].size(), R(0));
+        }
     }
   }
 
@@ -270,7 +340,7 @@ public:
       int dc = comp(MFD_D, cdir(sg.c));
       for (size_t j = 0; j < sg.idx.size(); j++) {
         std::complex<double> A = sg.amp[j] * vals[sg.src].dip_e;
-        fmp[dc][p.store_index_of_dense(sg.idx[j])] -= R(real(A));
+        fmp[dc][p.store_index_of_dense(sg.idx[j])] -= R(src_part(A));
       }
     }
     for (int d = 0; d < 3; d++) {
@@ -337,7 +407,7 @@ public:
         int64_t i = p.store_index_of_dense(sg.idx[j]);
         std::complex<double> A = sg.amp[j] * cur * p.dt;
         if (ci) A = A * double(ci[i]);
-        f[c][i] -= R(real(A));
+        f[c][i] -= R(src_part(A));
       }
     }
   }
@@ -381,7 +451,12 @@ public:
             else if (p.g.dim == 3) wgt = wz * (wy * (m.dV * wx));
             else wgt = 1.0 * (1.0 * (m.dV * wz));
           }
-          R fv;
+          R fv, fvi = R(0);
+          if (cplx) {
+            swap_parts();
+            fvi = dft_value(p, m.c, kk, ad, wgt);
+            swap_parts();
+          }
           if (ad[1] >= 0) {
             int q1[3] = {kk[0], kk[1], kk[2]}, q2[3] = {kk[0], kk[1], kk[2]}, q3[3] = {kk[0], kk[1], kk[2]};
             q1[ad[0]]++;
@@ -398,9 +473,36 @@ public:
           }
           else
             fv = R(wgt * value(p, m.c, kk));
-          for (int w = 0; w < nf; w++)
-            acc[cnt * nf + w] += std::complex<double>(double(fv * phr[w].real()), double(fv * phr[w].imag()));
+          if (cplx) {
+            // dft += phase * complex(f_re, f_im) in complex<realnum> (src/dft.cpp:296-299)
+            const std::complex<R> fc(fv, fvi);
+            for (int w = 0; w < nf; w++) {
+              const std::complex<R> q = phr[w] * fc;
+              acc[cnt * nf + w] += std::complex<double>(double(q.real()), double(q.imag()));
+            }
+          }
+          else
+            for (int w = 0; w < nf; w++)
+              acc[cnt * nf + w] += std::complex<double>(double(fv * phr[w].real()), double(fv * phr[w].imag()));
         }
+  }
+
+  // the (weighted, centred) monitor value at point kk
+  R dft_value(const Plan &p, int c, const int kk[3], const int ad[2], double wgt) const {
+    if (ad[1] >= 0) {
+      int q1[3] = {kk[0], kk[1], kk[2]}, q2[3] = {kk[0], kk[1], kk[2]}, q3[3] = {kk[0], kk[1], kk[2]};
+      q1[ad[0]]++;
+      q2[ad[1]]++;
+      q3[ad[0]]++;
+      q3[ad[1]]++;
+      return R((wgt * 0.25) * (value(p, c, kk) + value(p, c, q1) + value(p, c, q2) + value(p, c, q3)));
+    }
+    if (ad[0] >= 0) {
+      int q1[3] = {kk[0], kk[1], kk[2]};
+      q1[ad[0]]++;
+      return R((wgt * 0.5) * (value(p, c, kk) + value(p, c, q1)));
+    }
+    return R(wgt * value(p, c, kk));
   }
 
   // value of component c at point k; H is read from B where the owning chunk
@@ -416,15 +518,26 @@ public:
 
   void step(Plan &p, int64_t t, const std::vector<SrcStepValues> &vals) override {
     auto t0 = std::chrono::steady_clock::now();
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
-    step_source(p, MFD_B, vals);
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
-    for (int d = 0; d < 3; d++)
-      if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
-    step_source(p, MFD_D, vals);
-    update_e(p, vals);
+    const int nparts = cplx ? 2 : 1;
+    for (int q = 0; q < nparts; q++) {
+      if (q) swap_parts();
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_B, d)]) curl(p, comp(MFD_B, d));
+      step_source(p, MFD_B, vals);
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
+      if (q) swap_parts();
+    }
+    ghost_copy(p, MFD_B, MFD_H);
+    for (int q = 0; q < nparts; q++) {
+      if (q) swap_parts();
+      for (int d = 0; d < 3; d++)
+        if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
+      step_source(p, MFD_D, vals);
+      update_e(p, vals);
+      if (q) swap_parts();
+    }
+    ghost_copy(p, MFD_D, MFD_E);
     int64_t tn = t + 1;
     for (size_t id = 0; id < p.monitors.size(); id++) {
       const Monitor &m = p.monitors[id];
@@ -451,6 +564,16 @@ public:
         s = &f[comp(MFD_B, d)];
       out[di] = double((*s)[i]);
     }
+  }
+
+  void get_field_im(Plan &p, int c, double *out) override {
+    if (!cplx) {
+      std::fill(out, out + p.ndense, 0.0);
+      return;
+    }
+    swap_parts();
+    get_field(p, c, out);
+    swap_parts();
   }
 
   void get_dft(Plan &p, int id, double *out) override {

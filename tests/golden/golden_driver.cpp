@@ -192,6 +192,43 @@ static void case_disp3d(Writer &w, int nx, int ny, int nz, double res, double dp
    polariton.  Same structures, sources and run lengths. */
 static double one_eps(const vec &) { return 1.0; }
 static double sigma_763(const vec &) { return 7.63; }
+// rods of eps 12 on a unit lattice (tests/known_results.cpp:28-41)
+static double rods_eps(const vec &r) {
+  vec p = r;
+  while (p.x() < -0.5)
+    p.set_direction(X, p.x() + 1.0);
+  while (p.x() > 0.5)
+    p.set_direction(X, p.x() - 1.0);
+  while (p.y() < -0.5)
+    p.set_direction(Y, p.y() + 1.0);
+  while (p.y() > 0.5)
+    p.set_direction(Y, p.y() - 1.0);
+  if (p.x() * p.x() + p.y() * p.y() < 0.3) return 12.0;
+  return 1.0;
+}
+
+// Bloch-periodic known results (tests/known_results.cpp:63-101): the same
+// structures, sources, wavevectors and run lengths
+static double known_x_periodic(const grid_volume &gv, double eps(const vec &), bool ypml) {
+  structure s(gv, eps, ypml ? pml(1.0, Y) : boundary_region());
+  fields f(&s);
+  f.add_point_source(Ez, 0.2, 3.0, 0.0, 2.0, gv.center(), complex<double>(0, -2 * pi * 0.2));
+  f.use_bloch(X, 0.1);
+  while (f.round_time() < 30.0)
+    f.step();
+  return real(f.get_field(Ez, gv.center()));
+}
+
+static double known_periodic(const grid_volume &gv, double eps(const vec &)) {
+  structure s(gv, eps);
+  fields f(&s);
+  f.add_point_source(Ez, 0.2, 3.0, 0.0, 2.0, gv.center(), complex<double>(0, -2 * pi * 0.2));
+  vec k = gv.dim == D2 ? vec(0.3, 0.4) : vec(0.3, 0.5, 0.8);
+  f.use_bloch(k);
+  while (f.round_time() < 30.0)
+    f.step();
+  return real(f.get_field(Ez, gv.center()));
+}
 
 static void case_known(Writer &w) {
   const double a = 10.0;
@@ -233,6 +270,14 @@ static void case_known(Writer &w) {
       f.step();
     w.scalar("polariton_1d", real(f.get_field(Ex, gv.center())));
   }
+  w.scalar("x_periodic_2d", known_x_periodic(voltwo(1.0, 1.0, a), one_eps, false));
+  w.scalar("periodic_2d_rods", known_periodic(voltwo(1.0, 3.0, a), rods_eps));
+  w.scalar("periodic_2d", known_periodic(voltwo(1.0, 3.0, a), one_eps));
+  w.scalar("x_periodic_y_pml_2d", known_x_periodic(voltwo(1.0, 3.0, a), one_eps, true));
+  w.scalar("x_periodic_3d", known_x_periodic(vol3d(1.0, 1.0, 1.0, a), one_eps, false));
+  w.scalar("x_periodic_y_pml_3d", known_x_periodic(vol3d(1.0, 3.0, 1.0, a), one_eps, true));
+  w.scalar("periodic_3d_rods", known_periodic(vol3d(1.0, 1.0, 1.0, a), rods_eps));
+  w.scalar("periodic_3d", known_periodic(vol3d(1.0, 1.0, 1.0, a), one_eps));
 }
 
 /* Scripts of the reference's Python interface, restated as the C++ calls its

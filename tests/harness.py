@@ -70,7 +70,7 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
-                   nsrc=3, steps=60, n=None):
+                   nsrc=3, steps=60, n=None, bloch=None):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -95,8 +95,12 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
         for d in range(dim if dim == 3 else 2):
             for side in (0, 1):
                 pmlspec[(d, side)] = (float(rng.choice([0.3, 0.5])), 1e-15, 1.0)
+                if bloch is not None and d in bloch:
+                    del pmlspec[(d, side)]  # periodic direction: no PML
     sim = sim_factory(dim=dim, n=n, io=io, a=a, courant=0.5, pml=pmlspec, precision=precision,
                       components=comps)
+    if bloch is not None:
+        sim.set_bloch([int(d in bloch) for d in range(3)], [bloch.get(d, 0.0) for d in range(3)])
     ext = sim.ext
     shape = tuple(ext)
     for c in comps:
@@ -135,6 +139,8 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
                                 centered=True, freqs=np.linspace(0.3, 0.9, 5), decimation=2))
     sim.step(steps)
     out = {"c%d" % c: sim.get_field(c) for c in comps}
+    if bloch is not None:
+        out.update({"i%d" % c: sim.get_field_im(c) for c in comps})
     for m in mons:
         out["dft%d" % m] = sim.get_dft(m)
     out["flux"] = sim.flux([mons[0]], [mons[1]], 5)

@@ -44,3 +44,22 @@ def test_fp32_matches_fp32_oracle(seed, n, engine_lib, oracle_lib):
     o = _run(oracle_lib, seed, 3, 32, n=n)
     for k in o:
         assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
+
+
+# Bloch-periodic boundaries with complex fields (and k = 0: real fields,
+# periodic copies), PML in the other directions, dispersive and conductive
+# media: same random problems on the GPU and the oracle
+@pytest.mark.parametrize("dim,seed,bloch", [(2, 31, {0: 0.17}), (2, 32, {0: 0.0, 1: 0.23}),
+                                            (3, 33, {0: 0.11, 2: 0.3}), (3, 34, {1: 0.0})])
+def test_bloch_fp64_bitwise_class(dim, seed, bloch, engine_lib, oracle_lib):
+    g = _run(engine_lib, seed, dim, 64, bloch=bloch)
+    o = _run(oracle_lib, seed, dim, 64, bloch=bloch)
+    for k in o:
+        assert relerr(g[k], o[k]) <= 1e-12, (k, relerr(g[k], o[k]))
+
+
+def test_bloch_fp32_close(engine_lib, oracle_lib):
+    g = _run(engine_lib, 35, 3, 32, bloch={0: 0.2, 1: 0.1})
+    o = _run(oracle_lib, 35, 3, 64, bloch={0: 0.2, 1: 0.1})
+    for k in o:
+        assert relerr(g[k], o[k]) <= 1e-3, (k, relerr(g[k], o[k]))

@@ -22,10 +22,13 @@ def test_oracle_fp64_matches_reference(case, oracle_lib, tmp_path):
 
 
 def test_known_results_values(oracle_lib, tmp_path):
-    # published values of the reference's test suite (tests/known_results.cpp:146-153)
+    # published values of the reference's test suite (tests/known_results.cpp:146-165),
+    # including the Bloch-periodic ones
     out = run_driver(ORACLE_DRIVER[64], "known", tmp_path)
     expect = {"metallic_2d_tm": 5.20605, "pml_2d_tm": 0.883776, "metallic_3d": -41.8057,
-              "polariton_1d": -0.0894851}
+              "polariton_1d": -0.0894851, "x_periodic_2d": 0.110425, "periodic_2d_rods": -4.78767,
+              "periodic_2d": 1.12502, "x_periodic_y_pml_2d": 0.608815, "x_periodic_3d": -100.758,
+              "x_periodic_y_pml_3d": -101.398, "periodic_3d_rods": -103.844, "periodic_3d": -99.1618}
     for k, v in expect.items():
         assert abs(out[k][0] - v) <= abs(v) * 1e-5, (k, out[k][0], v)
 
