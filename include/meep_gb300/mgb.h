@@ -7,6 +7,7 @@
  * entry points expose the same C++ calls of this repository's drop-in
  * (include/meep_gb300/meep.hpp) to ctypes, with the geometry evaluated in C++
  * (blocks, spheres, cylinders; later objects take precedence, as in libctl).
+ * Cell walls are metallic unless mgb_use_bloch makes them periodic.
  * All functions return 0 on success and -1 on error; mgb_last_error() then
  * holds "meep: ...".
  */
@@ -46,8 +47,7 @@ typedef struct {
 
 /* grid and structure: vol1d/vol2d/vol3d(cell, resolution) centred on the
  * origin; pml: npml rows of (thickness, direction or -1 for all, side
- * (0 high, 1 low) or -1 for both, R_asymptotic, mean_stretch).  Real fields,
- * metallic cell walls (k_point = False). */
+ * (0 high, 1 low) or -1 for both, R_asymptotic, mean_stretch). */
 int mgb_create(int dim, const double cell[3], double resolution, double courant, int npml, const double *pml,
                int nmed, const mgb_medium *media, int default_medium, int nobj, const mgb_object *objects,
                int nsus, const mgb_susceptibility *sus, mgb_sim **out);
@@ -81,8 +81,12 @@ int mgb_time(const mgb_sim *s, double *time, double *round_time, double *dt, int
 /* fields::get_field at n points (interpolated as the reference does) */
 int mgb_get_field_points(mgb_sim *s, int component, int n, const double *xyz, double *re, double *im);
 /* component c at every Yee point of the cell, x slowest (n = prod(N_d + 1)
- * values; out NULL returns the count in *n) */
-int mgb_yee_array(mgb_sim *s, int component, double *out, long long *n);
+ * values; out NULL returns the count in *n); part 0 real, 1 imaginary */
+int mgb_yee_array(mgb_sim *s, int component, int part, double *out, long long *n);
+/* Bloch-periodic boundaries in every direction of the cell with wavevector
+ * k (fields::use_bloch(vec)); before the first step.  A nonzero k makes the
+ * fields complex. */
+int mgb_use_bloch(mgb_sim *s, const double k[3]);
 /* epsilon of the material at n points (no averaging) */
 int mgb_get_epsilon_points(mgb_sim *s, int n, const double *xyz, double *eps);
 

@@ -151,8 +151,8 @@ int mfd_backward(mfd_sim *sim, int nmon, const int *mon_ids, const double *const
  * (units of 2 pi / a); the other directions keep metallic walls.  A nonzero
  * k makes the fields complex (fields::use_real_fields then aborts in the
  * reference); mfd_get_field returns the real part, mfd_get_field_im the
- * imaginary part.  Before the first step; not with PML in the same
- * direction. */
+ * imaginary part.  Before the first step; PML may sit in front of a
+ * periodic wall. */
 int mfd_set_bloch(mfd_sim *s, const int periodic[3], const double k[3]);
 int mfd_get_field_im(mfd_sim *s, int c, double *out);
 

@@ -677,20 +677,27 @@ static void compute_boundary_weights(const grid_volume &gv, const volume &where,
   }
 }
 
-static LoopBox loop_global(const grid_volume &gv, const volume &where, component cgrid,
-                           bool snap_empty = false) {
+// One lattice image of a loop volume (fields::loop_in_chunks,
+// src/loop_in_chunks.cpp:355-470, one chunk = the whole cell, no symmetry):
+// the owned points of the volume shifted by -shift, their boundary weights,
+// and the Bloch phase of the shift.
+struct LoopImage {
   LoopBox L;
-  vec yee_c(gv.yee_shift(Centered) - gv.yee_shift(cgrid));
-  ivec iyee_c(gv.iyee_shift(Centered) - gv.iyee_shift(cgrid));
-  volume wherec(where + yee_c);
-  ivec is(vec2diel_floor(wherec.get_min_corner(), gv.a, zero_ivec(gv.dim)) - iyee_c);
-  ivec ie(vec2diel_ceil(wherec.get_max_corner(), gv.a, zero_ivec(gv.dim)) - iyee_c);
-  vec s0(gv.dim), e0(gv.dim), s1(gv.dim), e1(gv.dim);
-  compute_boundary_weights(gv, where, is, ie, snap_empty, s0, e0, s1, e1);
+  ivec shift;
+  std::complex<double> phase = 1.0;
+};
+
+static LoopBox loop_shifted(const grid_volume &gv, const volume &where, component cgrid, const ivec &is,
+                            const ivec &ie, const vec &s0, const vec &s1, const vec &e0, const vec &e1,
+                            const ivec &shifti) {
+  LoopBox L;
   ivec iscoS = gv.little_owned_corner(cgrid), iecoS = gv.big_owned_corner(cgrid);
-  ivec iscS(max(is, iscoS));
-  ivec iecS(min(ie, iecoS));
+  ivec iscS(max(is - shifti, iscoS));
+  ivec iecS(min(ie - shifti, iecoS));
   if (!(iscS <= iecS)) return L;
+  const ivec isc = iscS, iec = iecS;
+  iscS += shifti;
+  iecS += shifti;
   vec s0c(gv.dim, 1.0), s1c(gv.dim, 1.0), e0c(gv.dim, 1.0), e1c(gv.dim, 1.0);
   LOOP_OVER_DIRECTIONS(gv.dim, d) {
     if (iscS.in_direction(d) == is.in_direction(d)) {
@@ -733,14 +740,61 @@ static LoopBox loop_global(const grid_volume &gv, const volume &where, component
     if (where.in_direction(d) > 0.0) dV0 *= gv.inva;
   }
   L.empty = false;
-  L.is = iscS;
-  L.ie = iecS;
+  L.is = isc;
+  L.ie = iec;
   L.s0 = s0c;
   L.s1 = s1c;
   L.e0 = e0c;
   L.e1 = e1c;
   L.dV0 = dV0;
   return L;
+}
+
+// every image of `where` along the Bloch-periodic directions (lattice shifts
+// from floor((where_min - cell_max) / L) to ceil((where_max - cell_min) / L),
+// phase prod eikna^shift); a single unshifted image otherwise
+static std::vector<LoopImage> loop_images(const grid_volume &gv, const volume &where, component cgrid,
+                                          const int periodic[3], const std::complex<double> eikna[3],
+                                          bool snap_empty = false) {
+  vec yee_c(gv.yee_shift(Centered) - gv.yee_shift(cgrid));
+  ivec iyee_c(gv.iyee_shift(Centered) - gv.iyee_shift(cgrid));
+  volume wherec(where + yee_c);
+  ivec is(vec2diel_floor(wherec.get_min_corner(), gv.a, zero_ivec(gv.dim)) - iyee_c);
+  ivec ie(vec2diel_ceil(wherec.get_max_corner(), gv.a, zero_ivec(gv.dim)) - iyee_c);
+  vec s0(gv.dim), e0(gv.dim), s1(gv.dim), e1(gv.dim);
+  compute_boundary_weights(gv, where, is, ie, snap_empty, s0, e0, s1, e1);
+  const volume gvS = gv.surroundings();
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    if (d > Z || !periodic[d]) continue;
+    const double L = gv.num_direction(d) * gv.inva;
+    lo[d] = int(std::floor((where.in_direction_min(d) - gvS.in_direction_max(d)) / L));
+    hi[d] = int(std::ceil((where.in_direction_max(d) - gvS.in_direction_min(d)) / L));
+  }
+  std::vector<LoopImage> out;
+  for (int a = lo[0]; a <= hi[0]; a++)
+    for (int b = lo[1]; b <= hi[1]; b++)
+      for (int c = lo[2]; c <= hi[2]; c++) {
+        const int ish[3] = {a, b, c};
+        LoopImage im;
+        im.shift = zero_ivec(gv.dim);
+        LOOP_OVER_DIRECTIONS(gv.dim, d) {
+          if (d > Z) continue;
+          im.shift.set_direction(d, 2 * gv.num_direction(d) * ish[d]);
+          im.phase *= std::pow(eikna[d], ish[d]);
+        }
+        im.L = loop_shifted(gv, where, cgrid, is, ie, s0, s1, e0, e1, im.shift);
+        if (!im.L.empty) out.push_back(im);
+      }
+  return out;
+}
+
+static LoopBox loop_global(const grid_volume &gv, const volume &where, component cgrid,
+                           bool snap_empty = false) {
+  const int none[3] = {0, 0, 0};
+  const std::complex<double> ones[3] = {1.0, 1.0, 1.0};
+  std::vector<LoopImage> im = loop_images(gv, where, cgrid, none, ones, snap_empty);
+  return im.empty() ? LoopBox() : im[0].L;
 }
 
 // IVEC_LOOP_WEIGHT1x (src/meep/vec.hpp:365-372)
@@ -808,11 +862,15 @@ void fields::add_volume_source(component c, const src_time &src, const volume &w
   d->srcs.emplace_back(src.clone());
   int sidx = (int)d->srcs.size() - 1;
   vec center = (where.get_min_corner() + where.get_max_corner()) * 0.5;
-  LoopBox L = loop_global(gv, where, c);
   PendingSource ps;
   ps.c = mfd_comp(c);
   ps.src = sidx;
-  if (!L.empty) {
+  for (const LoopImage &img : loop_images(gv, where, c, d->periodic, d->eikna)) {
+    const LoopBox &L = img.L;
+    // src_vol_chunkloop (src/sources.cpp:259-273): amp * conj(shift phase),
+    // amplitude function at the unshifted position
+    const std::complex<double> iamp = damp * std::conj(img.phase);
+    const vec vshift = vec(img.shift.dim, 0.0) + (img.shift * (0.5 * gv.inva));
     Dense dn(gv);
     int k0[3], k1[3], n[3] = {1, 1, 1};
     dn.kof(gv, c, L.is, k0);
@@ -843,10 +901,10 @@ void fields::add_volume_source(component c, const src_time &src, const volume &w
           else wgt = 1.0 * (1.0 * (1.0 * wd[0]));
           ivec iloc = dn.iloc(gv, c, k);
           if (!gv.owns(iloc)) continue;
-          vec loc = loop_loc(gv, iloc);
+          vec loc = loop_loc(gv, iloc) + vshift;
           vec rel = loc - center;
           ps.idx.push_back(dn.index(k));
-          ps.amp.push_back(wgt * damp * A(rel));
+          ps.amp.push_back(wgt * iamp * A(rel));
         }
   }
   d->pending.push_back(std::move(ps));
@@ -885,8 +943,10 @@ static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const
   if (decimation_factor == 0) decimation_factor = auto_decimation(f, freq, Nfreq);
   const grid_volume &gv = f.gv;
   component cgrid = use_centered_grid ? Centered : c;
-  LoopBox L = loop_global(gv, where, cgrid);
-  if (L.empty) return next;
+  // one chunk per lattice image of the region (add_dft_chunkloop,
+  // src/dft.cpp:158-173: scale times the image's Bloch phase)
+  for (const LoopImage &img : loop_images(gv, where, cgrid, I.periodic, I.eikna)) {
+  const LoopBox &L = img.L;
   Dense dn(gv);
   // array index box of component c (for the centred grid, point k of c is the
   // base of the average centred at 2k+1)
@@ -905,7 +965,7 @@ static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const
       w[dd][i] = w1x(L, i, n, dd);
     wp[dd] = w[dd].data();
   }
-  std::complex<double> scale = stored_weight * std::complex<double>(1.0, 0.0) *
+  std::complex<double> scale = stored_weight * img.phase *
                                (f.dt / std::sqrt(2.0 * pi) * decimation_factor);
   int id = -1;
   chk(mfd_add_dft(I.sim, mc, lo, hi, wp, L.dV0, include_dV_and_interp_weights ? 1 : 0, scale.real(),
@@ -923,9 +983,10 @@ static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const
   ch->N = npts;
   ch->dft = new std::complex<realnum>[npts * Nfreq]();
   ch->next_in_dft = next;
-  dft_chunk *raw = ch.get();
+  next = ch.get();
   I.chunks.push_back(std::move(ch));
-  return raw;
+  }
+  return next;
 }
 
 dft_flux fields::add_dft_flux(const volume_list *where_, const double *freq, size_t Nfreq,

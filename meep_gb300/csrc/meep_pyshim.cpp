@@ -188,7 +188,6 @@ int mgb_create(int dim, const double cell[3], double resolution, double courant,
                                lorentzian_susceptibility(sus[q].frequency, sus[q].gamma, sus[q].drude != 0));
     }
     S->f.reset(new fields(S->s.get()));
-    S->f->use_real_fields();
     *out = S.release();
     return 0;
   } catch (const std::exception &e) {
@@ -349,7 +348,17 @@ int mgb_get_field_points(mgb_sim *s, int component_, int n, const double *xyz, d
   }
 }
 
-int mgb_yee_array(mgb_sim *s, int component_, double *out, long long *n) {
+int mgb_use_bloch(mgb_sim *s, const double k[3]) {
+  try {
+    if (!s || !k) throw std::runtime_error("null argument");
+    s->f->use_bloch(mkvec(s->dim, k));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_yee_array(mgb_sim *s, int component_, int part, double *out, long long *n) {
   try {
     if (!s || !n) throw std::runtime_error("null argument");
     const grid_volume &gv = s->f->gv;
@@ -373,7 +382,8 @@ int mgb_yee_array(mgb_sim *s, int component_, double *out, long long *n) {
           const int k[3] = {a, b, e};
           for (int r = 0; r < nd; r++)
             p.set_direction(ds[r], p.in_direction(ds[r]) + 2 * k[r]);
-          out[q++] = std::real(s->f->get_field(c, p, false));
+          const std::complex<double> v = s->f->get_field(c, p, false);
+          out[q++] = part ? v.imag() : v.real();
         }
     return 0;
   } catch (const std::exception &e) {

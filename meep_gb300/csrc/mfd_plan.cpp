@@ -291,7 +291,6 @@ void Plan::set_bloch(const int per[3], const double k[3]) {
     periodic[d] = present[d] && per[d] != 0;
     eikna[d] = std::complex<double>(1, 0);
     if (!periodic[d]) continue;
-    if (pml_dir[d]) throw Error("a direction cannot have both PML and Bloch-periodic boundaries");
     // the Brillouin-zone edge exactly: eikna = -1 (src/boundaries.cpp:98-103)
     if (k[d] * N[d] == 0.5 * g.a) eikna[d] = std::complex<double>(-1.0, 0.0); // -exp(-Im k ...), k real
     else eikna[d] = std::exp(std::complex<double>(0.0, 1.0) * std::complex<double>(k[d], 0.0) * ((2 * pi / g.a) * N[d]));

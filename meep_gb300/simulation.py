@@ -11,9 +11,10 @@ C++ drop-in (include/meep_gb300/meep.hpp) through its C interface
 (include/meep_gb300/mgb.h), which runs the CUDA engine.
 
 Differences from the reference, raised as errors where they would change
-results: no subpixel averaging (`eps_averaging` must be False), metallic cell
-walls only (`k_point` False), no symmetries, real fields, no material
-functions (per-point Python callables).
+results: no subpixel averaging (`eps_averaging` must be False), no
+symmetries, no material functions (per-point Python callables).  `k_point`
+gives Bloch-periodic walls (complex fields when it is nonzero), as in the
+reference.
 
     import meep_gb300 as mp
     sim = mp.Simulation(cell_size=mp.Vector3(16, 8), resolution=10,
@@ -369,7 +370,8 @@ _SIGS = [
     ("mgb_time", C.c_int, [_P, _DP, _DP, _DP, C.POINTER(C.c_int)]),
     ("mgb_get_field_points", C.c_int, [_P, C.c_int, C.c_int, _DP, _DP, _DP]),
     ("mgb_get_epsilon_points", C.c_int, [_P, C.c_int, _DP, _DP]),
-    ("mgb_yee_array", C.c_int, [_P, C.c_int, _DP, C.POINTER(C.c_longlong)]),
+    ("mgb_yee_array", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_longlong)]),
+    ("mgb_use_bloch", C.c_int, [_P, _DP]),
 ]
 
 _LIBS = {}
@@ -433,12 +435,11 @@ class Simulation:
         bad = set(kwargs) - _IGNORED_KWARGS
         if bad:
             raise TypeError("Simulation got unexpected keyword arguments %s" % sorted(bad))
-        if eps_averaging:
+        if eps_averaging and geometry:
+            # without geometric objects the medium is uniform and averaging
+            # changes nothing
             raise NotImplementedError("meep: subpixel averaging (eps_averaging=True, the reference's default) is "
                                       "not supported by the GB300 engine; pass eps_averaging=False")
-        if k_point not in (False, None):
-            raise NotImplementedError("meep: Bloch-periodic boundaries (k_point) are not supported by the GB300 "
-                                      "engine; the cell walls are metallic")
         if symmetries:
             raise NotImplementedError("meep: symmetries are not supported by the GB300 engine")
         if force_complex_fields:
@@ -454,6 +455,7 @@ class Simulation:
         self.sources = list(sources or [])
         self.boundary_layers = list(boundary_layers or [])
         self.default_material = default_material
+        self.k_point = _v3(k_point) if k_point not in (False, None) else False
         self.Courant = float(Courant)
         self.dft_objects = []
         self._lib = _load(_library or PRODUCT_LIB)
@@ -514,6 +516,11 @@ class Simulation:
                                          len(media), med, 0, len(self.geometry), objs, len(sus_keys), sus,
                                          C.byref(h)))
         self._h = h
+        if self.k_point is not False:
+            # Bloch-periodic walls in every direction (Simulation._init_fields);
+            # complex fields when k != 0
+            k_a, k_p = _arr(list(self.k_point))
+            self._check(self._lib.mgb_use_bloch(self._h, k_p))
         for s in self.sources:
             kind, params = s.src._params()
             p_a, p_p = _arr(params)
@@ -699,16 +706,20 @@ class Simulation:
         return np.squeeze(out.reshape(shape))
 
 
-    def get_yee_array(self, component):
+    def get_yee_array(self, component, cmplx=False):
         """Component `component` at every point of its own Yee grid over the
         whole cell (N_d + 1 points per direction, x slowest): the values the
         engine stores, without interpolation (an addition to the reference's
         interface)."""
         self.init_sim()
         n = C.c_longlong()
-        self._check(self._lib.mgb_yee_array(self._h, component, None, C.byref(n)))
+        self._check(self._lib.mgb_yee_array(self._h, component, 0, None, C.byref(n)))
         out = np.zeros(n.value)
-        self._check(self._lib.mgb_yee_array(self._h, component, out.ctypes.data_as(_DP), C.byref(n)))
+        self._check(self._lib.mgb_yee_array(self._h, component, 0, out.ctypes.data_as(_DP), C.byref(n)))
+        if cmplx:
+            im = np.zeros(n.value)
+            self._check(self._lib.mgb_yee_array(self._h, component, 1, im.ctypes.data_as(_DP), C.byref(n)))
+            out = out + 1j * im
         dims = [d for d in range(3) if (self.dimensions == 3 or (self.dimensions == 2 and d < 2)
                                          or (self.dimensions == 1 and d == 2))]
         shape = tuple(int(round(self.cell_size[d] * self.resolution)) + 1 for d in dims)

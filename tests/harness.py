@@ -70,7 +70,7 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
-                   nsrc=3, steps=60, n=None, bloch=None):
+                   nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -95,8 +95,8 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
         for d in range(dim if dim == 3 else 2):
             for side in (0, 1):
                 pmlspec[(d, side)] = (float(rng.choice([0.3, 0.5])), 1e-15, 1.0)
-                if bloch is not None and d in bloch:
-                    del pmlspec[(d, side)]  # periodic direction: no PML
+                if bloch is not None and d in bloch and not bloch_pml:
+                    del pmlspec[(d, side)]  # periodic direction without PML
     sim = sim_factory(dim=dim, n=n, io=io, a=a, courant=0.5, pml=pmlspec, precision=precision,
                       components=comps)
     if bloch is not None:

@@ -58,6 +58,16 @@ def test_bloch_fp64_bitwise_class(dim, seed, bloch, engine_lib, oracle_lib):
         assert relerr(g[k], o[k]) <= 1e-12, (k, relerr(g[k], o[k]))
 
 
+def test_bloch_with_pml_fp64_bitwise_class(engine_lib, oracle_lib):
+    """periodic boundaries behind PML in the same direction (Simulation with
+    k_point and PML layers)"""
+    for dim, seed, bloch in ((2, 36, {0: 0.0, 1: 0.0}), (3, 37, {0: 0.15, 1: 0.0, 2: 0.05})):
+        g = _run(engine_lib, seed, dim, 64, bloch=bloch, bloch_pml=True)
+        o = _run(oracle_lib, seed, dim, 64, bloch=bloch, bloch_pml=True)
+        for k in o:
+            assert relerr(g[k], o[k]) <= 1e-12, (dim, k, relerr(g[k], o[k]))
+
+
 def test_bloch_fp32_close(engine_lib, oracle_lib):
     g = _run(engine_lib, 35, 3, 32, bloch={0: 0.2, 1: 0.1})
     o = _run(oracle_lib, 35, 3, 64, bloch={0: 0.2, 1: 0.1})

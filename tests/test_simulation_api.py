@@ -100,10 +100,8 @@ def test_run_until_step_count(oracle_meep_lib):
 
 def test_unsupported_options_raise(oracle_meep_lib):
     with pytest.raises(NotImplementedError, match="eps_averaging"):
-        mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, _library=oracle_meep_lib)
-    with pytest.raises(NotImplementedError, match="k_point"):
-        mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, eps_averaging=False, k_point=mp.Vector3(),
-                      _library=oracle_meep_lib)
+        mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, _library=oracle_meep_lib,
+                      geometry=[mp.Block(mp.Vector3(1, 1), material=mp.Medium(epsilon=2))])
     with pytest.raises(NotImplementedError, match="material functions"):
         mp.Block(mp.Vector3(1, 1), material=lambda p: mp.Medium(epsilon=2))
 
@@ -127,3 +125,25 @@ def test_scripts_fp32_on_gpu(engine_lib):
             if k in ref64:
                 bound = max(3 * relerr(ref32[k], ref64[k]), 1e-5)
                 assert relerr(np.reshape(out[k], -1), ref64[k]) <= bound, (case, k)
+
+
+def integrated_source_std(lib):
+    """The reference's python/tests/test_integrated_source.py: an
+    is_integrated=True line source extending into the PML of a periodic cell
+    (k_point = 0) makes a planewave, so Ez on a parallel line is constant."""
+    sources = [mp.Source(mp.ContinuousSource(1, is_integrated=True), center=mp.Vector3(-2), size=mp.Vector3(y=6),
+                         component=mp.Ez)]
+    sim = mp.Simulation(resolution=20, cell_size=(6, 6), boundary_layers=[mp.PML(thickness=1)], sources=sources,
+                        k_point=mp.Vector3(), _library=lib)
+    sim.run(until=30)
+    ez = sim.get_array(mp.Ez, center=mp.Vector3(2), size=mp.Vector3(y=6))
+    return np.std(ez) / np.sqrt(np.mean(ez ** 2))
+
+
+def test_integrated_source_planewave_on_oracle(oracle_meep_lib):
+    assert abs(integrated_source_std(oracle_meep_lib)) < 1e-8
+
+
+@pytest.mark.gpu
+def test_integrated_source_planewave_on_gpu(engine_lib):
+    assert abs(integrated_source_std(PRODUCT_LIB)) < 1e-8
