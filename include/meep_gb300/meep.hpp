@@ -372,8 +372,12 @@ public:
     (void)r;
     return 0.0;
   }
-  // Effective inverse-permittivity row; without subpixel averaging this is
-  // 1/chi1p1 at the centre of the pixel (src/anisotropic_averaging.cpp:89-98).
+  // Gradient of chi1p1 over the pixel v by a sphere quadrature, zero where
+  // the material is uniform (src/anisotropic_averaging.cpp:60-85).
+  vec normal_vector(field_type ft, const volume &v);
+  // Effective inverse-permittivity row of the pixel v: 1/chi1p1 at its centre
+  // when maxeval == 0 or the material is uniform there, else the averaged
+  // tensor row (src/anisotropic_averaging.cpp:87-208).
   virtual void eff_chi1inv_row(component c, double chi1inv_row[3], const volume &v,
                                double tol = DEFAULT_SUBPIXEL_TOL,
                                int maxeval = DEFAULT_SUBPIXEL_MAXEVAL);
@@ -452,10 +456,19 @@ public:
             double tol = DEFAULT_SUBPIXEL_TOL, int maxeval = DEFAULT_SUBPIXEL_MAXEVAL);
   ~structure();
 
-  void set_materials(material_function &mat, bool use_anisotropic_averaging = false,
+  void set_materials(material_function &mat, bool use_anisotropic_averaging = true,
                      double tol = DEFAULT_SUBPIXEL_TOL, int maxeval = DEFAULT_SUBPIXEL_MAXEVAL);
-  void set_epsilon(material_function &eps, bool use_anisotropic_averaging = false,
+  void set_epsilon(material_function &eps, bool use_anisotropic_averaging = true,
                    double tol = DEFAULT_SUBPIXEL_TOL, int maxeval = DEFAULT_SUBPIXEL_MAXEVAL);
+  void set_epsilon(double eps(const vec &), bool use_anisotropic_averaging = true,
+                   double tol = DEFAULT_SUBPIXEL_TOL, int maxeval = DEFAULT_SUBPIXEL_MAXEVAL);
+  // inverse-permittivity tensor entry (c, d) at a grid point owned by the
+  // cell (frequency 0 only); 0 elsewhere (src/monitor.cpp:196-212)
+  std::complex<double> get_chi1inv(component c, direction d, const ivec &origloc, double frequency = 0,
+                                   bool parallel = true) const;
+  std::complex<double> get_inveps(component c, direction d, const ivec &origloc, double frequency = 0) const {
+    return get_chi1inv(c, d, origloc, frequency);
+  }
   void set_conductivity(component c, material_function &conductivity);
   void set_conductivity(component c, double Cfunc(const vec &));
   void add_susceptibility(material_function &sigma, field_type ft, const susceptibility &sus);

@@ -83,7 +83,8 @@ def build_engine(force=False, verbose=False):
     objs = [os.path.join(objdir, f) for f in ("mfd_cuda_f64.o", "mfd_cuda_f32.o", "mfd_noalloc.o",
                                                "mfd_plan.o", "mfd_capi.o")]
     _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
-    api = [os.path.join(CSRC, "meep_api.cpp"), os.path.join(CSRC, "meep_pyshim.cpp")]
+    api = [os.path.join(CSRC, "meep_api.cpp"), os.path.join(CSRC, "meep_pyshim.cpp"),
+           os.path.join(CSRC, "sphere_quadrature.cpp")]
     links = []
     for name, flag in (("libmeep_gb300.so", []), ("libmeep_gb300_single.so", ["-DMEEP_SINGLE=1"])):
         links.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"] + flag + INC +

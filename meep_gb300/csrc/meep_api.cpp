@@ -22,6 +22,7 @@
 #include <map>
 
 #include "mfd.h"
+#include "subpixel.hpp"
 
 namespace meep {
 
@@ -159,12 +160,56 @@ boundary_region pml(double thickness, double Rasymptotic, double mean_stretch) {
   return r;
 }
 
+/* Subpixel averaging through the shared host/device routine (subpixel.hpp):
+   the pixel as [lo, hi] in x, y, z order, chi1p1 called with a vec of the
+   grid's dimension. */
+static int subpixel_dim(ndim dim) {
+  if (dim == D1) return 1;
+  if (dim == D2) return 2;
+  if (dim == D3) return 3;
+  meep::abort("subpixel averaging in cylindrical coordinates is not supported by the GB300 engine");
+}
+
+static void volume_box(const volume &v, double lo[3], double hi[3]) {
+  for (int d = 0; d < 3; d++) {
+    lo[d] = hi[d] = 0.0;
+  }
+  LOOP_OVER_DIRECTIONS(v.dim, d) {
+    lo[d] = v.in_direction_min(d);
+    hi[d] = v.in_direction_max(d);
+  }
+}
+
+namespace {
+struct ChiOf {
+  material_function *m;
+  field_type ft;
+  ndim dim;
+  double operator()(const double p[3]) const {
+    vec r(dim);
+    LOOP_OVER_DIRECTIONS(dim, d) r.set_direction(d, p[d]);
+    return m->chi1p1(ft, r);
+  }
+};
+} // namespace
+
+vec material_function::normal_vector(field_type ft, const volume &v) {
+  double lo[3], hi[3], g[3];
+  volume_box(v, lo, hi);
+  mgb_subpixel::normal_vector(subpixel_dim(v.dim), lo, hi, mgb_subpixel::sphere_quadrature(),
+                              ChiOf{this, ft, v.dim}, g);
+  vec out(v.dim);
+  LOOP_OVER_DIRECTIONS(v.dim, d) out.set_direction(d, g[d]);
+  return out;
+}
+
 void material_function::eff_chi1inv_row(component c, double chi1inv_row[3], const volume &v,
                                         double tol, int maxeval) {
-  (void)tol;
-  (void)maxeval;
-  chi1inv_row[0] = chi1inv_row[1] = chi1inv_row[2] = 0.0;
-  chi1inv_row[component_direction(c) % 3] = 1 / chi1p1(type(c), v.center());
+  double lo[3], hi[3];
+  volume_box(v, lo, hi);
+  mgb_subpixel::eff_chi1inv_row(subpixel_dim(v.dim), component_direction(c) % 3, lo, hi, tol, maxeval,
+                                mgb_subpixel::sphere_quadrature(), ChiOf{this, type(c), v.dim},
+                                chi1inv_row);
 }
 
 std::vector<double> linspace(double freq_min, double freq_max, size_t Nfreq) {
@@ -263,8 +308,7 @@ structure::structure(const grid_volume &thegv, material_function &eps, const bou
       d(new impl) {
   (void)s;
   (void)num_chunks;
-  if (use_aa) meep::abort("subpixel averaging is not supported by the GB300 engine");
-  set_materials(eps, false, tol, maxeval);
+  set_materials(eps, use_aa, tol, maxeval);
 }
 
 static material_function *new_simple(double f(const vec &)) { return new simple_material_function(f); }
@@ -276,9 +320,8 @@ structure::structure(const grid_volume &thegv, double epsf(const vec &), const b
       d(new impl) {
   (void)s;
   (void)num_chunks;
-  if (use_aa) meep::abort("subpixel averaging is not supported by the GB300 engine");
   std::unique_ptr<material_function> m(new_simple(epsf));
-  set_materials(*m, false, tol, maxeval);
+  set_materials(*m, use_aa, tol, maxeval);
 }
 
 structure::~structure() {}
@@ -295,11 +338,12 @@ void structure::set_materials(material_function &mat, bool use_aa, double tol, i
       meep::abort("nonlinear susceptibilities are not supported by the GB300 engine");
 }
 
-// set_chi1inv without averaging: row from the pixel at the point, off-diagonal
-// entries from the pixel shifted by -1 along the component direction
+// set_chi1inv: the diagonal entry from the pixel centred at the point, the
+// off-diagonal entries from the pixel shifted half a cell back along the
+// component direction; entries equal to the identity everywhere are dropped
 // (src/anisotropic_averaging.cpp:211-324).
 void structure::set_epsilon(material_function &mat, bool use_aa, double tol, int maxeval) {
-  if (use_aa) meep::abort("subpixel averaging is not supported by the GB300 engine");
+  if (!use_aa) maxeval = 0;
   Dense dn(gv);
   const component ecs[3] = {Ex, Ey, Ez};
   for (component c : ecs) {
@@ -355,6 +399,27 @@ void structure::set_conductivity(component c, material_function &C) {
     if (v != 0.0) trivial = false;
   });
   d->cond[which][cd] = trivial ? std::vector<double>() : arr;
+}
+
+void structure::set_epsilon(double epsf(const vec &), bool use_aa, double tol, int maxeval) {
+  std::unique_ptr<material_function> m(new_simple(epsf));
+  set_epsilon(*m, use_aa, tol, maxeval);
+}
+
+std::complex<double> structure::get_chi1inv(component c, direction dd, const ivec &origloc, double frequency,
+                                            bool parallel) const {
+  (void)parallel;
+  if (frequency != 0) meep::abort("frequency-dependent chi1inv is not supported by the GB300 engine");
+  if (!gv.owns(origloc)) return 0.0;
+  const direction cd = component_direction(c);
+  const double ident = dd == cd ? 1.0 : 0.0;
+  if (!is_electric(c) || cd > Z || dd > Z) return ident;
+  const std::vector<double> &arr = d->chi1inv[cd][dd];
+  if (arr.empty()) return ident;
+  Dense dn(gv);
+  int k[3];
+  dn.kof(gv, c, origloc, k);
+  return arr[dn.index(k)];
 }
 
 void structure::set_conductivity(component c, double Cfunc(const vec &)) {

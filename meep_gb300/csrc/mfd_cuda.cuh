@@ -201,6 +201,14 @@ template <typename R> struct EArgs {
   int npoles;
   PoleArgs<R> pole[MAX_POLES];
   Box box;
+  // dfield already holds D - P - integrated sources (off-diagonal update:
+  // f_minus_p of every D component is formed before any E is computed)
+  int pre;
+  // off-diagonal terms: D component g[q] along direction with stride so[q],
+  // weights u[q]; s = stride along dir
+  int noff;
+  const R *og[2], *ou[2];
+  long long so[2], s;
 };
 
 template <typename R> struct EPoint {
@@ -215,23 +223,32 @@ __device__ __forceinline__ void e_point(const Geo &g, const Tables<R> &tb, const
                                         const int k[3], long long i, int nsrc, const R *srcA,
                                         EPoint<R> &out) {
   R gs = a.dfield[i];
-  for (int q = 0; q < a.npoles; q++)
-    if (a.pole[q].P) gs -= a.pole[q].P[i];
+  if (!a.pre)
+    for (int q = 0; q < a.npoles; q++)
+      if (a.pole[q].P) gs -= a.pole[q].P[i];
   for (int j = 0; j < nsrc; j++)
     gs -= srcA[j];
   const R us = a.chi[i];
+  R val = (gs * us);
+  // OFFDIAG(u, g, sx) = 0.25 ((g[i] + g[i-sx]) u[i] + (g[i+s] + g[i+s-sx]) u[i+s])
+  // (src/step_generic.cpp:580-582)
+  for (int q = 0; q < a.noff; q++) {
+    const R *og = a.og[q], *ou = a.ou[q];
+    const long long sx = a.so[q], s = a.s;
+    val = val + R(0.25) * ((og[i] + og[i - sx]) * ou[i] + (og[i + s] + og[(i + s) - sx]) * ou[i + s]);
+  }
   const int kw = a.shift[a.dir] + 2 * k[a.dir];
   const bool w = slab(g, a.dir, kw);
   R W;
   if (w) {
     R fwprev = a.fw[i], kapwkw = tb.kap[a.dir][kw], sigwkw = tb.sig[a.dir][kw];
-    R fwn = (gs * us);
+    R fwn = val;
     out.fw = fwn;
     out.e = a.e[i] + ((kapwkw + sigwkw) * fwn - (kapwkw - sigwkw) * fwprev);
     W = fwn;
   }
   else {
-    out.e = (gs * us);
+    out.e = val;
     out.fw = R(0);
     W = out.e;
   }
@@ -298,6 +315,40 @@ __global__ void src_pre_kernel(Geo g, Tables<R> tb, EArgs<R> a, const SrcPoint *
     A[t] = R(re);
   }
   e_point(g, tb, a, sp.k, sp.i, sp.nterm, A, out[j]);
+}
+
+// f_minus_p of one D component over the whole storage: D minus the
+// polarizations in list order (src/update_eh.cpp:108-123, subtract_P
+// src/susceptibility.cpp:264-279); used by the off-diagonal E update, which
+// reads D - P of the other components at neighbouring points
+template <typename R> struct FmpArgs {
+  R *out;
+  const R *d;
+  const R *p[MAX_POLES];
+  int np;
+  long long n;
+};
+
+template <typename R> __global__ void fmp_kernel(FmpArgs<R> a) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  R v = a.d[i];
+  for (int q = 0; q < a.np; q++)
+    if (a.p[q]) v -= a.p[q][i];
+  a.out[i] = v;
+}
+
+// integrated E sources subtracted from f_minus_p (src/update_eh.cpp:126-137)
+template <typename R> __global__ void src_fmp_kernel(R *fmp, const SrcPoint *pts, int n, DipoleVals dv) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const SrcPoint &sp = pts[j];
+  R v = fmp[sp.i];
+  for (int t = 0; t < sp.nterm; t++) {
+    const double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
+    v -= R(re);
+  }
+  fmp[sp.i] = v;
 }
 
 template <typename R>
@@ -616,6 +667,12 @@ public:
   Tables<R> tb{};
   R *f[NC] = {}, *fu[NC] = {}, *fw[NC] = {}, *fcnd[NC] = {}, *chi[NC] = {}, *cnd[NC] = {},
     *cndinv[NC] = {};
+  // off-diagonal chi1inv of E along d (terms in Plan::offdiag order) and the
+  // f_minus_p buffers of the off-diagonal update (one per D component that
+  // has polarizations or integrated sources; shared by the two parts of
+  // complex fields, which are updated one after the other)
+  R *chioff[3][2] = {};
+  R *fmp[3] = {};
   struct DPole {
     R *P[3] = {}, *PP[3] = {}, *s[3] = {};
     R *Pim[3] = {}, *PPim[3] = {}; // imaginary parts (complex fields)
@@ -648,25 +705,38 @@ public:
     }
     return o;
   }
+  // Bloch-periodic ghost plane along d of one array pair, for a component
+  // whose shift along d is 0 (shift0) or 1
+  void ghost_plane(const Plan &p, int d, bool shift0, R *re, R *im) {
+    int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+    if (o1 > o2) std::swap(o1, o2);
+    const std::complex<double> ph = shift0 ? std::conj(p.eikna[d]) : p.eikna[d];
+    const long long dst = shift0 ? 0 : (long long)p.N[d] * p.stride[d];
+    const long long src = shift0 ? (long long)p.N[d] * p.stride[d] : 0;
+    const int n1 = p.ext[o1], n2 = p.ext[o2];
+    const dim3 grid((unsigned)((n2 + 127) / 128), (unsigned)n1);
+    ghost_plane_kernel<R><<<grid, 128, 0, stream>>>(re, im, dst, src, n1, n2, (long long)p.stride[o1],
+                                                    (long long)p.stride[o2], R(ph.real()), R(ph.imag()));
+    nlaunch++;
+  }
   // Bloch-periodic ghost planes of the components of field types t0, t1
   void ghost_copy(const Plan &p, int t0, int t1) {
     for (int d = 0; d < 3; d++) {
       if (!p.periodic[d]) continue;
-      int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
-      if (o1 > o2) std::swap(o1, o2);
       for (int c = 0; c < NC; c++) {
         if (!f[c] || (ctype(c) != t0 && ctype(c) != t1)) continue;
-        const bool s0 = p.shift[c][d] == 0;
-        const std::complex<double> ph = s0 ? std::conj(p.eikna[d]) : p.eikna[d];
-        const long long dst = s0 ? 0 : (long long)p.N[d] * p.stride[d];
-        const long long src = s0 ? (long long)p.N[d] * p.stride[d] : 0;
-        const int n1 = p.ext[o1], n2 = p.ext[o2];
-        const dim3 grid((unsigned)((n2 + 127) / 128), (unsigned)n1);
-        ghost_plane_kernel<R><<<grid, 128, 0, stream>>>(f[c], cplx ? fim[c] : nullptr, dst, src, n1, n2,
-                                                        (long long)p.stride[o1], (long long)p.stride[o2],
-                                                        R(ph.real()), R(ph.imag()));
-        nlaunch++;
+        ghost_plane(p, d, p.shift[c][d] == 0, f[c], cplx ? fim[c] : nullptr);
       }
+    }
+  }
+  // polarizations of E at the not-owned points (the reference's PE_stuff
+  // boundary step, src/step.cpp:116-119); read by the off-diagonal update
+  void ghost_copy_pols(const Plan &p) {
+    for (int d = 0; d < 3; d++) {
+      if (!p.periodic[d]) continue;
+      for (DPole &dp : poles)
+        for (int e = 0; e < 3; e++)
+          if (dp.P[e]) ghost_plane(p, d, p.shift[comp(MFD_E, e)][d] == 0, dp.P[e], cplx ? dp.Pim[e] : nullptr);
     }
   }
   // sources
@@ -733,6 +803,7 @@ public:
   }
 
   void setup(Plan &p) override {
+    p.plan_offdiag();
     for (int d = 0; d < 3; d++) {
       geo.N[d] = p.N[d];
       geo.T[d][0] = p.T[d][0];
@@ -785,11 +856,9 @@ public:
       }
       if ((t == MFD_E || t == MFD_H) && p.pml_dir[d]) fw[c] = dzeros<R>(p.nstore);
       if (t == MFD_E) {
-        for (int dd = 0; dd < 3; dd++)
-          if (dd != d && !p.chi1inv[c][dd].empty())
-            for (double v : p.chi1inv[c][dd])
-              if (v != 0.0) throw Error("off-diagonal chi1inv is not supported yet by the CUDA engine");
         chi[c] = dupload(to_store(p, p.chi1inv[c][d], 1.0));
+        for (int q = 0; q < p.offdiag[d].n; q++)
+          chioff[d][q] = dupload(to_store(p, p.chi1inv[c][p.offdiag[d].dir[q]], 0.0));
       }
       if (t == MFD_H)
         for (int dd = 0; dd < 3; dd++)
@@ -830,6 +899,14 @@ public:
           }
     }
     setup_sources(p);
+    if (p.any_offdiag)
+      for (int d = 0; d < 3; d++) {
+        if (!p.have[comp(MFD_E, d)]) continue;
+        bool need = nsrcpts[d] > 0;
+        for (const DPole &dp : poles)
+          need = need || dp.P[d] != nullptr;
+        if (need) fmp[d] = dzeros<R>(p.nstore);
+      }
     int mask = 0;
     for (int c = 0; c < NC; c++)
       if (p.have[c]) mask |= 1 << c;
@@ -840,6 +917,7 @@ public:
       has_b_current = has_b_current || ncur[comp(MFD_B, d)] > 0;
     if (getenv("MFD_GENERIC_KERNELS")) fused_mask = -1;
     if (p.any_periodic()) fused_mask = -1; // Bloch boundaries: the per-component kernels
+    if (p.any_offdiag) fused_mask = -1;    // off-diagonal chi1inv: E needs D of all components first
     if (fused_mask >= 0) plan_boxes(p);
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
   }
@@ -1464,7 +1542,54 @@ public:
     return a;
   }
 
+  // E from f_minus_p of all D components (off-diagonal chi1inv): f_minus_p
+  // first, then every E component with its OFFDIAG terms and poles
+  void update_e_offdiag(Plan &p, const DipoleVals &dip) {
+    for (int d = 0; d < 3; d++) {
+      if (!fmp[d]) continue;
+      FmpArgs<R> fa{};
+      fa.out = fmp[d];
+      fa.d = f[comp(MFD_D, d)];
+      fa.np = (int)poles.size();
+      for (int q = 0; q < fa.np; q++)
+        fa.p[q] = poles[q].P[d];
+      fa.n = p.nstore;
+      fmp_kernel<R><<<(unsigned)((p.nstore + 255) / 256), 256, 0, stream>>>(fa);
+      nlaunch++;
+      if (nsrcpts[d]) {
+        src_fmp_kernel<R><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(fmp[d], d_srcpts[d], nsrcpts[d], dip);
+        nlaunch++;
+      }
+    }
+    for (int d = 0; d < 3; d++) {
+      int ec = comp(MFD_E, d);
+      if (!p.have[ec]) continue;
+      EArgs<R> a = eargs(p, d);
+      if (box_empty(a.box)) continue;
+      if (fmp[d]) {
+        a.dfield = fmp[d];
+        a.pre = 1;
+      }
+      a.noff = p.offdiag[d].n;
+      a.s = (long long)p.stride[d];
+      for (int q = 0; q < a.noff; q++) {
+        const int od = p.offdiag[d].dir[q];
+        a.og[q] = fmp[od] ? fmp[od] : f[comp(MFD_D, od)];
+        a.ou[q] = chioff[d][q];
+        a.so[q] = (long long)p.stride[od];
+      }
+      dim3 grid, block;
+      launch_dims(a.box, grid, block);
+      e_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+      nlaunch++;
+    }
+  }
+
   void update_e(Plan &p, const DipoleVals &dip) {
+    if (p.any_offdiag) {
+      update_e_offdiag(p, dip);
+      return;
+    }
     for (int d = 0; d < 3; d++) {
       int ec = comp(MFD_E, d);
       if (!p.have[ec]) continue;
@@ -1584,8 +1709,19 @@ public:
         for (int d = 0; d < 3; d++)
           if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
         step_current(p, MFD_D, part ? imag_part(curd) : curd);
-        update_e(p, part ? imag_part(dip) : dip);
+        if (!p.any_offdiag) update_e(p, part ? imag_part(dip) : dip);
         if (part) swap_parts();
+      }
+      if (p.any_offdiag) {
+        // the off-diagonal terms read D (and P) at the not-owned points:
+        // fill them first, as the reference's D boundary step does
+        ghost_copy(p, MFD_D, MFD_D);
+        for (int part = 0; part < nparts; part++) {
+          if (part) swap_parts();
+          update_e(p, part ? imag_part(dip) : dip);
+          if (part) swap_parts();
+        }
+        ghost_copy_pols(p);
       }
       ghost_copy(p, MFD_D, MFD_E);
     }
@@ -1634,6 +1770,8 @@ public:
     for (int c : comps)
       if (ctype(c) != MFD_E || !p.have[c]) throw Error("design components must be allocated E components");
     if (!p.poles.empty()) throw Error("the adjoint does not support dispersive materials yet");
+    p.plan_offdiag();
+    if (p.any_offdiag) throw Error("the adjoint does not support off-diagonal chi1inv yet");
     for (int c = 0; c < NC; c++)
       if (!p.cond[c].empty()) throw Error("the adjoint does not support conductivity yet");
     dcomps = comps;

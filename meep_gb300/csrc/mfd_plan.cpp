@@ -2,6 +2,8 @@
 // source time functions.  See mfd_plan.hpp for the model.
 #include "mfd_plan.hpp"
 
+#include <utility>
+
 #include <cmath>
 #include <cstring>
 
@@ -283,6 +285,35 @@ void Plan::compute_cond_chunks(int c) {
             }
         cond_chunk[c][rx * 9 + ry * 3 + rz] = any;
       }
+}
+
+void Plan::plan_offdiag() {
+  any_offdiag = false;
+  for (int d = 0; d < 3; d++) {
+    OffDiag &od = offdiag[d];
+    od = OffDiag();
+    const int ec = comp(MFD_E, d);
+    if (!have[ec]) continue;
+    int dir[2] = {cycle(d, 1), cycle(d, 2)};
+    bool g[2], u[2];
+    for (int q = 0; q < 2; q++) {
+      g[q] = have[comp(MFD_D, dir[q])];
+      u[q] = false;
+      if (g[q])
+        for (double v : chi1inv[ec][dir[q]])
+          if (v != 0.0) {
+            u[q] = true;
+            break;
+          }
+    }
+    if ((!g[0] && g[1]) || (g[0] && g[1] && !u[0] && u[1])) {
+      std::swap(dir[0], dir[1]);
+      std::swap(u[0], u[1]);
+    }
+    if (u[0]) od.dir[od.n++] = dir[0];
+    if (u[0] && u[1]) od.dir[od.n++] = dir[1];
+    any_offdiag = any_offdiag || od.n > 0;
+  }
 }
 
 void Plan::set_bloch(const int per[3], const double k[3]) {

@@ -139,6 +139,20 @@ public:
   std::vector<SourceGroup> sources;
   std::vector<Monitor> monitors;
 
+  // Off-diagonal inverse-permittivity terms of the E update: for E along d,
+  // E = chi_dd (D-P)_d + OFFDIAG over the D components along dir[0], dir[1]
+  // (in this order), each the 4-point average of that D component around
+  // the E point weighted by chi_d,dir at the two E-direction neighbours
+  // (src/update_eh.cpp:179-192; swap rule and OFFDIAG
+  // src/step_generic.cpp:574-582).  An entry counts when its array holds a
+  // nonzero value.  Set by plan_offdiag() once the materials are final.
+  struct OffDiag {
+    int n = 0;
+    int dir[2] = {-1, -1};
+  } offdiag[3];
+  bool any_offdiag = false;
+  void plan_offdiag();
+
   explicit Plan(const mfd_grid &grid);
 
   // chunk region of half-pixel position pos along d: 0 low slab, 1 interior, 2 high slab

@@ -36,6 +36,7 @@ public:
 
   std::vector<R> f[NC], fu[NC], fw[NC], fcnd[NC], fmp[NC];
   std::vector<R> chi[NC], cnd[NC], cndinv[NC];
+  std::vector<R> chioff[3][2]; // off-diagonal chi1inv of E along d, terms in Plan::offdiag order
   std::vector<R> sig[3], kap[3], siginv[3];
   struct PoleData {
     std::vector<R> P[3], PP[3], s[3];
@@ -74,30 +75,47 @@ public:
   // components = conj(eikna) x position 2N, position 2N+1 of shift-1
   // components = eikna x position 1 (src/boundaries.cpp:207-229,
   // src/step.cpp:172-222); product in complex<realnum>
+  // ghost plane along periodic d of one array (with its imaginary part for
+  // complex fields) of a component whose shift along d is shift0 ? 0 : 1
+  void ghost_plane(const Plan &p, int d, bool shift0, std::vector<R> &re, std::vector<R> *im) {
+    int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+    if (o1 > o2) std::swap(o1, o2);
+    const std::complex<double> ph = shift0 ? std::conj(p.eikna[d]) : p.eikna[d];
+    const std::complex<R> phr(R(ph.real()), R(ph.imag()));
+    const int64_t dst = shift0 ? 0 : (int64_t)p.N[d] * p.stride[d];
+    const int64_t src = shift0 ? (int64_t)p.N[d] * p.stride[d] : 0;
+    for (int j1 = 0; j1 < p.ext[o1]; j1++)
+      for (int j2 = 0; j2 < p.ext[o2]; j2++) {
+        const int64_t o = j1 * p.stride[o1] + j2 * p.stride[o2];
+        if (im) {
+          const std::complex<R> v = phr * std::complex<R>(re[src + o], (*im)[src + o]);
+          re[dst + o] = v.real();
+          (*im)[dst + o] = v.imag();
+        }
+        else
+          re[dst + o] = phr.real() * re[src + o];
+      }
+  }
   void ghost_copy(const Plan &p, int t0, int t1) {
     for (int d = 0; d < 3; d++) {
       if (!p.periodic[d]) continue;
-      int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
-      if (o1 > o2) std::swap(o1, o2);
       for (int c = 0; c < NC; c++) {
         if (f[c].empty() || (ctype(c) != t0 && ctype(c) != t1)) continue;
-        const bool s0 = p.shift[c][d] == 0;
-        const std::complex<double> ph = s0 ? std::conj(p.eikna[d]) : p.eikna[d];
-        const std::complex<R> phr(R(ph.real()), R(ph.imag()));
-        const int64_t dst = s0 ? 0 : (int64_t)p.N[d] * p.stride[d];
-        const int64_t src = s0 ? (int64_t)p.N[d] * p.stride[d] : 0;
-        for (int j1 = 0; j1 < p.ext[o1]; j1++)
-          for (int j2 = 0; j2 < p.ext[o2]; j2++) {
-            const int64_t o = j1 * p.stride[o1] + j2 * p.stride[o2];
-            if (cplx) {
-              const std::complex<R> v = phr * std::complex<R>(f[c][src + o], f_im[c][src + o]);
-              f[c][dst + o] = v.real();
-              f_im[c][dst + o] = v.imag();
-            }
-            else
-              f[c][dst + o] = phr.real() * f[c][src + o];
-          }
+        ghost_plane(p, d, p.shift[c][d] == 0, f[c], cplx ? &f_im[c] : nullptr);
       }
+    }
+  }
+  // polarizations of E at the not-owned points (the reference's PE_stuff
+  // boundary step, src/step.cpp:116-119); read by the off-diagonal update
+  void ghost_copy_pols(const Plan &p) {
+    for (int d = 0; d < 3; d++) {
+      if (!p.periodic[d]) continue;
+      for (size_t q = 0; q < poles.size(); q++)
+        for (int e = 0; e < 3; e++) {
+          if (poles[q].P[e].empty()) continue;
+          const bool s0 = p.shift[comp(MFD_E, e)][d] == 0;
+          ghost_plane(p, d, s0, poles[q].P[e], cplx ? &P_im[q * 3 + e] : nullptr);
+        }
     }
   }
 
@@ -118,6 +136,7 @@ public:
   }
 
   void setup(Plan &p) override {
+    p.plan_offdiag();
     for (int c = 0; c < NC; c++) {
       if (!p.have[c]) continue;
       f[c].assign(p.nstore, R(0));
@@ -137,13 +156,8 @@ public:
         fw[c].assign(p.nstore, R(0));
         if (t == MFD_E) {
           chi[c] = to_store(p, p.chi1inv[c][d], 1.0);
-          for (int dd = 0; dd < 3; dd++)
-            if (dd != d && !p.chi1inv[c][dd].empty()) {
-              bool any = false;
-              for (double v : p.chi1inv[c][dd])
-                any = any || v != 0.0;
-              if (any) throw Error("off-diagonal chi1inv is not supported by this backend");
-            }
+          for (int q = 0; q < p.offdiag[d].n; q++)
+            chioff[d][q] = to_store(p, p.chi1inv[c][p.offdiag[d].dir[q]], 0.0);
           fmp[comp(MFD_D, d)].assign(p.nstore, R(0));
         }
         else {
@@ -350,6 +364,18 @@ public:
       const R *G = fmp[dc].data(), *U = chi[ec].data();
       const bool pml = p.pml_dir[d];
       const int *klo = p.klo[ec], *khi = p.khi[ec];
+      // OFFDIAG(u, g, sx) = 0.25 ((g[i] + g[i-sx]) u[i] + (g[i+s] + g[i+s-sx]) u[i+s])
+      // with s the stride along d (src/step_generic.cpp:580-582)
+      const int noff = p.offdiag[d].n;
+      const R *OG[2] = {nullptr, nullptr}, *OU[2] = {nullptr, nullptr};
+      int64_t osx[2] = {0, 0};
+      for (int q = 0; q < noff; q++) {
+        const int od = p.offdiag[d].dir[q];
+        OG[q] = fmp[comp(MFD_D, od)].data();
+        OU[q] = chioff[d][q].data();
+        osx[q] = p.stride[od];
+      }
+      const int64_t s = p.stride[d];
 #pragma omp parallel for schedule(static)
       for (int k0 = klo[0]; k0 <= khi[0]; k0++)
         for (int k1 = klo[1]; k1 <= khi[1]; k1++)
@@ -358,13 +384,19 @@ public:
             const int64_t i = idx(p, k0, k1, k2);
             const int kw = p.shift[ec][d] + 2 * k[d];
             R gs = G[i], us = U[i];
+            R val = (gs * us);
+            for (int q = 0; q < noff; q++) {
+              const R *g = OG[q], *u = OU[q];
+              const int64_t sx = osx[q];
+              val = val + R(0.25) * ((g[i] + g[i - sx]) * u[i] + (g[i + s] + g[(i + s) - sx]) * u[i + s]);
+            }
             if (pml && p.in_slab(d, kw)) {
               R fwprev = FW[i], kapwkw = kap[d][kw], sigwkw = sig[d][kw];
-              FW[i] = (gs * us);
+              FW[i] = val;
               E[i] += (kapwkw + sigwkw) * FW[i] - (kapwkw - sigwkw) * fwprev;
             }
             else
-              E[i] = (gs * us);
+              E[i] = val;
           }
     }
     // update_pols(E): W = f_w inside the PML slab of the component, E elsewhere
@@ -534,8 +566,19 @@ public:
       for (int d = 0; d < 3; d++)
         if (p.have[comp(MFD_D, d)]) curl(p, comp(MFD_D, d));
       step_source(p, MFD_D, vals);
-      update_e(p, vals);
+      if (!p.any_offdiag) update_e(p, vals);
       if (q) swap_parts();
+    }
+    if (p.any_offdiag) {
+      // the off-diagonal terms read D (and P) at the not-owned points: fill
+      // them first, as the reference's D boundary step does before update_eh
+      ghost_copy(p, MFD_D, MFD_D);
+      for (int q = 0; q < nparts; q++) {
+        if (q) swap_parts();
+        update_e(p, vals);
+        if (q) swap_parts();
+      }
+      ghost_copy_pols(p);
     }
     ghost_copy(p, MFD_D, MFD_E);
     int64_t tn = t + 1;

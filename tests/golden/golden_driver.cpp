@@ -460,6 +460,265 @@ static void case_py_disp3d(Writer &w) {
   w.rec("Hy", global_field(f, gv, Hy));
 }
 
+/* ------------------------------------------ subpixel averaging, off-diagonal
+   Inverse-permittivity tensors with off-diagonal entries, from the default
+   subpixel averaging of scalar material functions (structure(...,
+   use_anisotropic_averaging = true), src/anisotropic_averaging.cpp) and from a
+   material that supplies them itself (as tests/pml.cpp's offdiag_material
+   does): the E update with OFFDIAG terms (src/step_generic.cpp:566-785),
+   inside PML, with polarizations and integrated sources (f_minus_p), and with
+   Bloch phases. */
+
+// chi1inv entry (c, d) at every Yee point of c (0 where the cell does not own
+// the point), same ordering as global_field
+static std::vector<double> global_chi1inv(structure &s, const grid_volume &gv, component c, direction dd) {
+  std::vector<double> out;
+  ivec io = gv.little_corner();
+  ivec sh = gv.iyee_shift(c);
+  int n[3] = {1, 1, 1};
+  direction ds[3];
+  int nd = 0;
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    ds[nd] = d;
+    n[nd] = gv.num_direction(d) + 1;
+    nd++;
+  }
+  for (int a = 0; a < n[0]; a++)
+    for (int b = 0; b < (nd > 1 ? n[1] : 1); b++)
+      for (int cc = 0; cc < (nd > 2 ? n[2] : 1); cc++) {
+        ivec p = io + sh;
+        int k[3] = {a, b, cc};
+        for (int q = 0; q < nd; q++)
+          p.set_direction(ds[q], p.in_direction(ds[q]) + 2 * k[q]);
+        out.push_back(real(s.get_chi1inv(c, dd, p, 0, false)));
+      }
+  return out;
+}
+
+static std::vector<double> global_field_im(fields &f, const grid_volume &gv, component c) {
+  std::vector<double> out;
+  ivec io = gv.little_corner();
+  ivec sh = gv.iyee_shift(c);
+  int n[3] = {1, 1, 1};
+  direction ds[3];
+  int nd = 0;
+  LOOP_OVER_DIRECTIONS(gv.dim, d) {
+    ds[nd] = d;
+    n[nd] = gv.num_direction(d) + 1;
+    nd++;
+  }
+  for (int a = 0; a < n[0]; a++)
+    for (int b = 0; b < (nd > 1 ? n[1] : 1); b++)
+      for (int cc = 0; cc < (nd > 2 ? n[2] : 1); cc++) {
+        ivec p = io + sh;
+        int k[3] = {a, b, cc};
+        for (int q = 0; q < nd; q++)
+          p.set_direction(ds[q], p.in_direction(ds[q]) + 2 * k[q]);
+        out.push_back(imag(f.get_field(c, p, false)));
+      }
+  return out;
+}
+
+// a disk and a slab tilted against the grid: interface normals in every
+// direction of the plane
+static double lens_eps2d(const vec &r) {
+  const double x = r.x(), y = r.y();
+  const double dx = x + 0.7, dy = y - 0.3;
+  if (dx * dx + dy * dy < 0.36) return 9.0;
+  if (x > 0 && std::fabs(0.6 * x + 0.8 * y - 0.4) < 0.25) return 4.0;
+  return 1.0;
+}
+static double lens_sigma2d(const vec &r) {
+  const double dx = r.x() + 0.7, dy = r.y() - 0.3;
+  return dx * dx + dy * dy < 0.36 ? 0.4 : 0.0;
+}
+static double lens_cond2d(const vec &r) {
+  return r.x() > 0 && std::fabs(0.6 * r.x() + 0.8 * r.y() - 0.4) < 0.25 ? 0.05 : 0.0;
+}
+
+// 2-D TE (Ex, Ey, Hz) through the averaged lens: PML, a Lorentzian in the
+// disk, D conductivity in the slab, an integrated Ey and a current Hz source
+static void case_aniso_te2d(Writer &w, int steps) {
+  grid_volume gv = vol2d(5.0, 4.0, 10.0);
+  gv.center_origin();
+  structure s(gv, lens_eps2d, pml(1.0), identity(), 0, 0.5, true);
+  s.set_conductivity(Dx, lens_cond2d);
+  s.set_conductivity(Dy, lens_cond2d);
+  s.add_susceptibility(lens_sigma2d, E_stuff, lorentzian_susceptibility(1.2, 0.1));
+  fields f(&s);
+  f.use_real_fields();
+  gaussian_src_time se(0.9, 0.6), sh(0.7, 0.5);
+  f.add_point_source(Ey, se, vec(0.3, -0.6));
+  sh.is_integrated = false;
+  f.add_point_source(Hz, sh, vec(-1.2, 1.0), complex<double>(0.5, 0.0));
+  std::vector<double> fr = {0.6, 0.75, 0.9, 1.05};
+  volume_list r(volume(vec(1.4, -1.2), vec(1.4, 1.2)), Sx, 1.0);
+  dft_flux flux = f.add_dft_flux(&r, fr.data(), fr.size(), true, true, 1);
+  for (int i = 0; i < steps; i++)
+    f.step();
+  sync_dfts(f);
+  double *F = flux.flux();
+  w.rec("flux", std::vector<double>(F, F + fr.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ex", global_field(f, gv, Ex));
+  w.rec("Ey", global_field(f, gv, Ey));
+  w.rec("Hz", global_field(f, gv, Hz));
+  w.rec("chi_ExX", global_chi1inv(s, gv, Ex, X));
+  w.rec("chi_ExY", global_chi1inv(s, gv, Ex, Y));
+  w.rec("chi_EyX", global_chi1inv(s, gv, Ey, X));
+  w.rec("chi_EyY", global_chi1inv(s, gv, Ey, Y));
+}
+
+// a sphere and a slab whose normal is along no axis: full 3x3 tensors
+static double lens_eps3d(const vec &r) {
+  const double dx = r.x() - 0.1, dy = r.y() + 0.05, dz = r.z() - 0.05;
+  if (dx * dx + dy * dy + dz * dz < 0.2025) return 6.0;
+  if (std::fabs(0.48 * r.x() + 0.6 * r.y() + 0.64 * r.z() + 0.45) < 0.2) return 3.0;
+  return 1.0;
+}
+static double lens_sigma3d(const vec &r) {
+  const double dx = r.x() - 0.1, dy = r.y() + 0.05, dz = r.z() - 0.05;
+  return dx * dx + dy * dy + dz * dz < 0.2025 ? 0.3 : 0.0;
+}
+
+static void case_aniso3d(Writer &w, int steps) {
+  grid_volume gv = vol3d(1.8, 1.8, 1.8, 10.0);
+  gv.center_origin();
+  structure s(gv, lens_eps3d, pml(0.4), identity(), 0, 0.5, true);
+  s.add_susceptibility(lens_sigma3d, E_stuff, lorentzian_susceptibility(1.0, 0.1));
+  fields f(&s);
+  f.use_real_fields();
+  gaussian_src_time se(0.8, 0.6);
+  f.add_point_source(Ex, se, vec(-0.3, 0.2, -0.1));
+  f.add_point_source(Ez, se, vec(0.25, -0.3, 0.2), complex<double>(0.7, 0.0));
+  std::vector<double> fr = {0.7, 0.8, 0.9};
+  volume_list r(volume(vec(-0.4, -0.4, 0.45), vec(0.4, 0.4, 0.45)), Sz, 1.0);
+  dft_flux flux = f.add_dft_flux(&r, fr.data(), fr.size(), true, true, 1);
+  for (int i = 0; i < steps; i++)
+    f.step();
+  sync_dfts(f);
+  double *F = flux.flux();
+  w.rec("flux", std::vector<double>(F, F + fr.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  const component cs[6] = {Ex, Ey, Ez, Hx, Hy, Hz};
+  const char *names[6] = {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"};
+  for (int i = 0; i < 6; i++)
+    w.rec(names[i], global_field(f, gv, cs[i]));
+  const char *dn[3] = {"X", "Y", "Z"};
+  for (int c = 0; c < 3; c++)
+    for (int d = 0; d < 3; d++)
+      w.rec(std::string("chi_") + names[c] + dn[d], global_chi1inv(s, gv, cs[c], direction(d)));
+}
+
+// a material with a constant xy off-diagonal tensor everywhere, PML included
+// (the tensor of tests/pml.cpp's offdiag_material, mu = 1)
+class xy_offdiag_material : public material_function {
+public:
+  double od;
+  explicit xy_offdiag_material(double o) : od(o) {}
+  virtual void eff_chi1inv_row(component c, double row[3], const volume &v, double tol, int maxeval) {
+    (void)v;
+    (void)tol;
+    (void)maxeval;
+    const double detinv = 1.0 / (1 + 2 * od);
+    row[0] = row[1] = row[2] = 0.0;
+    if (type(c) != E_stuff) {
+      row[component_direction(c) % 3] = 1.0;
+      return;
+    }
+    if (component_direction(c) == X) {
+      row[0] = (1 + od) * detinv;
+      row[1] = -od * detinv;
+    }
+    else if (component_direction(c) == Y) {
+      row[0] = -od * detinv;
+      row[1] = (1 + od) * detinv;
+    }
+    else
+      row[2] = 1.0;
+  }
+};
+
+static double unit_cond(const vec &) { return 0.3; }
+
+static void case_offdiag_te2d(Writer &w, int steps) {
+  grid_volume gv = vol2d(4.0, 4.0, 10.0);
+  gv.center_origin();
+  structure s(gv, one_eps, pml(1.0), identity(), 0, 0.5, false);
+  s.set_conductivity(Bz, unit_cond);
+  xy_offdiag_material mat(0.5);
+  s.set_materials(mat, false);
+  fields f(&s);
+  f.use_real_fields();
+  gaussian_src_time src(1.0, 0.5);
+  src.is_integrated = false;
+  f.add_point_source(Hz, src, gv.center() + vec(0.25, -0.15));
+  for (int i = 0; i < steps; i++)
+    f.step();
+  w.scalar("t", f.time());
+  w.rec("Ex", global_field(f, gv, Ex));
+  w.rec("Ey", global_field(f, gv, Ey));
+  w.rec("Hz", global_field(f, gv, Hz));
+}
+
+// periodic lattice of disks with a Bloch wavevector: complex fields whose
+// off-diagonal terms read D and P on the ghost planes
+static double disk_eps(const vec &r) {
+  vec p = r;
+  while (p.x() < -0.5)
+    p.set_direction(X, p.x() + 1.0);
+  while (p.x() > 0.5)
+    p.set_direction(X, p.x() - 1.0);
+  while (p.y() < -0.5)
+    p.set_direction(Y, p.y() + 1.0);
+  while (p.y() > 0.5)
+    p.set_direction(Y, p.y() - 1.0);
+  return p.x() * p.x() + p.y() * p.y() < 0.1 ? 8.0 : 1.0;
+}
+static double disk_sigma(const vec &r) { return disk_eps(r) > 1.0 ? 0.5 : 0.0; }
+
+static void case_aniso_bloch2d(Writer &w, int steps) {
+  grid_volume gv = voltwo(1.0, 1.0, 10.0);
+  structure s(gv, disk_eps, boundary_region(), identity(), 0, 0.5, true);
+  s.add_susceptibility(disk_sigma, E_stuff, lorentzian_susceptibility(0.9, 0.2));
+  fields f(&s);
+  f.use_bloch(vec(0.3, 0.1));
+  f.add_point_source(Hz, 0.5, 2.0, 0.0, 3.0, vec(0.3, 0.65), complex<double>(0.0, -1.0));
+  f.add_point_source(Ey, 0.6, 2.0, 0.0, 3.0, vec(0.7, 0.2), complex<double>(0.8, 0.3));
+  for (int i = 0; i < steps; i++)
+    f.step();
+  w.scalar("t", f.time());
+  const component cs[3] = {Ex, Ey, Hz};
+  const char *names[3] = {"Ex", "Ey", "Hz"};
+  for (int i = 0; i < 3; i++) {
+    w.rec(names[i], global_field(f, gv, cs[i]));
+    w.rec(std::string(names[i]) + "_im", global_field_im(f, gv, cs[i]));
+  }
+  w.rec("chi_ExY", global_chi1inv(s, gv, Ex, Y));
+}
+
+// 1-D: a slab whose faces fall between grid points; averaging of the
+// field parallel to the faces (harmonic mean of 1/eps)
+static double slab_eps1d(const vec &r) { return r.z() > -1.03 && r.z() < 0.77 ? 4.0 : 1.0; }
+
+static void case_aniso1d(Writer &w, int steps) {
+  grid_volume gv = volone(6.0, 20.0);
+  gv.center_origin();
+  structure s(gv, slab_eps1d, pml(1.0), identity(), 0, 0.5, true);
+  fields f(&s);
+  f.use_real_fields();
+  gaussian_src_time src(0.8, 0.5);
+  f.add_point_source(Ex, src, vec(-1.7));
+  for (int i = 0; i < steps; i++)
+    f.step();
+  w.scalar("t", f.time());
+  w.rec("Ex", global_field(f, gv, Ex));
+  w.rec("Hy", global_field(f, gv, Hy));
+  w.rec("chi_ExX", global_chi1inv(s, gv, Ex, X));
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -489,6 +748,16 @@ int main(int argc, char **argv) {
     case_py_tm2d(w);
   else if (cs == "py_disp3d")
     case_py_disp3d(w);
+  else if (cs == "aniso_te2d")
+    case_aniso_te2d(w, steps > 0 ? steps : 400);
+  else if (cs == "aniso3d")
+    case_aniso3d(w, steps > 0 ? steps : 200);
+  else if (cs == "offdiag_te2d")
+    case_offdiag_te2d(w, steps > 0 ? steps : 400);
+  else if (cs == "aniso_bloch2d")
+    case_aniso_bloch2d(w, steps > 0 ? steps : 300);
+  else if (cs == "aniso1d")
+    case_aniso1d(w, steps > 0 ? steps : 400);
   else {
     fprintf(stderr, "unknown case %s\n", cs.c_str());
     return 2;

@@ -7,9 +7,25 @@ set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 ROOT=$(cd "$HERE/../.." && pwd)
 make -C "$ROOT/oracle/ref" -j8 >/dev/null
-CASES=${CASES:-"known tm2d_small tm2d_small_dec1 vec3d_small disp3d_small tm2d_full"}
+CASES=${CASES:-"known tm2d_small tm2d_small_dec1 vec3d_small disp3d_small tm2d_full aniso1d aniso_te2d aniso3d offdiag_te2d aniso_bloch2d"}
 for c in $CASES; do
   for p in f64 f32; do
     OMP_NUM_THREADS=${OMP_NUM_THREADS:-8} "$ROOT/oracle/_ref/fp${p#f}/golden_driver" "$c" "$HERE/$c.$p.bin"
   done
 done
+# The sphere quadrature table of the reference's subpixel averaging, as the
+# reference's generator prints it (oracle/_ref/gen/sphere-quad.h): rows of
+# "dim index x y z weight".
+python3 - "$ROOT/oracle/_ref/gen/sphere-quad.h" "$HERE/sphere_quad.txt" <<'PY'
+import re, sys
+txt = open(sys.argv[1]).read()
+counts = [int(v) for v in re.search(r"num_sphere_quad\[3\]\s*=\s*\{([^}]*)\}", txt).group(1).split(",")]
+body = txt[txt.index("sphere_quad[3]"):]
+rows = re.findall(r"\{\s*([-\d.e+]+),\s*([-\d.e+]+),\s*([-\d.e+]+),\s*([-\d.e+]+)\s*\}", body)
+with open(sys.argv[2], "w") as f:
+    i = 0
+    for d, n in enumerate(counts):
+        for j in range(n):
+            f.write("%d %d %s\n" % (d + 1, j, " ".join(rows[i])))
+            i += 1
+PY
