@@ -382,6 +382,15 @@ public:
                                double tol = DEFAULT_SUBPIXEL_TOL,
                                int maxeval = DEFAULT_SUBPIXEL_MAXEVAL);
   virtual bool is_thread_safe() const { return false; }
+  // Extension of this engine, not in the reference: the rows of n pixels at
+  // once (lo, hi: n x 3 pixel corners in x, y, z order; rows: n x 3).  A
+  // material that evaluates them in bulk (on the GPU) returns true; the
+  // default returns false and the structure calls eff_chi1inv_row per pixel.
+  virtual bool eff_chi1inv_rows(component c, size_t n, const double *lo, const double *hi, double tol,
+                                int maxeval, double *rows) {
+    (void)c, (void)n, (void)lo, (void)hi, (void)tol, (void)maxeval, (void)rows;
+    return false;
+  }
   virtual void sigma_row(component c, double sigrow[3], const vec &r) {
     (void)c;
     (void)r;

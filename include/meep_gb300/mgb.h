@@ -47,10 +47,15 @@ typedef struct {
 
 /* grid and structure: vol1d/vol2d/vol3d(cell, resolution) centred on the
  * origin; pml: npml rows of (thickness, direction or -1 for all, side
- * (0 high, 1 low) or -1 for both, R_asymptotic, mean_stretch). */
+ * (0 high, 1 low) or -1 for both, R_asymptotic, mean_stretch).
+ * eps_averaging: subpixel averaging of the permittivity (isotropic media),
+ * computed on the GPU by the reference's default material-function method
+ * (sphere-quadrature normal, sampled means of eps and 1/eps; tolerance
+ * subpixel_tol, at most subpixel_maxeval evaluations per pixel). */
 int mgb_create(int dim, const double cell[3], double resolution, double courant, int npml, const double *pml,
                int nmed, const mgb_medium *media, int default_medium, int nobj, const mgb_object *objects,
-               int nsus, const mgb_susceptibility *sus, mgb_sim **out);
+               int nsus, const mgb_susceptibility *sus, int eps_averaging, double subpixel_tol,
+               int subpixel_maxeval, mgb_sim **out);
 void mgb_destroy(mgb_sim *s);
 const char *mgb_last_error(void);
 

@@ -156,6 +156,29 @@ int mfd_backward(mfd_sim *sim, int nmon, const int *mon_ids, const double *const
 int mfd_set_bloch(mfd_sim *s, const int periodic[3], const double k[3]);
 int mfd_get_field_im(mfd_sim *s, int c, double *out);
 
+/* Subpixel averaging of a geometry on the GPU.  The reference computes the
+ * averaged inverse-permittivity rows on the host, pixel by pixel
+ * (structure_chunk::set_chi1inv -> material_function::eff_chi1inv_row,
+ * src/anisotropic_averaging.cpp:87-324); this evaluates the same rows for
+ * npix pixels at once, one GPU thread per pixel, for a geometry of blocks,
+ * spheres and cylinders with scalar permittivities (the last object
+ * containing a point wins; eps_default elsewhere).  lo, hi: npix x 3 pixel
+ * corners (x, y, z; dim 1 uses z only, dim 2 x and y); rows: npix x 3 output,
+ * the row of the component along cdir (0, 1, 2).  tol, maxeval as in
+ * structure(); maxeval == 0 gives the unaveraged 1 / eps at the pixel centre.
+ * Host pointers; no mfd_sim needed. */
+typedef struct {
+  int kind; /* 0 block (axis-aligned), 1 sphere, 2 cylinder */
+  double center[3];
+  double size[3];  /* block edge lengths */
+  double radius;   /* sphere, cylinder */
+  double height;   /* cylinder */
+  double axis[3];  /* cylinder axis (unit vector) */
+  double eps;      /* chi1p1 inside the object */
+} mfd_object;
+int mfd_subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const double *hi, double tol, int maxeval,
+                      int nobj, const mfd_object *objs, double eps_default, double *rows);
+
 /* Allocation-free flux reduction.  No counterpart in the reference: it is the
  * reduction of mfd_flux (sum_k Re(E conj H) per frequency) for callers that
  * must not allocate device memory when they call it -- code recording a CUDA

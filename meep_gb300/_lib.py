@@ -41,6 +41,18 @@ class mfd_grid(C.Structure):
     ]
 
 
+class mfd_object(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("center", C.c_double * 3),
+        ("size", C.c_double * 3),
+        ("radius", C.c_double),
+        ("height", C.c_double),
+        ("axis", C.c_double * 3),
+        ("eps", C.c_double),
+    ]
+
+
 # (name, restype, argtypes) of every entry point in include/mfd.h
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
@@ -70,6 +82,8 @@ SIGNATURES = [
     ("mfd_backward", C.c_int, [_P, C.c_int, _IP, C.POINTER(_DP), _DP]),
     ("mfd_set_bloch", C.c_int, [_P, C.POINTER(C.c_int), _DP]),
     ("mfd_get_field_im", C.c_int, [_P, C.c_int, _DP]),
+    ("mfd_subpixel_rows", C.c_int, [C.c_int, C.c_int, C.c_int64, _DP, _DP, C.c_double, C.c_int, C.c_int,
+                                    C.POINTER(mfd_object), C.c_double, _DP]),
     ("mfd_flux_noalloc", C.c_int, [_P, _P, C.c_int64, C.c_int, _P, _P]),
     ("mfd_noalloc_last_error", C.c_char_p, []),
     ("mfd_kernel_launches", C.c_int64, [_P]),
@@ -107,6 +121,26 @@ class Engine:
     def check(self, status):
         if status != 0:
             raise MeepError(self.lib.mfd_last_error().decode())
+
+    def subpixel_rows(self, dim, cdir, lo, hi, objects, eps_default=1.0, tol=1e-4, maxeval=100000):
+        """Averaged inverse-permittivity rows (mfd_subpixel_rows) of the pixels
+        [lo[i], hi[i]] (arrays n x 3); objects: list of dicts with kind (0
+        block, 1 sphere, 2 cylinder), center, size, radius, height, axis, eps."""
+        lo = np.ascontiguousarray(lo, dtype=np.float64).reshape(-1, 3)
+        hi = np.ascontiguousarray(hi, dtype=np.float64).reshape(-1, 3)
+        objs = (mfd_object * max(1, len(objects)))()
+        for q, o in enumerate(objects):
+            objs[q].kind = int(o["kind"])
+            objs[q].center[:] = list(o.get("center", (0, 0, 0)))
+            objs[q].size[:] = list(o.get("size", (0, 0, 0)))
+            objs[q].radius = float(o.get("radius", 0.0))
+            objs[q].height = float(o.get("height", 0.0))
+            objs[q].axis[:] = list(o.get("axis", (0, 0, 1)))
+            objs[q].eps = float(o["eps"])
+        rows = np.zeros((lo.shape[0], 3))
+        self.check(self.lib.mfd_subpixel_rows(dim, cdir, lo.shape[0], _dptr(lo), _dptr(hi), tol, maxeval,
+                                              len(objects), objs, eps_default, _dptr(rows)))
+        return rows
 
 
 def _dptr(a):

@@ -72,7 +72,9 @@ def build_engine(force=False, verbose=False):
                              "-o", os.path.join(objdir, "mfd_cuda_f32.o")])
     jobs.append(cu_common + ["-c", os.path.join(CSRC, "mfd_noalloc.cu"),
                              "-o", os.path.join(objdir, "mfd_noalloc.o")])
-    for src in ("mfd_plan.cpp", "mfd_capi.cpp"):
+    jobs.append(cu_common + ["--fmad=false", "-c", os.path.join(CSRC, "mfd_subpixel.cu"),
+                             "-o", os.path.join(objdir, "mfd_subpixel.o")])
+    for src in ("mfd_plan.cpp", "mfd_capi.cpp", "sphere_quadrature.cpp"):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"] + INC +
                     ["-c", os.path.join(CSRC, src), "-o", os.path.join(objdir, src.replace(".cpp", ".o"))])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
@@ -81,10 +83,10 @@ def build_engine(force=False, verbose=False):
         for o in outs:
             sys.stdout.write(o)
     objs = [os.path.join(objdir, f) for f in ("mfd_cuda_f64.o", "mfd_cuda_f32.o", "mfd_noalloc.o",
-                                               "mfd_plan.o", "mfd_capi.o")]
+                                               "mfd_subpixel.o", "mfd_plan.o", "mfd_capi.o",
+                                               "sphere_quadrature.o")]
     _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
-    api = [os.path.join(CSRC, "meep_api.cpp"), os.path.join(CSRC, "meep_pyshim.cpp"),
-           os.path.join(CSRC, "sphere_quadrature.cpp")]
+    api = [os.path.join(CSRC, "meep_api.cpp"), os.path.join(CSRC, "meep_pyshim.cpp")]
     links = []
     for name, flag in (("libmeep_gb300.so", []), ("libmeep_gb300_single.so", ["-DMEEP_SINGLE=1"])):
         links.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"] + flag + INC +

@@ -238,6 +238,12 @@ struct Dense {
   }
   size_t count() const { return (size_t)ext[0] * ext[1] * ext[2]; }
   int64_t index(const int k[3]) const { return ((int64_t)k[0] * ext[1] + k[1]) * ext[2] + k[2]; }
+  void coords(int64_t di, int k[3]) const {
+    k[2] = int(di % ext[2]);
+    di /= ext[2];
+    k[1] = int(di % ext[1]);
+    k[0] = int(di / ext[1]);
+  }
   // k of an ivec location for component c (no range check)
   void kof(const grid_volume &gv, component c, const ivec &p, int k[3]) const {
     ivec sh = gv.iyee_shift(c);
@@ -355,6 +361,33 @@ void structure::set_epsilon(material_function &mat, bool use_aa, double tol, int
       arr[q].assign(dn.count(), 0.0);
     ivec shift1(gv.dim, 0);
     shift1.set_direction(direction(dc), 1);
+    // bulk evaluation first (two pixels per point, in batches), else pixel
+    // by pixel through eff_chi1inv_row
+    bool bulk = true;
+    {
+      const size_t npts = dn.count(), B = size_t(1) << 18;
+      std::vector<double> lo, hi, rows;
+      for (size_t p0 = 0; p0 < npts && bulk; p0 += B) {
+        const size_t nb = std::min(B, npts - p0);
+        lo.resize(6 * nb);
+        hi.resize(6 * nb);
+        rows.resize(6 * nb);
+        for (size_t j = 0; j < nb; j++) {
+          int k[3];
+          dn.coords((int64_t)(p0 + j), k);
+          const ivec here = dn.iloc(gv, c, k);
+          volume_box(dV(gv, here), &lo[6 * j], &hi[6 * j]);
+          volume_box(dV(gv, here - shift1), &lo[6 * j + 3], &hi[6 * j + 3]);
+        }
+        if (!mat.eff_chi1inv_rows(c, 2 * nb, lo.data(), hi.data(), tol, maxeval, rows.data())) {
+          bulk = false;
+          break;
+        }
+        for (size_t j = 0; j < nb; j++)
+          for (int q = 0; q < 3; q++)
+            arr[q][p0 + j] = (q == dc) ? rows[6 * j + q] : rows[6 * j + 3 + q];
+      }
+    }
     auto body = [&](const int k[3], int64_t di) {
       ivec here = dn.iloc(gv, c, k);
       double row[3], row_off[3];
@@ -363,8 +396,10 @@ void structure::set_epsilon(material_function &mat, bool use_aa, double tol, int
       for (int q = 0; q < 3; q++)
         arr[q][di] = (q == dc) ? row[q] : row_off[q];
     };
-    if (mat.is_thread_safe()) dn.for_each_parallel(body);
-    else dn.for_each(body);
+    if (!bulk) {
+      if (mat.is_thread_safe()) dn.for_each_parallel(body);
+      else dn.for_each(body);
+    }
     for (int q = 0; q < 3; q++)
       for (double v : arr[q])
         if (v != (q == dc ? 1.0 : 0.0)) {

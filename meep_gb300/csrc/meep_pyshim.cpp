@@ -20,7 +20,9 @@
 #include <vector>
 
 #include "meep.hpp"
+#include "mfd.h"
 #include "mgb.h"
+#include "geom_eval.hpp"
 
 using namespace meep;
 
@@ -40,23 +42,8 @@ struct Geometry {
     return d == 0 ? r.x() : (d == 1 ? r.y() : r.z());
   }
   bool inside(const mgb_object &o, const vec &r) const {
-    double p[3];
-    for (int d = 0; d < 3; d++)
-      p[d] = coord(r, d, dim) - o.center[d];
-    if (o.kind == 0) {
-      for (int d = 0; d < 3; d++)
-        if (std::fabs(p[d]) > 0.5 * o.size[d]) return false;
-      return true;
-    }
-    if (o.kind == 1) return p[0] * p[0] + p[1] * p[1] + p[2] * p[2] <= o.radius * o.radius;
-    const double h = p[0] * o.axis[0] + p[1] * o.axis[1] + p[2] * o.axis[2];
-    if (std::fabs(h) > 0.5 * o.height) return false;
-    double q2 = 0;
-    for (int d = 0; d < 3; d++) {
-      const double q = p[d] - h * o.axis[d];
-      q2 += q * q;
-    }
-    return q2 <= o.radius * o.radius;
+    const double p[3] = {coord(r, 0, dim), coord(r, 1, dim), coord(r, 2, dim)};
+    return mgb_geom::contains(o, p);
   }
   const mgb_medium &at(const vec &r) const {
     for (size_t q = objs.size(); q-- > 0;)
@@ -68,11 +55,36 @@ struct Geometry {
 class GeomMaterial : public material_function {
 public:
   const Geometry *g;
-  explicit GeomMaterial(const Geometry *geo) : g(geo) {}
+  std::vector<mfd_object> dev; // the objects with their scalar permittivity
+  explicit GeomMaterial(const Geometry *geo) : g(geo) {
+    for (const mgb_object &o : g->objs) {
+      mfd_object m{};
+      m.kind = o.kind;
+      for (int d = 0; d < 3; d++) {
+        m.center[d] = o.center[d];
+        m.size[d] = o.size[d];
+        m.axis[d] = o.axis[d];
+      }
+      m.radius = o.radius;
+      m.height = o.height;
+      m.eps = g->media[o.material].eps[0];
+      dev.push_back(m);
+    }
+  }
+  bool isotropic() const {
+    for (const mgb_medium &m : g->media)
+      if (m.eps[1] != m.eps[0] || m.eps[2] != m.eps[0]) return false;
+    return true;
+  }
   double chi1p1(field_type ft, const vec &r) override { return ft == H_stuff ? 1.0 : g->at(r).eps[0]; }
+  // without averaging: 1 / epsilon_diag at the pixel centre; with averaging
+  // (isotropic media): the default material_function averaging
   void eff_chi1inv_row(component c, double row[3], const volume &v, double tol, int maxeval) override {
-    (void)tol;
-    (void)maxeval;
+    if (maxeval && type(c) == E_stuff) {
+      if (!isotropic()) meep::abort("subpixel averaging of anisotropic media is not supported by the GB300 engine");
+      material_function::eff_chi1inv_row(c, row, v, tol, maxeval);
+      return;
+    }
     row[0] = row[1] = row[2] = 0.0;
     const int d = component_direction(c) % 3;
     if (type(c) == H_stuff) {
@@ -80,6 +92,16 @@ public:
       return;
     }
     row[d] = 1.0 / g->at(v.center()).eps[d];
+  }
+  // averaged rows of many pixels at once on the GPU (mfd_subpixel_rows)
+  bool eff_chi1inv_rows(component c, size_t n, const double *lo, const double *hi, double tol, int maxeval,
+                        double *rows) override {
+    if (!maxeval || type(c) != E_stuff) return false;
+    if (!isotropic()) meep::abort("subpixel averaging of anisotropic media is not supported by the GB300 engine");
+    if (mfd_subpixel_rows(g->dim, component_direction(c) % 3, (int64_t)n, lo, hi, tol, maxeval, (int)dev.size(),
+                          dev.data(), g->media[g->def].eps[0], rows) != 0)
+      throw std::runtime_error(mfd_last_error());
+    return true;
   }
   bool is_thread_safe() const override { return true; }
   bool has_conductivity(component c) override {
@@ -150,7 +172,8 @@ const char *mgb_last_error(void) { return g_err.c_str(); }
 
 int mgb_create(int dim, const double cell[3], double resolution, double courant, int npml, const double *pmlspec,
                int nmed, const mgb_medium *media, int default_medium, int nobj, const mgb_object *objects,
-               int nsus, const mgb_susceptibility *sus, mgb_sim **out) {
+               int nsus, const mgb_susceptibility *sus, int eps_averaging, double subpixel_tol,
+               int subpixel_maxeval, mgb_sim **out) {
   try {
     if (!out || !cell || (nmed > 0 && !media)) throw std::runtime_error("null argument");
     if (dim < 1 || dim > 3) throw std::runtime_error("dimensions must be 1, 2 or 3");
@@ -180,7 +203,8 @@ int mgb_create(int dim, const double cell[3], double resolution, double courant,
       }
     }
     S->mat.reset(new GeomMaterial(&S->geo));
-    S->s.reset(new structure(S->gv, *S->mat, br, identity(), 0, courant, false));
+    S->s.reset(new structure(S->gv, *S->mat, br, identity(), 0, courant, eps_averaging != 0, subpixel_tol,
+                             subpixel_maxeval));
     for (int q = 0; q < nsus; q++) {
       S->sigmas.emplace_back(new SusSigma(&S->geo, q));
       // Drude: the Lorentzian without the omega_0^2 term (src/meepgeom.cpp)

@@ -67,5 +67,8 @@ public:
 
 // Defined by whichever backend is linked in.
 Backend *make_backend(const Plan &p);
+// mfd_subpixel_rows (arguments checked by the C ABI)
+void subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const double *hi, double tol, int maxeval,
+                   int nobj, const mfd_object *objs, double eps_default, double *rows);
 
 } // namespace mfd

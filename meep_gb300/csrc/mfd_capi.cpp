@@ -372,6 +372,22 @@ int mfd_get_field_im(mfd_sim *s, int c, double *out) {
   MFD_CATCH
 }
 
+int mfd_subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const double *hi, double tol, int maxeval,
+                      int nobj, const mfd_object *objs, double eps_default, double *rows) {
+  MFD_TRY
+  need(dim >= 1 && dim <= 3, "dim must be 1, 2 or 3");
+  need(cdir >= 0 && cdir < 3, "cdir must be 0, 1 or 2");
+  need(npix >= 0, "negative pixel count");
+  need(nobj >= 0 && (nobj == 0 || objs), "null object list");
+  need(npix == 0 || (lo && hi && rows), "null pixel or row array");
+  need(maxeval >= 0, "negative maxeval");
+  for (int q = 0; q < nobj; q++)
+    need(objs[q].kind >= 0 && objs[q].kind <= 2, "unknown object kind");
+  if (npix > 0) subpixel_rows(dim, cdir, npix, lo, hi, tol, maxeval, nobj, objs, eps_default, rows);
+  return 0;
+  MFD_CATCH
+}
+
 int mfd_set_bloch(mfd_sim *s, const int periodic[3], const double k[3]) {
   MFD_TRY
   need(s && s->plan && periodic && k, "null argument");

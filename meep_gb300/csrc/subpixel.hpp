@@ -51,7 +51,7 @@ const SphereQuad &sphere_quadrature();
 template <class Chi>
 MGB_HD void normal_vector(int dim, const double lo[3], const double hi[3], const SphereQuad &sq, Chi chi,
                           double grad[3]) {
-  const bool act[3] = {dim >= 2, dim >= 2, true};
+  const bool act[3] = {dim >= 2, dim >= 2, dim != 2};
   double cen[3] = {0, 0, 0};
   double R = 0.0;
   for (int d = 0; d < 3; d++) {
@@ -90,7 +90,7 @@ MGB_HD void normal_vector(int dim, const double lo[3], const double hi[3], const
 template <class Chi>
 MGB_HD void eff_chi1inv_row(int dim, int cdir, const double lo[3], const double hi[3], double tol, int maxeval,
                             const SphereQuad &sq, Chi chi, double row[3]) {
-  const bool act[3] = {dim >= 2, dim >= 2, true};
+  const bool act[3] = {dim >= 2, dim >= 2, dim != 2};
   double cen[3] = {0, 0, 0}, ext[3] = {0, 0, 0};
   for (int d = 0; d < 3; d++)
     if (act[d]) {

@@ -10,11 +10,15 @@ volumes, DFT flux regions and DFT field monitors, `run(until=...)` and
 C++ drop-in (include/meep_gb300/meep.hpp) through its C interface
 (include/meep_gb300/mgb.h), which runs the CUDA engine.
 
-Differences from the reference, raised as errors where they would change
-results: no subpixel averaging (`eps_averaging` must be False), no
-symmetries, no material functions (per-point Python callables).  `k_point`
-gives Bloch-periodic walls (complex fields when it is nonzero), as in the
-reference.
+Subpixel averaging (`eps_averaging=True`, the default) runs on the GPU with
+the reference's default material-function method (sphere-quadrature normal,
+sampled means of eps and 1/eps, `subpixel_tol`, `subpixel_maxeval`): the
+reference's Python layer averages through libctl's analytic overlaps instead,
+so interface pixels differ from it at the level of the averaging tolerance.
+Averaging needs isotropic media.  Differences from the reference, raised as
+errors where they would change results: no symmetries, no material functions
+(per-point Python callables).  `k_point` gives Bloch-periodic walls (complex
+fields when it is nonzero), as in the reference.
 
     import meep_gb300 as mp
     sim = mp.Simulation(cell_size=mp.Vector3(16, 8), resolution=10,
@@ -356,7 +360,8 @@ _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
 _SIGS = [
     ("mgb_create", C.c_int, [C.c_int, _DP, C.c_double, C.c_double, C.c_int, _DP, C.c_int, C.POINTER(_Med), C.c_int,
-                             C.c_int, C.POINTER(_Obj), C.c_int, C.POINTER(_Sus), C.POINTER(_P)]),
+                             C.c_int, C.POINTER(_Obj), C.c_int, C.POINTER(_Sus), C.c_int, C.c_double, C.c_int,
+                             C.POINTER(_P)]),
     ("mgb_destroy", None, [_P]),
     ("mgb_last_error", C.c_char_p, []),
     ("mgb_add_source", C.c_int, [_P, C.c_int, C.c_int, _DP, C.c_int, _DP, _DP, C.c_double, C.c_double]),
@@ -421,8 +426,7 @@ def _fix_dft_args(args, i):
 
 _IGNORED_KWARGS = {"progress_interval", "split_chunks_evenly", "num_chunks", "chunk_layout", "filename_prefix",
                    "output_volume", "output_single_precision", "collect_stats", "ensure_periodicity",
-                   "accurate_fields_near_cylorigin", "subpixel_tol", "subpixel_maxeval", "loop_tile_base_db",
-                   "loop_tile_base_eh"}
+                   "accurate_fields_near_cylorigin", "loop_tile_base_db", "loop_tile_base_eh"}
 
 
 class Simulation:
@@ -431,15 +435,20 @@ class Simulation:
 
     def __init__(self, cell_size, resolution, geometry=None, sources=None, eps_averaging=True, dimensions=3,
                  boundary_layers=None, symmetries=None, force_complex_fields=False, default_material=Medium(),
-                 k_point=False, Courant=0.5, geometry_center=Vector3(), _library=None, **kwargs):
+                 k_point=False, Courant=0.5, geometry_center=Vector3(), subpixel_tol=1e-4,
+                 subpixel_maxeval=100000, _library=None, **kwargs):
         bad = set(kwargs) - _IGNORED_KWARGS
         if bad:
             raise TypeError("Simulation got unexpected keyword arguments %s" % sorted(bad))
-        if eps_averaging and geometry:
-            # without geometric objects the medium is uniform and averaging
-            # changes nothing
-            raise NotImplementedError("meep: subpixel averaging (eps_averaging=True, the reference's default) is "
-                                      "not supported by the GB300 engine; pass eps_averaging=False")
+        self.eps_averaging = bool(eps_averaging)
+        self.subpixel_tol = float(subpixel_tol)
+        self.subpixel_maxeval = int(subpixel_maxeval)
+        if self.eps_averaging:
+            for g in geometry or []:
+                m = getattr(g, "material", None)
+                if isinstance(m, Medium) and len(set(m.epsilon_diag)) > 1:
+                    raise NotImplementedError("meep: subpixel averaging of anisotropic media is not supported by "
+                                              "the GB300 engine; pass eps_averaging=False")
         if symmetries:
             raise NotImplementedError("meep: symmetries are not supported by the GB300 engine")
         if force_complex_fields:
@@ -514,6 +523,7 @@ class Simulation:
         h = _P()
         self._check(self._lib.mgb_create(self.dimensions, cell_p, self.resolution, self.Courant, len(rows), pml_p,
                                          len(media), med, 0, len(self.geometry), objs, len(sus_keys), sus,
+                                         int(self.eps_averaging), self.subpixel_tol, self.subpixel_maxeval,
                                          C.byref(h)))
         self._h = h
         if self.k_point is not False:

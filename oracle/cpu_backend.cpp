@@ -17,6 +17,8 @@
 //   flux                dft_flux::flux            src/dft.cpp:542-556
 // The per-chunk choice of formula is made per point from its chunk region
 // (Plan::region), see meep_gb300/csrc/mfd_plan.hpp.
+#include "geom_eval.hpp"
+#include "subpixel.hpp"
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -647,6 +649,20 @@ public:
 Backend *make_backend(const Plan &p) {
   if (p.g.precision == 64) return new CpuBackend<double>(p);
   return new CpuBackend<float>(p);
+}
+
+// mfd_subpixel_rows on the host: the shared averaging routine over the same
+// object list, pixel by pixel (the reference's order of work)
+void subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const double *hi, double tol, int maxeval,
+                   int nobj, const mfd_object *objs, double eps_default, double *rows) {
+  const mgb_subpixel::SphereQuad &sq = mgb_subpixel::sphere_quadrature();
+  auto chi = [objs, nobj, eps_default](const double p[3]) {
+    const int q = mgb_geom::object_at(objs, nobj, p);
+    return q < 0 ? eps_default : objs[q].eps;
+  };
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < npix; i++)
+    mgb_subpixel::eff_chi1inv_row(dim, cdir, lo + 3 * i, hi + 3 * i, tol, maxeval, sq, chi, rows + 3 * i);
 }
 
 } // namespace mfd

@@ -719,6 +719,161 @@ static void case_aniso1d(Writer &w, int steps) {
   w.rec("chi_ExX", global_chi1inv(s, gv, Ex, X));
 }
 
+/* Scripts with the Python front end's default eps_averaging=True.  The
+   package averages its geometry with the reference's default
+   material_function method (not libctl's analytic overlaps, which the
+   reference's Python layer uses), so these restate the scripts as a C++
+   structure built with use_anisotropic_averaging = true over a material
+   function of the same objects: blocks, spheres and cylinders with any axis,
+   the last containing object winning. */
+struct PyAvgObj {
+  int kind; // 0 block, 1 sphere, 2 cylinder
+  double center[3], size[3], radius, height, axis[3];
+  double eps, cond, sig;
+};
+class PyGeomAvg : public material_function {
+public:
+  int dim = 2;
+  std::vector<PyAvgObj> objs;
+  double eps_default = 1.0;
+  static bool contains(const PyAvgObj &o, const double r[3]) {
+    double p[3];
+    for (int d = 0; d < 3; d++)
+      p[d] = r[d] - o.center[d];
+    if (o.kind == 0) {
+      for (int d = 0; d < 3; d++)
+        if (std::fabs(p[d]) > 0.5 * o.size[d]) return false;
+      return true;
+    }
+    if (o.kind == 1) return p[0] * p[0] + p[1] * p[1] + p[2] * p[2] <= o.radius * o.radius;
+    const double h = p[0] * o.axis[0] + p[1] * o.axis[1] + p[2] * o.axis[2];
+    if (std::fabs(h) > 0.5 * o.height) return false;
+    double q2 = 0;
+    for (int d = 0; d < 3; d++) {
+      const double q = p[d] - h * o.axis[d];
+      q2 += q * q;
+    }
+    return q2 <= o.radius * o.radius;
+  }
+  const PyAvgObj *at(const vec &r) const {
+    const double p[3] = {dim == 1 ? 0.0 : r.x(), dim == 1 ? 0.0 : r.y(), dim == 2 ? 0.0 : r.z()};
+    for (size_t q = objs.size(); q-- > 0;)
+      if (contains(objs[q], p)) return &objs[q];
+    return nullptr;
+  }
+  virtual double chi1p1(field_type ft, const vec &r) {
+    if (ft == H_stuff) return 1.0;
+    const PyAvgObj *o = at(r);
+    return o ? o->eps : eps_default;
+  }
+  virtual bool has_conductivity(component c) {
+    if (!is_D(c)) return false;
+    for (const PyAvgObj &o : objs)
+      if (o.cond != 0) return true;
+    return false;
+  }
+  virtual double conductivity(component c, const vec &r) {
+    const PyAvgObj *o = at(r);
+    return is_D(c) && o ? o->cond : 0.0;
+  }
+};
+class PyAvgSigma : public material_function {
+public:
+  const PyGeomAvg *g;
+  explicit PyAvgSigma(const PyGeomAvg *geo) : g(geo) {}
+  virtual void sigma_row(component c, double row[3], const vec &r) {
+    row[0] = row[1] = row[2] = 0.0;
+    const PyAvgObj *o = g->at(r);
+    row[component_direction(c) % 3] = o ? o->sig : 0.0;
+  }
+};
+
+/* Script:
+     geometry = [mp.Block(mp.Vector3(mp.inf, 1, mp.inf), center=mp.Vector3(y=0.17),
+                          material=mp.Medium(epsilon=12)),
+                 mp.Cylinder(0.8, center=mp.Vector3(3, 1.5), material=mp.Medium(index=2)),
+                 mp.Sphere(0.6, center=mp.Vector3(-2, -1.7),
+                           material=mp.Medium(epsilon=6, D_conductivity=0.05))]
+     sim = mp.Simulation(cell_size=mp.Vector3(16, 8), resolution=10, geometry=geometry,
+                         boundary_layers=[mp.PML(1.0)],
+                         sources=[mp.Source(mp.GaussianSource(0.15, fwidth=0.1), component=mp.Ey,
+                                            center=mp.Vector3(-6), size=mp.Vector3(y=1))])
+     tran = sim.add_flux([0.1, 0.15, 0.2], mp.FluxRegion(center=mp.Vector3(6), size=mp.Vector3(y=2)))
+     sim.run(until_after_sources=20) */
+static void case_py_aniso_te2d(Writer &w) {
+  const double inf = 1.0e20;
+  grid_volume gv = vol2d(16, 8, 10);
+  gv.center_origin();
+  PyGeomAvg g;
+  g.dim = 2;
+  g.objs = {{0, {0, 0.17, 0}, {inf, 1, inf}, 0, 0, {0, 0, 0}, 12, 0, 0},
+            {2, {3, 1.5, 0}, {0, 0, 0}, 0.8, inf, {0, 0, 1}, 4, 0, 0},
+            {1, {-2, -1.7, 0}, {0, 0, 0}, 0.6, 0, {0, 0, 0}, 6, 0.05, 0}};
+  structure s(gv, g, pml(1.0), identity(), 0, 0.5, true, 1e-4, 100000);
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.1);
+  gaussian_src_time src(0.15, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ey, src, volume(vec(-6, -0.5), vec(-6, 0.5)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = {0.1, 0.15, 0.2};
+  volume_list r(volume(vec(6, -1), vec(6, 1)), Sx, 1.0);
+  dft_flux tran = f.add_dft_flux(&r, fr.data(), fr.size(), true, true, 0);
+  py_run_until_after_sources(f, 20);
+  sync_dfts(f);
+  double *F = tran.flux();
+  w.rec("flux", std::vector<double>(F, F + fr.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ex", global_field(f, gv, Ex));
+  w.rec("Ey", global_field(f, gv, Ey));
+  w.rec("Hz", global_field(f, gv, Hz));
+  w.rec("chi_ExY", global_chi1inv(s, gv, Ex, Y));
+}
+
+/* Script:
+     mat = mp.Medium(epsilon=2.5, E_susceptibilities=[
+         mp.LorentzianSusceptibility(frequency=1.1, gamma=0.1, sigma=0.5)])
+     geometry = [mp.Block(mp.Vector3(1.1, 0.9, 0.73), center=mp.Vector3(0.05, -0.1, 0.02), material=mat),
+                 mp.Cylinder(0.35, height=1.0, axis=mp.Vector3(0.6, 0, 0.8),
+                             center=mp.Vector3(0.2, 0.3, -0.1), material=mp.Medium(epsilon=5))]
+     sim = mp.Simulation(cell_size=mp.Vector3(2, 2, 2), resolution=10, geometry=geometry,
+                         boundary_layers=[mp.PML(0.5)],
+                         sources=[mp.Source(mp.GaussianSource(0.8, fwidth=0.5, is_integrated=True),
+                                            component=mp.Ex, center=mp.Vector3(-0.4, 0.1))])
+     flux = sim.add_flux(0.8, 0.4, 3, mp.FluxRegion(center=mp.Vector3(z=0.45), size=mp.Vector3(1, 1)))
+     sim.run(until=6) */
+static void case_py_aniso3d(Writer &w) {
+  grid_volume gv = vol3d(2, 2, 2, 10);
+  gv.center_origin();
+  PyGeomAvg g;
+  g.dim = 3;
+  g.objs = {{0, {0.05, -0.1, 0.02}, {1.1, 0.9, 0.73}, 0, 0, {0, 0, 0}, 2.5, 0, 0.5},
+            {2, {0.2, 0.3, -0.1}, {0, 0, 0}, 0.35, 1.0, {0.6, 0, 0.8}, 5, 0, 0}};
+  structure s(gv, g, pml(0.5), identity(), 0, 0.5, true, 1e-4, 100000);
+  PyAvgSigma sg(&g);
+  s.add_susceptibility(sg, E_stuff, lorentzian_susceptibility(1.1, 0.1));
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.5);
+  gaussian_src_time src(0.8, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = true;
+  f.add_volume_source(Ex, src, volume(vec(-0.4, 0.1, 0), vec(-0.4, 0.1, 0)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = np_linspace(0.8 - 0.5 * 0.4, 0.8 + 0.5 * 0.4, 3);
+  volume_list r(volume(vec(-0.5, -0.5, 0.45), vec(0.5, 0.5, 0.45)), Sz, 1.0);
+  dft_flux flux = f.add_dft_flux(&r, fr.data(), fr.size(), true, true, 0);
+  py_run_until(f, 6);
+  double *F = flux.flux();
+  w.rec("flux", std::vector<double>(F, F + fr.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ex", global_field(f, gv, Ex));
+  w.rec("Ez", global_field(f, gv, Ez));
+  w.rec("Hy", global_field(f, gv, Hy));
+  w.rec("chi_ExZ", global_chi1inv(s, gv, Ex, Z));
+  w.rec("chi_EzY", global_chi1inv(s, gv, Ez, Y));
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -756,6 +911,10 @@ int main(int argc, char **argv) {
     case_offdiag_te2d(w, steps > 0 ? steps : 400);
   else if (cs == "aniso_bloch2d")
     case_aniso_bloch2d(w, steps > 0 ? steps : 300);
+  else if (cs == "py_aniso_te2d")
+    case_py_aniso_te2d(w);
+  else if (cs == "py_aniso3d")
+    case_py_aniso3d(w);
   else if (cs == "aniso1d")
     case_aniso1d(w, steps > 0 ? steps : 400);
   else {

@@ -93,3 +93,64 @@ def test_gpu_fp32_close_to_reference_fp64(case, gpu_drivers, tmp_path):
     for k, err in out.items():
         floor = 1e-5 if k == "flux" else 1e-6
         assert err <= max(3 * ref32[k], floor), (case, k, err, ref32[k])
+
+
+def _random_geometry(rng, n):
+    objs = []
+    for _ in range(n):
+        kind = int(rng.integers(0, 3))
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        objs.append({"kind": kind, "center": rng.uniform(-1, 1, 3), "size": rng.uniform(0.2, 1.2, 3),
+                     "radius": rng.uniform(0.1, 0.6), "height": rng.uniform(0.3, 2.0), "axis": ax,
+                     "eps": rng.uniform(1.5, 12.0)})
+    return objs
+
+
+def _pixels(rng, dim, n, res=10.0):
+    k = rng.integers(-15, 16, size=(n, 3)) * 2 + rng.integers(0, 2, size=(n, 3))
+    cen = k * (0.5 / res)
+    if dim == 2:
+        cen[:, 2] = 0
+    if dim == 1:
+        cen[:, :2] = 0
+    lo, hi = cen - 0.5 / res, cen + 0.5 / res
+    if dim == 2:
+        lo[:, 2] = hi[:, 2] = 0
+    if dim == 1:
+        lo[:, :2] = hi[:, :2] = 0
+    return lo, hi
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_device_rows_match_host(dim, engine_lib, oracle_lib):
+    """mfd_subpixel_rows on the GPU equals the same routine on the host bit for
+    bit, over random objects and pixels (many of them on interfaces)."""
+    from meep_gb300 import _lib
+    rng = np.random.default_rng(7 + dim)
+    objs = _random_geometry(rng, 12)
+    lo, hi = _pixels(rng, dim, 20000)
+    for cdir in range(3):
+        gpu = _lib.Engine(engine_lib).subpixel_rows(dim, cdir, lo, hi, objs, eps_default=1.3)
+        cpu = _lib.Engine(oracle_lib).subpixel_rows(dim, cdir, lo, hi, objs, eps_default=1.3)
+        if dim > 1 and cdir < 2:
+            assert np.count_nonzero(cpu[:, 1 - cdir]) > 100  # interface pixels with off-diagonal entries
+        assert np.array_equal(gpu, cpu), (dim, cdir, int(np.count_nonzero(gpu != cpu)))
+
+
+def test_host_rows_cases(oracle_lib):
+    """CPU: uniform pixels give 1/eps on the diagonal; an interface pixel of a
+    plane x = 0 gives the harmonic/arithmetic means along/against the normal."""
+    from meep_gb300 import _lib
+    eng = _lib.Engine(oracle_lib)
+    objs = [{"kind": 0, "center": (-5, 0, 0), "size": (10, 100, 100), "eps": 4.0}]
+    lo = np.array([[1.0, 1.0, 1.0], [-0.05, -0.05, -0.05]])
+    hi = lo + 0.1
+    rx = eng.subpixel_rows(3, 0, lo, hi, objs)
+    ry = eng.subpixel_rows(3, 1, lo, hi, objs)
+    assert rx[0].tolist() == [1.0, 0.0, 0.0] and ry[0].tolist() == [0.0, 1.0, 0.0]
+    # half-filled pixel: E normal to the interface sees <1/eps>, E along it 1/<eps>
+    assert abs(rx[1, 0] - 0.5 * (1 + 0.25)) < 0.02
+    assert abs(ry[1, 1] - 1 / 2.5) < 0.02
+    assert abs(rx[1, 1]) < 1e-12 and abs(ry[1, 0]) < 1e-12
