@@ -623,8 +623,13 @@ public:
     cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
     cuda_check(cudaEventCreate(&ev0), "event");
     cuda_check(cudaEventCreate(&ev1), "event");
+    // the side streams carry the PML shell of each half-step: higher priority,
+    // so their (latency-bound) blocks are dispatched ahead of the pending
+    // core blocks and finish under them instead of trailing after them
+    int prio_lo = 0, prio_hi = 0;
+    cuda_check(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi), "stream priorities");
     for (int q = 0; q < NSIDE; q++) {
-      cuda_check(cudaStreamCreateWithFlags(&side[q], cudaStreamNonBlocking), "stream");
+      cuda_check(cudaStreamCreateWithPriority(&side[q], cudaStreamNonBlocking, prio_hi), "stream");
       cuda_check(cudaEventCreateWithFlags(&side_ev[q], cudaEventDisableTiming), "event");
     }
     cuda_check(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming), "event");
@@ -987,7 +992,13 @@ public:
   // splits the rows into the core (quads) and the z ends of the rows.
   // slabs split by how many directions can hold slab points: faces (one) run
   // the lean single-flag code, edges and corners the general code
-  Band band_rows{}, band_zend{}, band_xface{}, band_yface{}, band_xyedge{}, band_xzedge{}, band_yzedge{};
+  Band band_rows{}, band_zend{}, band_xface{}, band_yface{}, band_xyedge{};
+  // FP64 (issue-bound) shell: faces over the z interior only (no z flags) and
+  // the z edges of the faces
+  Band band_xface_zi{}, band_yface_zi{}, band_xzedge{}, band_yzedge{};
+  // the rows without their z slabs and walls (z range of the quad core): no
+  // PML flag in any direction; band_zend holds the rest of the rows
+  Band band_core{};
   QCore qcore{};
 
   static Span span_run(int lo, int hi) {
@@ -1111,14 +1122,19 @@ public:
       xhi = std::max(xhi, xlo - 1);
       yhi = std::max(yhi, ylo - 1);
       band_rows = Band{{span_run(xlo, xhi), span_run(ylo, yhi), span_run(0, p.N[2] - 1)}};
-      int zlo = std::min(p.T[2][0] + 1, p.N[2]), zhi = p.N[2] - p.T[2][1] - 1;
-      zhi = std::max(zhi, zlo - 1);
       const Span sxr = span_run(xlo, xhi), sxo = span_outside(p.N[0], xlo, xhi);
       const Span syr = span_run(ylo, yhi), syo = span_outside(p.N[1], ylo, yhi);
-      const Span szr = span_run(zlo, zhi), szo = span_outside(p.N[2], zlo, zhi), sza = span_run(0, p.N[2] - 1);
-      band_xface = Band{{sxo, syr, szr}};
-      band_yface = Band{{sxr, syo, szr}};
+      const Span sza = span_run(0, p.N[2] - 1);
+      // the x and y slabs take whole z rows (warps start on 128-byte
+      // boundaries; the z slabs ride along on the z flags)
+      band_xface = Band{{sxo, syr, sza}};
+      band_yface = Band{{sxr, syo, sza}};
       band_xyedge = Band{{sxo, syo, sza}};
+      int zlo = std::min(p.T[2][0] + 1, p.N[2]), zhi = p.N[2] - p.T[2][1] - 1;
+      zhi = std::max(zhi, zlo - 1);
+      const Span szr = span_run(zlo, zhi), szo = span_outside(p.N[2], zlo, zhi);
+      band_xface_zi = Band{{sxo, syr, szr}};
+      band_yface_zi = Band{{sxr, syo, szr}};
       band_xzedge = Band{{sxo, syr, szo}};
       band_yzedge = Band{{sxr, syo, szo}};
       // the B core: z interior (no slab, off the low wall) rounded inwards to quads
@@ -1132,6 +1148,9 @@ public:
       band_zend = Band{{span_run(xlo, xhi), span_run(ylo, yhi),
                         qcore.zend > qcore.lo[2] ? span_outside(p.N[2], qcore.lo[2], qcore.zend - 1)
                                                  : span_run(0, p.N[2] - 1)}};
+      band_core = qcore.zend > qcore.lo[2]
+                      ? Band{{span_run(xlo, xhi), span_run(ylo, yhi), span_run(qcore.lo[2], qcore.zend - 1)}}
+                      : Band{{span_run(0, -1), span_run(0, -1), span_run(0, -1)}};
       check_bands(p);
       return;
     }
@@ -1177,17 +1196,39 @@ public:
           for (int t2 = 0; t2 < b.s[2].n; t2++)
             mark(kof(b.s[0], t0), kof(b.s[1], t1), kof(b.s[2], t2));
     };
+    bool zi = false; // which shell: full-row faces or z-interior faces + z edges
     auto slabs = [&] {
-      band(band_xface);
-      band(band_yface);
+      if (zi) {
+        band(band_xface_zi);
+        band(band_yface_zi);
+        band(band_xzedge);
+        band(band_yzedge);
+      }
+      else {
+        band(band_xface);
+        band(band_yface);
+      }
       band(band_xyedge);
-      band(band_xzedge);
-      band(band_yzedge);
     };
     slabs();
     band(band_rows);
     for (unsigned char v : seen)
       if (v != 1) throw Error("internal: launch bands do not tile the grid");
+    // the one-point core + z ends instead of the rows, with the FP64 shell
+    for (int pass = 0; pass < 2; pass++) {
+      zi = pass == 1;
+      std::fill(seen.begin(), seen.end(), 0);
+      slabs();
+      if (band_core.s[2].n > 0) {
+        band(band_core);
+        band(band_zend);
+      }
+      else
+        band(band_rows);
+      for (unsigned char v : seen)
+        if (v != 1) throw Error("internal: launch bands do not tile the grid");
+    }
+    zi = false;
     // the FP32 B update: core + z ends instead of the rows
     std::fill(seen.begin(), seen.end(), 0);
     slabs();
@@ -1237,13 +1278,23 @@ public:
         }
         launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
       }
+      else if (band_core.s[2].n > 0) {
+        launch_b_band<false, false, false>(band_core, a, cndB, zp, stream);
+        launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
+      }
       else
         launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
-      launch_b_band<true, false, false>(band_xface, a, cndB, zp, side[0]);
-      launch_b_band<false, true, false>(band_yface, a, cndB, zp, side[1]);
+      if (F32) {
+        launch_b_band<true, false>(band_xface, a, cndB, zp, side[0]);
+        launch_b_band<false, true>(band_yface, a, cndB, zp, side[1]);
+      }
+      else {
+        launch_b_band<true, false, false>(band_xface_zi, a, cndB, zp, side[0]);
+        launch_b_band<false, true, false>(band_yface_zi, a, cndB, zp, side[1]);
+        launch_b_band<true, false>(band_xzedge, a, cndB, zp, side[4]);
+        launch_b_band<false, true>(band_yzedge, a, cndB, zp, side[5]);
+      }
       launch_b_band<true, true>(band_xyedge, a, cndB, zp, side[3]);
-      launch_b_band<true, false>(band_xzedge, a, cndB, zp, side[4]);
-      launch_b_band<false, true>(band_yzedge, a, cndB, zp, side[5]);
       join();
     }
     else {
@@ -1282,12 +1333,25 @@ public:
       }
     if constexpr (DIM == 3) {
       fork();
-      launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
-      launch_de_band<true, false, false>(band_xface, a, cndD, zp, side[0]);
-      launch_de_band<false, true, false>(band_yface, a, cndD, zp, side[1]);
+      // FP64 (issue-bound): the flagless core and the z ends; FP32
+      // (bandwidth-bound): whole rows, whose z slabs ride along in full warps
+      if (!F32 && band_core.s[2].n > 0) {
+        launch_de_band<false, false, false>(band_core, a, cndD, zp, stream);
+        launch_de_band<false, false>(band_zend, a, cndD, zp, side[2]);
+      }
+      else
+        launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
+      if (F32) {
+        launch_de_band<true, false>(band_xface, a, cndD, zp, side[0]);
+        launch_de_band<false, true>(band_yface, a, cndD, zp, side[1]);
+      }
+      else {
+        launch_de_band<true, false, false>(band_xface_zi, a, cndD, zp, side[0]);
+        launch_de_band<false, true, false>(band_yface_zi, a, cndD, zp, side[1]);
+        launch_de_band<true, false>(band_xzedge, a, cndD, zp, side[4]);
+        launch_de_band<false, true>(band_yzedge, a, cndD, zp, side[5]);
+      }
       launch_de_band<true, true>(band_xyedge, a, cndD, zp, side[3]);
-      launch_de_band<true, false>(band_xzedge, a, cndD, zp, side[4]);
-      launch_de_band<false, true>(band_yzedge, a, cndD, zp, side[5]);
       join();
     }
     else {

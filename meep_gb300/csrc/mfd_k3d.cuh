@@ -365,13 +365,13 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
 }
 
 template <typename R, bool CND, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256) b3_band_kernel(const FusedArgs<R> a, const Band bd) {
+__global__ void __launch_bounds__(256, 8) b3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];
   if (band_coords(bd, k)) b3_point<R, CND, FX, FY, FZ>(a, k);
 }
 
 template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256) de3_band_kernel(const FusedArgs<R> a, const Band bd) {
+__global__ void __launch_bounds__(256, 8) de3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];
   if (band_coords(bd, k)) de3_point<R, CND, POLES, FX, FY, FZ>(a, k);
 }
