@@ -338,12 +338,17 @@ template <typename R> __global__ void fmp_kernel(FmpArgs<R> a) {
   a.out[i] = v;
 }
 
-// integrated E sources subtracted from f_minus_p (src/update_eh.cpp:126-137)
-template <typename R> __global__ void src_fmp_kernel(R *fmp, const SrcPoint *pts, int n, DipoleVals dv) {
+// integrated E sources subtracted from f_minus_p (src/update_eh.cpp:126-137);
+// f_minus_p at the source point is formed afresh from D and P first, since a
+// source may sit on a point that the D pass does not visit (a wall)
+template <typename R> __global__ void src_fmp_kernel(FmpArgs<R> fa, const SrcPoint *pts, int n, DipoleVals dv) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const SrcPoint &sp = pts[j];
-  R v = fmp[sp.i];
+  R *fmp = fa.out;
+  R v = fa.d[sp.i];
+  for (int q = 0; q < fa.np; q++)
+    if (fa.p[q]) v -= fa.p[q][sp.i];
   for (int t = 0; t < sp.nterm; t++) {
     const double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
     v -= R(re);
@@ -922,7 +927,9 @@ public:
       has_b_current = has_b_current || ncur[comp(MFD_B, d)] > 0;
     if (getenv("MFD_GENERIC_KERNELS")) fused_mask = -1;
     if (p.any_periodic()) fused_mask = -1; // Bloch boundaries: the per-component kernels
-    if (p.any_offdiag) fused_mask = -1;    // off-diagonal chi1inv: E needs D of all components first
+    // off-diagonal chi1inv: E needs D - P of all components first; the 3-D
+    // band kernels run it as two passes, the 2-D/1-D fused kernels not at all
+    if (p.any_offdiag && p.g.dim != 3) fused_mask = -1;
     if (fused_mask >= 0) plan_boxes(p);
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
   }
@@ -979,6 +986,15 @@ public:
     a.dtdx = R(p.g.courant);
     a.dt2 = R(p.dt) * R(0.5);
     a.fuse_h = fuse_h;
+    for (int d = 0; d < 3; d++) {
+      a.fmp[d] = fmp[d];
+      a.noff[d] = p.offdiag[d].n;
+      for (int q = 0; q < p.offdiag[d].n; q++) {
+        a.chio[d][q] = chioff[d][q];
+        a.odir[d][q] = p.offdiag[d].dir[q];
+        a.osx[d][q] = (int)p.stride[p.offdiag[d].dir[q]];
+      }
+    }
     return a;
   }
 
@@ -1064,6 +1080,91 @@ public:
     if (a.npoles > 0) launch_de_band_p<FX, FY, true>(bd, g, blk, a, cnd, zp, st);
     else launch_de_band_p<FX, FY, false>(bd, g, blk, a, cnd, zp, st);
     nlaunch++;
+  }
+
+  // the two passes of the off-diagonal D/E half-step (3-D)
+  template <bool FX, bool FY, bool ZCAN = true>
+  void launch_d_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp_, cudaStream_t st) {
+    const bool zp = ZCAN && zp_;
+    dim3 g, blk;
+    band_shape(bd, g, blk);
+    if (g.x == 0) return;
+    if (cnd && zp) d3_band_kernel<R, true, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else if (cnd) d3_band_kernel<R, true, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    else if (zp) d3_band_kernel<R, false, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else d3_band_kernel<R, false, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    nlaunch++;
+  }
+  template <bool FX, bool FY, bool ZCAN = true>
+  void launch_e_band(const Band &bd, const FusedArgs<R> &a, bool zp_, cudaStream_t st) {
+    const bool zp = ZCAN && zp_;
+    dim3 g, blk;
+    band_shape(bd, g, blk);
+    if (g.x == 0) return;
+    const bool poles = a.npoles > 0;
+    if (poles && zp) e3_band_kernel<R, true, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else if (poles) e3_band_kernel<R, true, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    else if (zp) e3_band_kernel<R, false, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else e3_band_kernel<R, false, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    nlaunch++;
+  }
+  // launches one pass over rows + shell (the shell on the side streams)
+  template <class F> void over_bands3(const Plan &p, F &&launch) {
+    constexpr bool F32 = std::is_same<R, float>::value;
+    (void)p;
+    fork();
+    launch(band_rows, 0, stream);
+    if (F32) {
+      launch(band_xface, 1, side[0]);
+      launch(band_yface, 2, side[1]);
+    }
+    else {
+      launch(band_xface_zi, 4, side[0]);
+      launch(band_yface_zi, 5, side[1]);
+      launch(band_xzedge, 6, side[4]);
+      launch(band_yzedge, 7, side[5]);
+    }
+    launch(band_xyedge, 3, side[3]);
+    join();
+  }
+  void offdiag_de3(const Plan &p, const FusedArgs<R> &a, bool cnd, bool zp, const DipoleVals &dip) {
+    // kind: 0 rows, 1 full-row x faces, 2 full-row y faces, 3 xy edges,
+    // 4/5 z-interior x/y faces, 6/7 their z edges
+    over_bands3(p, [&](const Band &b, int kind, cudaStream_t st) {
+      switch (kind) {
+        case 0: launch_d_band<false, false>(b, a, cnd, zp, st); break;
+        case 1: launch_d_band<true, false>(b, a, cnd, zp, st); break;
+        case 2: launch_d_band<false, true>(b, a, cnd, zp, st); break;
+        case 3: launch_d_band<true, true>(b, a, cnd, zp, st); break;
+        case 4: launch_d_band<true, false, false>(b, a, cnd, zp, st); break;
+        case 5: launch_d_band<false, true, false>(b, a, cnd, zp, st); break;
+        case 6: launch_d_band<true, false>(b, a, cnd, zp, st); break;
+        default: launch_d_band<false, true>(b, a, cnd, zp, st); break;
+      }
+    });
+    for (int d = 0; d < 3; d++)
+      if (nsrcpts[d] && fmp[d]) {
+        FmpArgs<R> fa{};
+        fa.out = fmp[d];
+        fa.d = f[comp(MFD_D, d)];
+        fa.np = (int)poles.size();
+        for (int q = 0; q < fa.np; q++)
+          fa.p[q] = poles[q].P[d];
+        src_fmp_kernel<R><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(fa, d_srcpts[d], nsrcpts[d], dip);
+        nlaunch++;
+      }
+    over_bands3(p, [&](const Band &b, int kind, cudaStream_t st) {
+      switch (kind) {
+        case 0: launch_e_band<false, false>(b, a, zp, st); break;
+        case 1: launch_e_band<true, false>(b, a, zp, st); break;
+        case 2: launch_e_band<false, true>(b, a, zp, st); break;
+        case 3: launch_e_band<true, true>(b, a, zp, st); break;
+        case 4: launch_e_band<true, false, false>(b, a, zp, st); break;
+        case 5: launch_e_band<false, true, false>(b, a, zp, st); break;
+        case 6: launch_e_band<true, false>(b, a, zp, st); break;
+        default: launch_e_band<false, true>(b, a, zp, st); break;
+      }
+    });
   }
 
   dim3 core_grid() const {
@@ -1325,6 +1426,12 @@ public:
       update_e(p, dip);
       return;
     }
+    if constexpr (DIM == 3) {
+      if (p.any_offdiag) {
+        offdiag_de3(p, a, cndD, zp, dip);
+        return;
+      }
+    }
     for (int d = 0; d < 3; d++)
       if (nsrcpts[d]) {
         fused_src_pre_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(
@@ -1408,14 +1515,16 @@ public:
           sp.nterm++;
         }
       }
-      // points outside the updated range are never advanced (metal walls)
+      // points outside the updated range are never advanced (metal walls);
+      // with off-diagonal chi1inv their f_minus_p is still read by the
+      // neighbouring E points, so they stay (only f_minus_p uses the list then)
       std::vector<SrcPoint> keep;
       int ec = comp(MFD_E, d);
       for (const SrcPoint &sp : pts) {
         bool in = true;
         for (int q = 0; q < 3; q++)
           in = in && sp.k[q] >= p.klo[ec][q] && sp.k[q] <= p.khi[ec][q];
-        if (in) keep.push_back(sp);
+        if (in || p.any_offdiag) keep.push_back(sp);
       }
       nsrcpts[d] = (int)keep.size();
       if (!keep.empty()) {
@@ -1621,7 +1730,7 @@ public:
       fmp_kernel<R><<<(unsigned)((p.nstore + 255) / 256), 256, 0, stream>>>(fa);
       nlaunch++;
       if (nsrcpts[d]) {
-        src_fmp_kernel<R><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(fmp[d], d_srcpts[d], nsrcpts[d], dip);
+        src_fmp_kernel<R><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(fa, d_srcpts[d], nsrcpts[d], dip);
         nlaunch++;
       }
     }

@@ -38,6 +38,12 @@ template <typename R> struct FusedArgs {
   int s[3];
   const R *sig[3], *kap[3], *siginv[3]; // PML tables by half-pixel position
   bool fuse_h;   // update H in the PML slab right after B
+  // off-diagonal inverse permittivity (3-D, two-pass D/E): f_minus_p of each
+  // D component (null: D itself), the off-diagonal terms of each E component
+  // (arrays, strides of their directions) in the reference's order
+  R *fmp[3];
+  const R *chio[3][2];
+  int noff[3], odir[3][2], osx[3][2];
   __device__ __forceinline__ R tbs(int d, int p) const { return sig[d][p]; }
   __device__ __forceinline__ R tbk(int d, int p) const { return kap[d][p]; }
   __device__ __forceinline__ R tbsi(int d, int p) const { return siginv[d][p]; }

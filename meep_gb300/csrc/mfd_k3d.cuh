@@ -364,6 +364,125 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
   }
 }
 
+// Off-diagonal inverse permittivity: E along d reads D - P of the other
+// components at the four points around it, so the D/E half-step runs as two
+// passes.  Pass 1: D (with f_u, f_cond) exactly as in de3_point, then
+// f_minus_p = D - P (poles in list order) where the component has poles or
+// integrated sources (src/update_eh.cpp:108-123).
+template <typename R, bool CND, bool FX, bool FY, bool FZ>
+__device__ __forceinline__ void d3_point(const FusedArgs<R> &a, const int k[3]) {
+  const int sx = a.s[0], sy = a.s[1];
+  const int i = k[0] * sx + k[1] * sy + k[2];
+  ShellFlags<R> F;
+  band_flags<R, FX, FY, FZ>(a, k, F);
+  const bool vx = k[1] >= 1 && k[2] >= 1, vy = k[0] >= 1 && k[2] >= 1, vz = k[0] >= 1 && k[1] >= 1;
+  const R *Hx = F.s0[0] ? a.h[0] : a.b[0];
+  const R *Hy = F.s0[1] ? a.h[1] : a.b[1];
+  const R *Hz = F.s0[2] ? a.h[2] : a.b[2];
+  const int mx = k[0] >= 1 ? sx : 0, my = k[1] >= 1 ? sy : 0, mz = k[2] >= 1 ? 1 : 0;
+  const R hx = Hx[i], hxy = Hx[i - my], hxz = Hx[i - mz];
+  const R hy = Hy[i], hyx = Hy[i - mx], hyz = Hy[i - mz];
+  const R hz = Hz[i], hzx = Hz[i - mx], hzy = Hz[i - my];
+  const R dx = a.d[0][i], dy = a.d[1][i], dz = a.d[2][i];
+  const R Xx = (hzy - hz) + hy - hyz;
+  const R Xy = (hxz - hx) + hz - hzx;
+  const R Xz = (hyx - hy) + hx - hxy;
+  const R dtdx = a.dtdx, dt2 = a.dt2;
+  const int p0x = 2 * k[0], p0y = 2 * k[1], p0z = 2 * k[2];
+  bool hcx = CND && a.cnd[2][0] != nullptr, hcy = CND && a.cnd[2][1] != nullptr, hcz = CND && a.cnd[2][2] != nullptr;
+  if (hcx && F.s0[1]) hcx = chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]);
+  if (hcy && F.s0[2]) hcy = chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]);
+  if (hcz && F.s0[0]) hcz = chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]);
+  const CurlRes<R> c[3] = {
+      curl_general(dx, Xx, dtdx, dt2, F.s0[1], F.s0[2], hcx, a.sig[1], a.kap[1], a.siginv[1], p0y, a.sig[2],
+                   a.kap[2], a.siginv[2], p0z, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i),
+      curl_general(dy, Xy, dtdx, dt2, F.s0[2], F.s0[0], hcy, a.sig[2], a.kap[2], a.siginv[2], p0z, a.sig[0],
+                   a.kap[0], a.siginv[0], p0x, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i),
+      curl_general(dz, Xz, dtdx, dt2, F.s0[0], F.s0[1], hcz, a.sig[0], a.kap[0], a.siginv[0], p0x, a.sig[1],
+                   a.kap[1], a.siginv[1], p0y, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i)};
+  const bool v[3] = {vx, vy, vz};
+#pragma unroll
+  for (int dc = 0; dc < 3; dc++) {
+    if (!v[dc]) continue;
+    a.d[dc][i] = c[dc].f;
+    if (c[dc].wfu) a.fu[2][dc][i] = c[dc].fu;
+    if (c[dc].wfc) a.fcnd[2][dc][i] = c[dc].fc;
+    if (a.fmp[dc]) {
+      R g = c[dc].f;
+#pragma unroll
+      for (int q = 0; q < MAX_POLES; q++)
+        if (q < a.npoles && a.P[q][dc]) g -= a.P[q][dc][i];
+      a.fmp[dc][i] = g;
+    }
+  }
+}
+
+// Pass 2: E = chi_dd g + OFFDIAG terms (g = f_minus_p or D), f_w inside the
+// slab along E's own direction, then the poles (src/step_generic.cpp:566-785,
+// OFFDIAG :580-582).
+template <typename R, bool POLES, bool FX, bool FY, bool FZ>
+__device__ __forceinline__ void e3_point(const FusedArgs<R> &a, const int k[3]) {
+  const int sx = a.s[0], sy = a.s[1];
+  const int i = k[0] * sx + k[1] * sy + k[2];
+  ShellFlags<R> F;
+  band_flags<R, FX, FY, FZ>(a, k, F);
+  const bool v[3] = {k[1] >= 1 && k[2] >= 1, k[0] >= 1 && k[2] >= 1, k[0] >= 1 && k[1] >= 1};
+  const int pw[3] = {2 * k[0] + 1, 2 * k[1] + 1, 2 * k[2] + 1};
+#pragma unroll
+  for (int dc = 0; dc < 3; dc++) {
+    if (!v[dc]) continue;
+    const R *G = a.fmp[dc] ? a.fmp[dc] : a.d[dc];
+    const R gs = G[i], us = a.chi[dc][i];
+    R val = (gs * us);
+    const int s = a.s[dc];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      if (q >= a.noff[dc]) break;
+      const int od = a.odir[dc][q], sxo = a.osx[dc][q];
+      const R *g = a.fmp[od] ? a.fmp[od] : a.d[od];
+      const R *u = a.chio[dc][q];
+      val = val + R(0.25) * ((g[i] + g[i - sxo]) * u[i] + (g[i + s] + g[(i + s) - sxo]) * u[i + s]);
+    }
+    EShell<R> o;
+    o.wfw = false;
+    o.fw = R(0);
+    R W;
+    if (F.s1[dc]) {
+      const R fwprev = a.fw[0][dc][i], kk = a.kap[dc][pw[dc]], ss = a.sig[dc][pw[dc]];
+      o.fw = val;
+      o.wfw = true;
+      o.e = a.e[dc][i] + ((kk + ss) * val - (kk - ss) * fwprev);
+      W = val;
+    }
+    else {
+      o.e = val;
+      W = o.e;
+    }
+    if (POLES) {
+#pragma unroll
+      for (int q = 0; q < MAX_POLES; q++)
+        if (q < a.npoles && a.P[q][dc]) {
+          o.pc[q] = a.P[q][dc][i];
+          o.pn[q] = a.pg1inv[q] * (o.pc[q] * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][dc][i] +
+                                   a.pw0[q] * (a.ps[q][dc][i] * W));
+        }
+    }
+    e_store<R, POLES>(a, dc, i, o);
+  }
+}
+
+template <typename R, bool CND, bool FX, bool FY, bool FZ>
+__global__ void __launch_bounds__(256, 8) d3_band_kernel(const FusedArgs<R> a, const Band bd) {
+  int k[3];
+  if (band_coords(bd, k)) d3_point<R, CND, FX, FY, FZ>(a, k);
+}
+
+template <typename R, bool POLES, bool FX, bool FY, bool FZ>
+__global__ void __launch_bounds__(256, 8) e3_band_kernel(const FusedArgs<R> a, const Band bd) {
+  int k[3];
+  if (band_coords(bd, k)) e3_point<R, POLES, FX, FY, FZ>(a, k);
+}
+
 template <typename R, bool CND, bool FX, bool FY, bool FZ>
 __global__ void __launch_bounds__(256, 8) b3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];

@@ -40,6 +40,7 @@ int main(int argc, char **argv) {
   std::unique_ptr<Workload> wl;
   if (name == "vec3d_full") wl = make_vec3d(256, 256, 256, 20.0, 0.8, 60, 42, 200, 50);
   else if (name == "vec3d_mid") wl = make_vec3d(128, 128, 128, 20.0, 0.8, 30, 42, 100, 50);
+  else if (name == "vec3d_rot") wl = make_vec3d(256, 256, 256, 20.0, 0.8, 60, 42, 200, 50, true);
   else if (name == "tm2d_full") wl = make_tm2d(512, 512, 16.0, 1.0, 40, 1234, 400, 51, 0);
   else if (name == "disp3d_full") wl = make_disp3d(384, 384, 192, 20.0, 0.8, 200, 1);
   else if (name == "disp3d_mid") wl = make_disp3d(192, 192, 96, 20.0, 0.8, 200, 1);

@@ -23,6 +23,7 @@
 #include <meep.hpp>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <memory>
 #include <random>
@@ -52,6 +53,11 @@ public:
   double split = 0.0;
   double sigma_lower = 0.0; // susceptibility strength below the split
   double cond_upper = 0.0;  // D conductivity above the split
+
+  // anisotropic boxes rotated by 30 degrees about z: chi1inv = R diag(1/eps) R^T
+  // has xy off-diagonal entries (the structure then takes the two-pass
+  // off-diagonal D/E update)
+  bool rotate_aniso = false;
 
   double coord_split(const vec &r) const { return dim == 3 ? r.z() : r.y(); }
 
@@ -91,7 +97,16 @@ public:
       return;
     }
     eps_diag(v.center(), e);
-    row[component_direction(c) % 3] = 1.0 / e[component_direction(c) % 3];
+    const int d = component_direction(c) % 3;
+    if (rotate_aniso && d < 2 && (e[0] != e[1])) {
+      const double cs = std::sqrt(0.75), sn = 0.5;
+      const double i0 = 1.0 / e[0], i1 = 1.0 / e[1];
+      const double xx = cs * cs * i0 + sn * sn * i1, yy = sn * sn * i0 + cs * cs * i1, xy = cs * sn * (i0 - i1);
+      row[0] = d == 0 ? xx : xy;
+      row[1] = d == 0 ? xy : yy;
+      return;
+    }
+    row[d] = 1.0 / e[d];
   }
   virtual bool is_thread_safe() const { return true; }
   virtual bool has_conductivity(component c) { return cond_upper != 0.0 && is_D(c); }
@@ -179,12 +194,14 @@ inline std::unique_ptr<Workload> make_tm2d(int ncells_x, int ncells_y, double re
 }
 
 inline std::unique_ptr<Workload> make_vec3d(int nx, int ny, int nz, double res, double dpml,
-                                            int nbox, uint64_t seed, int flux_cells, int nfreq) {
+                                            int nbox, uint64_t seed, int flux_cells, int nfreq,
+                                            bool rotate_aniso = false) {
   std::unique_ptr<Workload> w(new Workload);
   double sx = nx / res, sy = ny / res, sz = nz / res;
   w->gv = vol3d(sx, sy, sz, res);
   w->gv.center_origin();
   w->mat.dim = 3;
+  w->mat.rotate_aniso = rotate_aniso;
   std::mt19937_64 rng(seed);
   std::uniform_real_distribution<double> u01(0.0, 1.0);
   const double choices[3] = {2.1, 4.0, 12.0};

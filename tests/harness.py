@@ -70,13 +70,16 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
-                   nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False):
+                   nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
     arrays on a small grid with PML; integrated E sources at random points and
     a current source; two DFT monitors.  Returns dict of field arrays and DFT
-    sums after `steps` steps; `n` overrides the random grid size."""
+    sums after `steps` steps; `n` overrides the random grid size.  offdiag:
+    off-diagonal inverse permittivities on 40% of the points (Ex: xy and xz,
+    Ey: yz only, Ez: zy only -- the reference's 3x3, 2x2 and swapped 2x2
+    cases); ecur=False makes every E source integrated (no D current)."""
     rng = np.random.default_rng(seed)
     nrand = n
     if dim == 2:
@@ -106,6 +109,13 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     for c in comps:
         if c // 3 == _lib.E:
             sim.set_chi1inv(c, c % 3, 1.0 / rng.uniform(1.0, 12.0, size=shape))
+    if offdiag:
+        for c, dirs in ((_lib.comp(_lib.E, 0), (1, 2)), (_lib.comp(_lib.E, 1), (2,)), (_lib.comp(_lib.E, 2), (1,))):
+            if c not in comps:
+                continue
+            for d in dirs:
+                arr = np.where(rng.uniform(size=shape) < 0.4, rng.uniform(-0.08, 0.08, size=shape), 0.0)
+                sim.set_chi1inv(c, d, arr)
     if cond:
         for c in comps:
             if c // 3 == _lib.D:
@@ -126,7 +136,7 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
         c = ecomps[j % len(ecomps)]
         idx = rng.choice(ndense, size=4, replace=False)
         amp = rng.normal(size=4) + 1j * rng.normal(size=4)
-        sim.add_source_points(c, s_int if j else s_cur, idx, amp)
+        sim.add_source_points(c, s_int if (j or not ecur) else s_cur, idx, amp)
     # an H current source
     hc = [c for c in comps if c // 3 == _lib.H][0]
     sim.add_source_points(hc, s_cur, rng.choice(ndense, size=3, replace=False), rng.normal(size=3))

@@ -73,3 +73,26 @@ def test_bloch_fp32_close(engine_lib, oracle_lib):
     o = _run(oracle_lib, 35, 3, 64, bloch={0: 0.2, 1: 0.1})
     for k in o:
         assert relerr(g[k], o[k]) <= 1e-3, (k, relerr(g[k], o[k]))
+
+
+@pytest.mark.parametrize("seed,poles,pml", [(41, True, True), (42, False, True), (43, True, False)])
+def test_offdiag_3d_fp64_bitwise(seed, poles, pml, engine_lib, oracle_lib):
+    """Off-diagonal inverse permittivity on the 3-D two-pass band kernels (D,
+    f_minus_p; then E with OFFDIAG terms and poles): the same bits as the
+    oracle's restatement of update_eh, with PML, poles and integrated sources."""
+    kw = dict(poles=poles, pml=pml, offdiag=True, ecur=False, steps=50)
+    out = random_problem(lambda **k: _lib.Sim(_lib.Engine(engine_lib), **k), seed, 3, **kw)
+    ref = random_problem(lambda **k: _lib.Sim(_lib.Engine(oracle_lib), **k), seed, 3, **kw)
+    for k in ref:
+        if k.startswith("c"):
+            assert np.array_equal(out[k], ref[k]), k
+        else:
+            assert relerr(out[k], ref[k]) <= 1e-13, k
+
+
+def test_offdiag_3d_fp32_close(engine_lib, oracle_lib):
+    kw = dict(offdiag=True, ecur=False, steps=50, precision=32)
+    out = random_problem(lambda **k: _lib.Sim(_lib.Engine(engine_lib), **k), 44, 3, **kw)
+    ref = random_problem(lambda **k: _lib.Sim(_lib.Engine(oracle_lib), **k), 44, 3, **kw)
+    for k in ref:
+        assert relerr(out[k], ref[k]) <= 1e-4, (k, relerr(out[k], ref[k]))
