@@ -126,8 +126,8 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_driver(exe, warmup, steps, e2e_steps, total, env=None, timeout=3600):
-    out = subprocess.run([exe, WORKLOAD, str(warmup), str(steps), str(e2e_steps), str(total)],
+def run_driver(exe, warmup, steps, e2e_steps, total, env=None, timeout=3600, workload=WORKLOAD):
+    out = subprocess.run([exe, workload, str(warmup), str(steps), str(e2e_steps), str(total)],
                          stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env,
                          timeout=timeout)
     if out.returncode != 0:
@@ -366,6 +366,9 @@ def main():
     with ClockSampler(local) as clk:
         r32 = run_driver(exe32, args.warmup, args.steps, e2e_steps, 0)
     r64 = run_driver(exe64, args.warmup, args.steps, 0, 0)
+    # the same cells with off-diagonal inverse permittivity (the 20% anisotropic
+    # boxes rotated by 30 degrees about z): two-pass D/E update
+    rrot = run_driver(exe32, args.warmup, max(100, args.steps // 4), 0, 0, workload="vec3d_rot")
     # the configuration's flux comparison: FULL_STEPS steps from t = 0
     total = FULL_STEPS
     f32 = run_driver(exe32, 0, 0, 0, total)
@@ -424,6 +427,10 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"value": value64, "unit": "Mcell-updates/s", "ms_per_step": t64 / args.steps * 1e3},
         "fp32_over_fp64": value / value64,
+        "offdiag_fp32": {"workload": "vec3d_rot (20% of the boxes with rotated anisotropic tensors: off-diagonal "
+                                     "chi1inv, two-pass D/E update)",
+                         "value": world * cells * rrot["steps"] / (rrot["device_ms"] * 1e-3) / 1e6,
+                         "unit": "Mcell-updates/s", "ms_per_step": rrot["device_ms"] / rrot["steps"]},
         "flux_rel_err_fp32_vs_fp64": flux_err,
         "flux_steps": total,
         "e2e": {"value": e2e, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
