@@ -370,6 +370,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 #include "mfd_q3d.cuh"
 #include "mfd_dft_tc.cuh"
 #include "mfd_adjoint.cuh"
+#include "mfd_adjoint3.cuh"
 namespace mfd {
 namespace cuda_impl {
 
@@ -2134,6 +2135,11 @@ public:
       adj_inject_kernel<R><<<(unsigned)((ia.npts + 255) / 256), 256, 0, stream>>>(geo, ia);
       nlaunch += 2;
     }
+    // 2-3. the 3-D band kernels when the forward runs them
+    if (p.g.dim == 3 && fused_mask == MASK3) {
+      adjoint_step3(p, slot);
+      return;
+    }
     // 2. reverse D/E half step
     for (int d = 0; d < 3; d++) {
       int c = comp(MFD_D, d);
@@ -2175,6 +2181,78 @@ public:
       adj_bh_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
       nlaunch++;
     }
+  }
+
+  // reversed step on the 3-D bands: D/E (E part and D curl of all three
+  // components per point), then B/H
+  void adjoint_step3(Plan &p, int64_t slot) {
+    Adj3Args<R> a{};
+    a.g = fused_args(p, true);
+    for (int d = 0; d < 3; d++) {
+      a.lE[d] = lam_f[comp(MFD_E, d)];
+      a.lfwE[d] = lam_fw[comp(MFD_E, d)];
+      a.lD[d] = lam_f[comp(MFD_D, d)];
+      a.lfuD[d] = lam_fu[comp(MFD_D, d)];
+      a.xbD[d] = xbar[comp(MFD_D, d)];
+      a.lH[d] = lam_f[comp(MFD_H, d)];
+      a.lfwH[d] = lam_fw[comp(MFD_H, d)];
+      a.lB[d] = lam_f[comp(MFD_B, d)];
+      a.lfuB[d] = lam_fu[comp(MFD_B, d)];
+      a.xbB[d] = xbar[comp(MFD_B, d)];
+      a.chi[d] = chi[comp(MFD_E, d)];
+      a.rec[d] = nullptr;
+      a.grad[d] = nullptr;
+      a.dlo[d] = dbox.lo[d];
+      a.dn[d] = dbox.n[d];
+    }
+    a.c = R(p.g.courant);
+    for (size_t q = 0; q < dcomps.size(); q++)
+      if (rec && ctype(dcomps[q]) == MFD_E) {
+        const int d = cdir(dcomps[q]);
+        a.rec[d] = rec + ((size_t)slot * dcomps.size() + q) * dnpts;
+        a.grad[d] = grad + q * dnpts;
+      }
+    const bool zp = a.g.pml[2] != 0;
+    auto launch = [&](auto kern_tag, const Band &b, int kind, cudaStream_t st) {
+      dim3 g, blk;
+      band_shape(b, g, blk);
+      if (g.x == 0) return;
+      constexpr int which = decltype(kern_tag)::value;
+      // kind: 0 rows, 1/2 full-row x/y faces, 3 xy edges, 4/5 z-interior x/y
+      // faces, 6/7 their z edges
+      const bool fx = kind == 1 || kind == 3 || kind == 4 || kind == 6;
+      const bool fy = kind == 2 || kind == 3 || kind == 5 || kind == 7;
+      const bool fz = zp && kind != 4 && kind != 5;
+#define MFD_ADJ3(FX, FY, FZ)                                                                     \
+  do {                                                                                             \
+    if (which == 0) adj3_de_band_kernel<R, FX, FY, FZ><<<g, blk, 0, st>>>(a, b);                   \
+    else adj3_bh_band_kernel<R, FX, FY, FZ><<<g, blk, 0, st>>>(a, b);                              \
+  } while (0)
+      if (fx && fy) {
+        if (fz) MFD_ADJ3(true, true, true);
+        else MFD_ADJ3(true, true, false);
+      }
+      else if (fx) {
+        if (fz) MFD_ADJ3(true, false, true);
+        else MFD_ADJ3(true, false, false);
+      }
+      else if (fy) {
+        if (fz) MFD_ADJ3(false, true, true);
+        else MFD_ADJ3(false, true, false);
+      }
+      else {
+        if (fz) MFD_ADJ3(false, false, true);
+        else MFD_ADJ3(false, false, false);
+      }
+#undef MFD_ADJ3
+      nlaunch++;
+    };
+    over_bands3(p, [&](const Band &b, int kind, cudaStream_t st) {
+      launch(std::integral_constant<int, 0>{}, b, kind, st);
+    });
+    over_bands3(p, [&](const Band &b, int kind, cudaStream_t st) {
+      launch(std::integral_constant<int, 1>{}, b, kind, st);
+    });
   }
 
   void adjoint_end(Plan &p, double *out) override {

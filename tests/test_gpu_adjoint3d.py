@@ -50,6 +50,17 @@ def test_adjoint3d_matches_finite_differences(small):
     assert relerr(adj, fd) <= 1e-6, (adj, fd)
 
 
+def test_adjoint3d_bands_equal_per_component(small, monkeypatch):
+    """The reversed steps on the 3-D band kernels give the gradient of the
+    per-component adjoint kernels to the bit (same per-point arithmetic and
+    gather order)."""
+    prob, eps = small
+    _, g_band = _grad(prob, eps, 64, 0)
+    monkeypatch.setenv("MFD_GENERIC_KERNELS", "1")
+    _, g_comp = _grad(prob, eps, 64, 0)
+    assert np.array_equal(g_band, g_comp)
+
+
 def test_adjoint3d_checkpointed_equals_recorded(small):
     prob, eps = small
     _, g_rec = _grad(prob, eps, 64, 0)
