@@ -41,40 +41,66 @@ __device__ __forceinline__ R gterm(const R *xb, const FusedArgs<R> &g, const int
   return v;
 }
 
-// adjoint of step_curl's branches for one component (adj_curl_core)
+// adjoint of step_curl's branches for one component (adj_curl_core), with
+// lambda of f_u already loaded (lfuv): returns lambda of f, xbar and the new
+// lambda of f_u (written only when both slabs apply)
+template <typename R> struct AdjCurl3 {
+  R lf, xb, lfu;
+};
 template <typename R>
-__device__ __forceinline__ void adj3_curl(const FusedArgs<R> &g, R c, bool sg, bool su, int ds, int ps, int du,
-                                          int pu, R *lf, R *lfu, R *xbar, int i, R lam) {
-  R lfv, xb;
+__device__ __forceinline__ AdjCurl3<R> adj3_curl(const FusedArgs<R> &g, R c, bool sg, bool su, int ds, int ps,
+                                                 int du, int pu, R lfuv, R lam) {
+  AdjCurl3<R> o;
+  o.lfu = lfuv;
   if (!sg && !su) {
-    lfv = lam;
-    xb = -c * lam;
+    o.lf = lam;
+    o.xb = -c * lam;
   }
   else if (!sg && su) {
     const R siu = g.siginv[du][pu], ku = g.kap[du][pu] - g.sig[du][pu];
-    const R lt = lfu[i] + siu * lam;
-    lfv = siu * ku * lam;
-    xb = -c * lt;
+    const R lt = lfuv + siu * lam;
+    o.lf = siu * ku * lam;
+    o.xb = -c * lt;
   }
   else if (sg && !su) {
     const R si = g.siginv[ds][ps], ks = g.kap[ds][ps] - g.sig[ds][ps];
-    lfv = ks * si * lam;
-    xb = -c * si * lam;
+    o.lf = ks * si * lam;
+    o.xb = -c * si * lam;
   }
   else {
     const R si = g.siginv[ds][ps], ks = g.kap[ds][ps] - g.sig[ds][ps];
     const R siu = g.siginv[du][pu], ku = g.kap[du][pu] - g.sig[du][pu];
-    const R lt = lfu[i] + siu * lam;
-    lfv = siu * ku * lam;
-    lfu[i] = ks * si * lt - siu * lam;
-    xb = -c * si * lt;
+    const R lt = lfuv + siu * lam;
+    o.lf = siu * ku * lam;
+    o.lfu = ks * si * lt - siu * lam;
+    o.xb = -c * si * lt;
   }
-  lf[i] = lfv;
-  xbar[i] = xb;
+  return o;
+}
+
+// gathered curl adjoints of the other half-step into component d (terms of
+// the forward curl plan, in its order)
+template <typename R, int STEP>
+__device__ __forceinline__ R gather3(const FusedArgs<R> &g, R *const *xb, int d, const int k[3], int i) {
+  R acc = R(0);
+  if (d == 0) {
+    acc += gterm<R, STEP>(xb[1], g, k, i, 2);
+    acc += -gterm<R, STEP>(xb[2], g, k, i, 1);
+  }
+  else if (d == 1) {
+    acc += -gterm<R, STEP>(xb[0], g, k, i, 2);
+    acc += gterm<R, STEP>(xb[2], g, k, i, 0);
+  }
+  else {
+    acc += gterm<R, STEP>(xb[0], g, k, i, 1);
+    acc += -gterm<R, STEP>(xb[1], g, k, i, 0);
+  }
+  return acc;
 }
 
 // reverse of the D/E half-step at one point: E part (objective terms already
-// in lambda_E, plus the gathered B-curl adjoints), then the D curl
+// in lambda_E, plus the gathered B-curl adjoints), then the D curl.  All
+// loads of the three components first, then the arithmetic, then the stores.
 template <typename R, bool FX, bool FY, bool FZ>
 __device__ __forceinline__ void adj3_de_point(const Adj3Args<R> &a, const int k[3]) {
   const FusedArgs<R> &g = a.g;
@@ -82,36 +108,35 @@ __device__ __forceinline__ void adj3_de_point(const Adj3Args<R> &a, const int k[
   ShellFlags<R> F;
   band_flags<R, FX, FY, FZ>(g, k, F);
   const bool v[3] = {k[1] >= 1 && k[2] >= 1, k[0] >= 1 && k[2] >= 1, k[0] >= 1 && k[1] >= 1};
+  R acc[3], lE[3], lD[3], ch[3], lfw[3], lfu[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int ds = (d + 1) % 3, du = (d + 2) % 3;
+    acc[d] = v[d] ? gather3<R, 1>(g, a.xbB, d, k, i) : R(0);
+    lE[d] = v[d] ? a.lE[d][i] : R(0);
+    lD[d] = v[d] ? a.lD[d][i] : R(0);
+    ch[d] = v[d] ? a.chi[d][i] : R(0);
+    lfw[d] = (v[d] && F.s1[d]) ? a.lfwE[d][i] : R(0);
+    lfu[d] = (v[d] && F.s0[du]) ? a.lfuD[d][i] : R(0);
+    (void)ds;
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (!v[d]) continue;
-    R acc = R(0);
-    if (d == 0) {
-      acc += gterm<R, 1>(a.xbB[1], g, k, i, 2);
-      acc += -gterm<R, 1>(a.xbB[2], g, k, i, 1);
-    }
-    else if (d == 1) {
-      acc += -gterm<R, 1>(a.xbB[0], g, k, i, 2);
-      acc += gterm<R, 1>(a.xbB[2], g, k, i, 0);
-    }
-    else {
-      acc += gterm<R, 1>(a.xbB[0], g, k, i, 1);
-      acc += -gterm<R, 1>(a.xbB[1], g, k, i, 0);
-    }
-    const R le = a.lE[d][i] + acc;
-    R lam = a.lD[d][i];
+    const R le = lE[d] + acc[d];
+    R lam = lD[d];
     const int pw = 2 * k[d] + 1;
     R gsrc;
     if (F.s1[d]) {
       const R kk = g.kap[d][pw], ss = g.sig[d][pw];
-      const R lfw = a.lfwE[d][i] + (kk + ss) * le;
+      const R lfwn = lfw[d] + (kk + ss) * le;
       a.lfwE[d][i] = -(kk - ss) * le;
       a.lE[d][i] = le;
-      lam += a.chi[d][i] * lfw;
-      gsrc = lfw;
+      lam += ch[d] * lfwn;
+      gsrc = lfwn;
     }
     else {
-      lam += a.chi[d][i] * le;
+      lam += ch[d] * le;
       a.lE[d][i] = R(0);
       gsrc = le;
     }
@@ -124,7 +149,11 @@ __device__ __forceinline__ void adj3_de_point(const Adj3Args<R> &a, const int k[
     }
     // D_d at shift 1 along d, 0 elsewhere: dsig = d+1, dsigu = d+2 at 2k
     const int ds = (d + 1) % 3, du = (d + 2) % 3;
-    adj3_curl<R>(g, a.c, F.s0[ds], F.s0[du], ds, 2 * k[ds], du, 2 * k[du], a.lD[d], a.lfuD[d], a.xbD[d], i, lam);
+    const bool sg = F.s0[ds], su = F.s0[du];
+    const AdjCurl3<R> o = adj3_curl<R>(g, a.c, sg, su, ds, 2 * k[ds], du, 2 * k[du], lfu[d], lam);
+    a.lD[d][i] = o.lf;
+    a.xbD[d][i] = o.xb;
+    if (sg && su) a.lfuD[d][i] = o.lfu;
   }
 }
 
@@ -137,48 +166,48 @@ __device__ __forceinline__ void adj3_bh_point(const Adj3Args<R> &a, const int k[
   ShellFlags<R> F;
   band_flags<R, FX, FY, FZ>(g, k, F);
   const bool v[3] = {k[0] >= 1, k[1] >= 1, k[2] >= 1};
+  R gs[3], lB[3], lH[3], lfw[3], lfu[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int du = (d + 2) % 3;
+    gs[d] = v[d] ? gather3<R, -1>(g, a.xbD, d, k, i) : R(0);
+    lB[d] = v[d] ? a.lB[d][i] : R(0);
+    lH[d] = (v[d] && F.s0[d]) ? a.lH[d][i] : R(0);
+    lfw[d] = (v[d] && F.s0[d]) ? a.lfwH[d][i] : R(0);
+    lfu[d] = (v[d] && F.s1[du]) ? a.lfuB[d][i] : R(0);
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (!v[d]) continue;
-    R gsum = R(0);
-    if (d == 0) {
-      gsum += gterm<R, -1>(a.xbD[1], g, k, i, 2);
-      gsum += -gterm<R, -1>(a.xbD[2], g, k, i, 1);
-    }
-    else if (d == 1) {
-      gsum += -gterm<R, -1>(a.xbD[0], g, k, i, 2);
-      gsum += gterm<R, -1>(a.xbD[2], g, k, i, 0);
-    }
-    else {
-      gsum += gterm<R, -1>(a.xbD[0], g, k, i, 1);
-      gsum += -gterm<R, -1>(a.xbD[1], g, k, i, 0);
-    }
-    R lam = a.lB[d][i];
+    R lam = lB[d];
     if (F.s0[d]) {
       const int pw = 2 * k[d];
       const R kk = g.kap[d][pw], ss = g.sig[d][pw];
-      const R lh = a.lH[d][i] + gsum;
+      const R lh = lH[d] + gs[d];
       a.lH[d][i] = lh;
-      lam += (kk + ss) * lh + a.lfwH[d][i];
+      lam += (kk + ss) * lh + lfw[d];
       a.lfwH[d][i] = -(kk - ss) * lh;
     }
     else
-      lam += gsum;
+      lam += gs[d];
     // B_d at shift 0 along d, 1 elsewhere: dsig = d+1, dsigu = d+2 at 2k+1
     const int ds = (d + 1) % 3, du = (d + 2) % 3;
-    adj3_curl<R>(g, a.c, F.s1[ds], F.s1[du], ds, 2 * k[ds] + 1, du, 2 * k[du] + 1, a.lB[d], a.lfuB[d], a.xbB[d], i,
-                 lam);
+    const bool sg = F.s1[ds], su = F.s1[du];
+    const AdjCurl3<R> o = adj3_curl<R>(g, a.c, sg, su, ds, 2 * k[ds] + 1, du, 2 * k[du] + 1, lfu[d], lam);
+    a.lB[d][i] = o.lf;
+    a.xbB[d][i] = o.xb;
+    if (sg && su) a.lfuB[d][i] = o.lfu;
   }
 }
 
 template <typename R, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256) adj3_de_band_kernel(const Adj3Args<R> a, const Band bd) {
+__global__ void __launch_bounds__(256, 8) adj3_de_band_kernel(const Adj3Args<R> a, const Band bd) {
   int k[3];
   if (band_coords(bd, k)) adj3_de_point<R, FX, FY, FZ>(a, k);
 }
 
 template <typename R, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256) adj3_bh_band_kernel(const Adj3Args<R> a, const Band bd) {
+__global__ void __launch_bounds__(256, 8) adj3_bh_band_kernel(const Adj3Args<R> a, const Band bd) {
   int k[3];
   if (band_coords(bd, k)) adj3_bh_point<R, FX, FY, FZ>(a, k);
 }
