@@ -11,7 +11,12 @@
 //   normal kernel (one thread per pixel): the quadrature normal in IEEE
 //     double over all objects; pixels that see one material (most of them)
 //     are finished here, the others go to a work list with their gradient.
-//   mean kernel (one warp per listed pixel): the objects whose bounding box
+//   level kernel (warps of 32 listed pixels, one refinement level per
+//     launch, the pixels that need the next level compacted into the next
+//     list): per pixel the warp evaluates tiles of samples, then each lane
+//     adds its own pixel's tile in sample order (details at the kernel);
+//   mean kernel (one warp per pixel, for pixels meeting more than LMAXC
+//     objects): the objects whose bounding box
 //     meets the pixel are gathered in shared memory (list order kept); the
 //     lanes evaluate the sample grid a tile at a time, deciding point-in-object
 //     in FP32 with a margin of 1e-5 of the magnitudes involved (FP32 error is
@@ -25,7 +30,9 @@
 // the reference's non-FMA x86-64 build.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "geom_eval.hpp"
@@ -335,6 +342,269 @@ __global__ void __launch_bounds__(32 * MEAN_WARPS)
   }
 }
 
+// ------------------------------------------------- phase 2, level by level
+// The per-pixel-warp kernel above adds every sample on lane 0, and GB300
+// issues a one-lane FP64 add at the cost of a full warp instruction.  Here a
+// warp takes 32 listed pixels at one refinement level (the same ms for the
+// whole list): for each pixel the warp evaluates a tile of samples (one per
+// lane, FP32 filter, exact FP64 test near surfaces), then every lane adds its
+// own pixel's tile in sample order -- 32 in-order sums per FP64 instruction.
+// Pixels that need the next level are compacted into the next list, so the
+// warps stay full.  A pixel meeting more than LMAXC objects' boxes goes to the
+// per-pixel-warp kernel instead.
+constexpr int LV_WARPS = 2; // warps per block
+constexpr int LMAXC = 6;    // objects per pixel
+constexpr int LTILE = 128;  // samples per pixel per round
+
+constexpr int LQMAX = 512; // samples queued for the exact test per round
+
+struct LvShared {
+  Cand cand[32][LMAXC];
+  double eps[32][LMAXC + 1], inv[32][LMAXC + 1];
+  double lo[32][3], ext[32][3];
+  unsigned char res[32][LTILE];
+  unsigned short q[LQMAX]; // (pixel << 8) | sample of the round
+  int nc[32], neg[32], nq;
+};
+
+// the material slot of sample si of pixel j in this round: FP32 tests in
+// list order from the last object; `exact` settles undecided ones in double
+// (false: return -1 at the first undecided object instead)
+__device__ __forceinline__ int sample_slot(const LvShared &S, const DeviceChi &chi, int dim, const bool act[3],
+                                           int j, const int ti[3], const float t[3], int ms, bool exact) {
+  const int nc = S.nc[j];
+  for (int c = nc - 1; c >= 0; c--) {
+    int r = test32(S.cand[j][c], t);
+    if (r == 0) {
+      if (!exact) return -1;
+      // lo + i * ext / ms, as in the reference
+      double p[3];
+      for (int d = 0; d < 3; d++)
+        p[d] = act[d] ? S.lo[j][d] + ti[d] * S.ext[j][d] / ms : 0.0;
+      r = mgb_geom::contains(chi.objs[S.cand[j][c].obj], p) ? 1 : -1;
+    }
+    if (r > 0) return c;
+  }
+  (void)dim;
+  return nc;
+}
+
+// the averaged row from the normal (gradient) and the means
+__device__ __forceinline__ void row_from_means(int cdir, const bool act[3], const double *g3, double meps,
+                                               double minveps, double *row) {
+  double g[3], g2 = 0.0;
+  for (int d = 0; d < 3; d++) {
+    g[d] = g3[d];
+    if (act[d]) g2 += g[d] * g[d];
+  }
+  const double inv = 1.0 / sqrt(g2);
+  double n[3] = {0, 0, 0};
+  for (int d = 0; d < 3; d++)
+    if (act[d]) n[d] = g[d] * inv;
+  for (int q = 0; q < 3; ++q)
+    row[q] = n[cdir] * n[q] * (minveps - 1 / meps);
+  row[cdir] += 1 / meps;
+}
+
+// means (meps, minveps) carried from one level to the next, per pixel
+struct LvState {
+  double meps, minveps;
+};
+
+__global__ void __launch_bounds__(32 * LV_WARPS, 6)
+    subpixel_level_kernel(int dim, int cdir, const double *lo, const double *hi, double tol, int ms, int first,
+                          int stop, DeviceChi chi, const double *grad, const int *win, int nin, LvState *st,
+                          int *wnext, int *nnext, int *wover, int *nover, double *rows) {
+  __shared__ LvShared sh_all[LV_WARPS];
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  LvShared &S = sh_all[wib];
+  const bool act[3] = {dim >= 2, dim >= 2, dim != 2};
+  const int n2 = dim >= 2 ? ms : 1, n3 = dim >= 3 ? ms : 1, cnt = ms * n2 * n3;
+  for (int w0 = (blockIdx.x * LV_WARPS + wib) * 32; w0 < nin; w0 += gridDim.x * LV_WARPS * 32) {
+    const int item = w0 + lane;
+    const bool mine = item < nin;
+    const int pix = mine ? win[item] : 0;
+    double l[3] = {0, 0, 0}, h[3] = {0, 0, 0};
+    if (mine) load_pixel(lo, hi, pix, l, h);
+    double cen[3] = {0, 0, 0};
+    for (int d = 0; d < 3; d++)
+      if (act[d]) cen[d] = (h[d] + l[d]) * 0.5;
+    // the objects meeting each pixel of the warp, in list order
+    for (int j = 0; j < 32; j++) {
+      const int jmine = __shfl_sync(full, (int)mine, j);
+      double lj[3], hj[3];
+      for (int d = 0; d < 3; d++) {
+        lj[d] = __shfl_sync(full, l[d], j);
+        hj[d] = __shfl_sync(full, h[d], j);
+      }
+      if (!jmine) {
+        if (lane == 0) S.nc[j] = 0;
+        continue;
+      }
+      int nc = 0;
+      for (int base = 0; base < chi.nobj; base += 32) {
+        const int q = base + lane;
+        const bool hit = q < chi.nobj && box_meets(chi.objs[q], lj, hj, act);
+        const unsigned mask = __ballot_sync(full, hit);
+        const int pos = nc + __popc(mask & ((1u << lane) - 1u));
+        if (hit && pos < LMAXC) {
+          const mfd_object &o = chi.objs[q];
+          Cand &c = S.cand[j][pos];
+          c.obj = q;
+          c.kind = o.kind;
+          for (int d = 0; d < 3; d++) {
+            c.a[d] = (float)((act[d] ? lj[d] : 0.0) - o.center[d]);
+            c.ax[d] = (float)o.axis[d];
+            c.hs[d] = (float)(0.5 * o.size[d]);
+          }
+          c.r2 = (float)(o.radius * o.radius);
+          c.hh = (float)(0.5 * o.height);
+          S.eps[j][pos] = o.eps;
+          S.inv[j][pos] = 1 / o.eps;
+        }
+        nc += __popc(mask);
+      }
+      if (lane < 3) {
+        S.lo[j][lane] = act[lane] ? lj[lane] : 0.0;
+        S.ext[j][lane] = act[lane] ? hj[lane] - lj[lane] : 0.0;
+      }
+      if (lane == 0) {
+        S.nc[j] = nc;
+        if (nc <= LMAXC) {
+          S.eps[j][nc] = chi.eps_default;
+          S.inv[j][nc] = 1 / chi.eps_default;
+        }
+      }
+    }
+    S.neg[lane] = 0;
+    __syncwarp();
+    const bool run = mine && S.nc[lane] <= LMAXC;
+    if (mine && !run && first) wover[atomicAdd(nover, 1)] = pix;
+    double old_meps = 1, old_minveps = 1;
+    if (run && !first) {
+      old_meps = st[pix].meps;
+      old_minveps = st[pix].minveps;
+    }
+    double sm = 0, smi = 0;
+    for (int base = 0; base < cnt; base += LTILE) {
+      const int nt = min(LTILE, cnt - base);
+      if (lane == 0) S.nq = 0;
+      __syncwarp();
+      for (int j = 0; j < 32; j++) {
+        const int jrun = __shfl_sync(full, (int)run, j);
+        if (!jrun) continue;
+        // sample spacing in FP32 for the filter (ext / ms to ~1e-7: far inside
+        // the filter's margin)
+        const float stf[3] = {(float)(S.ext[j][0] / ms), (float)(S.ext[j][1] / ms), (float)(S.ext[j][2] / ms)};
+        // this lane's samples si = lane + 32 m: grid indices carried forward
+        // by 32 at a time
+        int ix, jy, kz;
+        {
+          const int idx = base + lane;
+          if (dim == 1) {
+            ix = idx;
+            jy = kz = 0;
+          }
+          else {
+            ix = idx % ms;
+            jy = (idx / ms) % n2;
+            kz = idx / (ms * n2);
+          }
+        }
+#pragma unroll 4
+        for (int si = lane; si < nt; si += 32) {
+          // per-axis sample index: 1-D samples run along z
+          const int ti[3] = {dim == 1 ? 0 : ix, dim == 1 ? 0 : jy, dim == 1 ? ix : (dim == 3 ? kz : 0)};
+          float t[3];
+          for (int d = 0; d < 3; d++)
+            t[d] = act[d] ? (float)ti[d] * stf[d] : 0.f;
+          int slot = sample_slot(S, chi, dim, act, j, ti, t, ms, false);
+          if (slot < 0) {
+            // too close to a surface for FP32: queued for the exact test
+            const int qn = atomicAdd(&S.nq, 1);
+            if (qn < LQMAX) S.q[qn] = (unsigned short)((j << 8) | si);
+            else slot = sample_slot(S, chi, dim, act, j, ti, t, ms, true);
+          }
+          if (slot >= 0) {
+            S.res[j][si] = (unsigned char)slot;
+            if (S.eps[j][slot] < 0) S.neg[j] = 1;
+          }
+          if (dim == 1)
+            ix += 32;
+          else {
+            ix += 32;
+            while (ix >= ms) {
+              ix -= ms;
+              if (++jy >= n2) {
+                jy = 0;
+                kz++;
+              }
+            }
+          }
+        }
+      }
+      __syncwarp();
+      // the queued samples of all pixels of the round, with every lane busy
+      const int nq = min(S.nq, LQMAX);
+      for (int e = lane; e < nq; e += 32) {
+        const int j = S.q[e] >> 8, si = S.q[e] & 0xff, idx = base + si;
+        int ti[3] = {0, 0, 0};
+        if (dim == 1) ti[2] = idx;
+        else {
+          ti[0] = idx % ms;
+          ti[1] = (idx / ms) % n2;
+          if (dim == 3) ti[2] = idx / (ms * n2);
+        }
+        float t[3];
+        for (int d = 0; d < 3; d++)
+          t[d] = act[d] ? (float)ti[d] * (float)(S.ext[j][d] / ms) : 0.f;
+        const int slot = sample_slot(S, chi, dim, act, j, ti, t, ms, true);
+        S.res[j][si] = (unsigned char)slot;
+        if (S.eps[j][slot] < 0) S.neg[j] = 1;
+      }
+      __syncwarp();
+      if (run)
+        for (int q = 0; q < nt; q++) {
+          const int c = S.res[lane][q];
+          sm += S.eps[lane][c];
+          smi += S.inv[lane][c];
+        }
+      __syncwarp();
+    }
+    if (run) {
+      double *row = rows + 3 * pix;
+      double meps = sm, minveps = smi;
+      bool done;
+      if (S.neg[lane]) {
+        done = true;
+        if (dim != 1) {
+          row[0] = row[1] = row[2] = 0.0;
+          row[cdir] = 1 / chi(cen);
+        }
+        else {
+          meps = chi(cen);
+          minveps = 1 / meps;
+          row_from_means(cdir, act, grad + 3 * pix, meps, minveps, row);
+        }
+      }
+      else {
+        meps /= cnt;
+        minveps /= cnt;
+        done = stop || !(fabs(meps - old_meps) > tol * fabs(old_meps) &&
+                         fabs(minveps - old_minveps) > tol * fabs(old_minveps));
+        if (done) row_from_means(cdir, act, grad + 3 * pix, meps, minveps, row);
+      }
+      if (!done) {
+        st[pix].meps = meps;
+        st[pix].minveps = minveps;
+        wnext[atomicAdd(nnext, 1)] = pix;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 void check(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw Error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
 }
@@ -381,12 +651,36 @@ void subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const doub
     int sms = 0, dev = 0;
     check(cudaGetDevice(&dev), "cudaGetDevice");
     check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-    const int per_block = MEAN_WARPS;
-    const long long want = (nwork + per_block - 1) / per_block;
-    const unsigned blocks = (unsigned)std::min<long long>(want, (long long)sms * 16);
-    subpixel_mean_kernel<<<blocks, 32 * MEAN_WARPS>>>(dim, cdir, dlo, dhi, tol, maxeval, chi, dgrad, dwork, dnwork,
-                                                      drows);
-    check(cudaGetLastError(), "subpixel_mean_kernel launch");
+    // refinement levels: ms = 10, 20, 40, ... for the pixels still running
+    LvState *dst = b.alloc<LvState>(npix);
+    int *dnext = b.alloc<int>(nwork), *dover = b.alloc<int>(nwork), *dcount = b.alloc<int>(2);
+    check(cudaMemset(dcount, 0, 2 * sizeof(int)), "clear counts");
+    int *cur = dwork, *nxt = dnext, n = nwork, ms = 10, iter = 0, first = 1;
+    while (n > 0) {
+      const int ms2 = 2 * ms;
+      iter += dim == 3 ? ms2 * ms2 * ms2 : ms2 * ms2;
+      const int stop = maxeval && iter >= maxeval;
+      check(cudaMemset(dcount, 0, sizeof(int)), "clear next count");
+      const long long want = ((long long)n + 32 * LV_WARPS - 1) / (32 * LV_WARPS);
+      const unsigned blocks = (unsigned)std::min<long long>(want, (long long)sms * 8);
+      subpixel_level_kernel<<<blocks, 32 * LV_WARPS>>>(dim, cdir, dlo, dhi, tol, ms, first, stop, chi, dgrad, cur,
+                                                       n, dst, nxt, dcount, dover, dcount + 1, drows);
+      check(cudaGetLastError(), "subpixel_level_kernel launch");
+      check(cudaMemcpy(&n, dcount, sizeof(int), cudaMemcpyDeviceToHost), "next count");
+      std::swap(cur, nxt);
+      ms = ms2;
+      first = 0;
+    }
+    // pixels meeting too many objects: one warp each, all levels
+    int nover = 0;
+    check(cudaMemcpy(&nover, dcount + 1, sizeof(int), cudaMemcpyDeviceToHost), "overflow count");
+    if (nover > 0) {
+      const long long want = ((long long)nover + MEAN_WARPS - 1) / MEAN_WARPS;
+      const unsigned blocks = (unsigned)std::min<long long>(want, (long long)sms * 16);
+      subpixel_mean_kernel<<<blocks, 32 * MEAN_WARPS>>>(dim, cdir, dlo, dhi, tol, maxeval, chi, dgrad, dover,
+                                                        dcount + 1, drows);
+      check(cudaGetLastError(), "subpixel_mean_kernel launch");
+    }
   }
   check(cudaMemcpy(rows, drows, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost), "copy rows");
 }
