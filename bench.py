@@ -322,6 +322,90 @@ def subpixel_timing():
             "note": "wall time incl. host<->device copies; 2 pixels per Ex point (set_chi1inv)"}
 
 
+def near2far_setup(engine, n=60, res=20.0, box=(15, 45), nfreq=10, precision=64, steps=40):
+    """The near-to-far workload: a 3-D cell of n^3 cells at resolution res
+    with an Ez pulse at the centre, a closed box of near2far surfaces (the
+    four tangential E and H components on each of its six faces, on their own
+    Yee grids: 24 sheets of 31 x 31 points) and nfreq frequencies, stepped a
+    few steps so the sums are nonzero.  Returns (sim, sheets)."""
+    import numpy as np
+    from meep_gb300 import _lib
+    io = [-n, -n, -n]
+    pml = {(d, sd): (0.5, 1e-15, 1.0) for d in range(3) for sd in range(2)}
+    sim = _lib.Sim(engine, 3, (n, n, n), io, res, pml=pml, precision=precision, components=range(12))
+    src = sim.add_gaussian_src(1.0, 0.5)
+    c = n // 2
+    sim.add_source_points(2, src, [(c * (n + 1) + c) * (n + 1) + c], [1.0])
+    freqs = list(np.linspace(0.8, 1.2, nfreq))
+    sheets = []
+    lo_b, hi_b = box
+    for nd in range(3):
+        fd = [(nd + 1) % 3, (nd + 2) % 3]
+        for k in (lo_b, hi_b):
+            for e in (0, 1):           # E, then H
+                for j in (0, 1):
+                    comp = 3 * e + fd[j]
+                    c0 = 3 * (1 - e) + fd[1 - j]
+                    sgn = (1.0 if j == 0 else -1.0) * (-1.0 if e == 0 else 1.0) * (1.0 if k == hi_b else -1.0)
+                    lo = [lo_b] * 3
+                    hi = [hi_b] * 3
+                    lo[nd] = hi[nd] = k
+                    w = [np.ones(hi[d] - lo[d] + 1) for d in range(3)]
+                    mid = sim.add_dft(comp, lo, hi, w, dV=(1 / res) ** 2, include_weights=True, scale=sgn,
+                                      centered=False, freqs=freqs, decimation=1)
+                    # Yee offset: E_d shifted along d, H_d along the other two
+                    shift = [(1 if d == comp % 3 else 0) if e == 0 else (0 if d == comp % 3 else 1)
+                             for d in range(3)]
+                    is_half = [0.5 * (io[d] + shift[d] + 2 * lo[d]) for d in range(3)]
+                    sheets.append((mid, c0, is_half, [0.0, 0.0, 0.0]))
+    sim.step(steps)
+    return sim, sheets
+
+
+def near2far_points(m=64, z=50.0, half=50.0):
+    import numpy as np
+    ax = np.linspace(-half, half, m)
+    X, Y = np.meshgrid(ax, ax, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), np.full(m * m, z)], axis=1)
+
+
+def near2far_timing():
+    """Near-to-far transform (dft_near2far::get_farfields_array): far fields
+    of 24 sheets (23,064 source points, 10 frequencies) at 64 x 64 points on
+    a plane 50 away, i.e. 944M Green's function evaluations in FP64, on the
+    GPU (mfd_farfield, wall time of the call incl. copies) against the CPU
+    oracle (the reference's loop, all host threads) on 64 of the points; the
+    sample must agree within 1e-11."""
+    import numpy as np
+    from meep_gb300 import _lib, build
+    pts = near2far_points()
+    gpu_sim, sheets = near2far_setup(_lib.Engine())
+    nsrc = len(sheets) * 31 * 31
+    gpu_sim.farfield(sheets, pts[:8])  # warm-up
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ff = gpu_sim.farfield(sheets, pts)
+        times.append(time.perf_counter() - t0)
+    t_gpu = min(times)
+    nf = ff.shape[1]
+    cpu_sim, sheets_c = near2far_setup(_lib.Engine(build.build_oracle()))
+    sample = pts[::64]
+    t0 = time.perf_counter()
+    ffc = cpu_sim.farfield(sheets_c, sample)
+    t_cpu = time.perf_counter() - t0
+    evals_gpu = pts.shape[0] * nf * nsrc
+    evals_cpu = sample.shape[0] * nf * nsrc
+    ref = ff[::64]
+    return {"far_points": int(pts.shape[0]), "freqs": int(nf), "source_points": int(nsrc),
+            "green_evals": int(evals_gpu), "gpu_s": t_gpu, "gpu_gevals_per_s": evals_gpu / t_gpu / 1e9,
+            "cpu_sample_points": int(sample.shape[0]), "cpu_s": t_cpu, "cpu_gevals_per_s": evals_cpu / t_cpu / 1e9,
+            "cpu_threads": cpu_threads(), "gpu_over_cpu": (evals_gpu / t_gpu) / (evals_cpu / t_cpu),
+            "sample_rel_err": float(np.abs(ref - ffc).max() / np.abs(ffc).max()),
+            "note": "FP64 Green's functions (sin/cos, sqrt, divisions) on the CUDA cores; wall time of one "
+                    "mfd_farfield call incl. uploading the points and downloading 4096 x 10 x 6 fields"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,6 +508,10 @@ def main():
         sub = subpixel_timing()
     except Exception as e:
         sub = {"error": str(e)[:200]}
+    try:
+        n2f = near2far_timing()
+    except Exception as e:
+        n2f = {"error": str(e)[:200]}
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
@@ -454,6 +542,7 @@ def main():
         "clocks": clk.summary(r32.get("timed_wall")),
         "adjoint": adj,
         "subpixel_setup": sub,
+        "near2far": n2f,
     }
     print(json.dumps(line))
     if dist is not None:

@@ -167,8 +167,21 @@ public:
     LOOP_OVER_DIRECTIONS(dim, d) t[d] -= a.t[d];
     return *this;
   }
+  // multiplies by 1 / s, as the reference's vec does
+  vec operator/(double s) const {
+    vec r(dim);
+    LOOP_OVER_DIRECTIONS(dim, d) r.t[d] = t[d] * (1.0 / s);
+    return r;
+  }
+  // dot product
+  double operator&(const vec &a) const {
+    double out = 0.0;
+    LOOP_OVER_DIRECTIONS(dim, d) out += t[d] * a.t[d];
+    return out;
+  }
 };
 inline vec zero_vec(ndim di) { return vec(di, 0.0); }
+inline double abs(const vec &v) { return std::sqrt(v & v); }
 
 class ivec {
 public:
@@ -264,6 +277,8 @@ public:
   void set_direction_max(direction d, double v) { max_corner.set_direction(d, v); }
   vec center() const { return (min_corner + max_corner) * 0.5; }
   volume operator+(const vec &a) const { return volume(min_corner + a, max_corner + a); }
+  // smallest volume containing both
+  volume operator|(const volume &a) const;
 };
 
 class grid_volume {
@@ -530,6 +545,8 @@ public:
 };
 
 /* ------------------------------------------------------------ monitors */
+class fields;
+
 class dft_chunk {
 public:
   std::vector<double> omega;
@@ -538,9 +555,15 @@ public:
   std::complex<realnum> *dft;
   dft_chunk *next_in_dft;
   ivec is, ie;
+  ivec shift; // lattice-image shift of the chunk's points
+  int vc;     // equivalent source component (near2far), else c
   int monitor_id;
-  dft_chunk() : c(Ex), N(0), dft(nullptr), next_in_dft(nullptr), monitor_id(-1) {}
+  fields *fld;
+  dft_chunk()
+      : c(Ex), N(0), dft(nullptr), next_in_dft(nullptr), vc(Ex), monitor_id(-1), fld(nullptr) {}
   ~dft_chunk() { delete[] dft; }
+  // multiply the sums of this chunk and the chunks after it (device sums)
+  void scale_dft(std::complex<double> scale);
 };
 
 class volume_list {
@@ -563,6 +586,44 @@ public:
   dft_flux() : E(nullptr), H(nullptr), cE(Ex), cH(Hy), f(nullptr) {}
   double *flux();
 };
+
+/* Near-to-far transform (src/near2far.cpp): DFT chunks of the tangential
+   fields on closed or open surfaces in a homogeneous medium; far fields by
+   the 2-D or 3-D Green's function, evaluated on the GPU. */
+class dft_near2far {
+public:
+  dft_near2far(dft_chunk *F, const double *freq, size_t Nfreq, double eps, double mu, const volume &where,
+               const direction periodic_d[2], const int periodic_n[2], const double periodic_k[2],
+               const double period[2]);
+  // (Ex, Ey, Ez, Hx, Hy, Hz) x Nfreq at x, newly allocated
+  std::complex<double> *farfield(const vec &x, double greencyl_tol = 1e-3);
+  // the same into a caller array of 6 * Nfreq values
+  void farfield_lowlevel(std::complex<double> *EH, const vec &x, double greencyl_tol = 1e-3);
+  // 6 x 2 x N x Nfreq fields on a grid over `where` at `resolution`
+  double *get_farfields_array(const volume &where, int &rank, size_t *dims, size_t &N, double resolution,
+                              double greencyl_tol = 1e-3);
+  // Poynting flux through `where` (normal df) of the far fields
+  double *flux(direction df, const volume &where, double resolution);
+  void scale_dfts(std::complex<double> scale);
+  void remove();
+  // the far fields at many points in one engine call (an extension): out
+  // has npts * Nfreq * 6 values, point-major like farfield's result
+  void farfields_at(const std::vector<vec> &pts, std::complex<double> *out);
+
+  std::vector<double> freq;
+  dft_chunk *F;
+  double eps, mu;
+  volume where;
+  direction periodic_d[2];
+  int periodic_n[2];
+  double periodic_k[2], period[2];
+};
+
+// homogeneous-medium Green's functions (src/near2far.cpp:131-245), on the GPU
+void green3d(std::complex<double> *EH, const vec &x, double freq, double eps, double mu, const vec &x0,
+             component c0, std::complex<double> f0);
+void green2d(std::complex<double> *EH, const vec &x, double freq, double eps, double mu, const vec &x0,
+             component c0, std::complex<double> f0);
 
 class dft_fields {
 public:
@@ -624,6 +685,16 @@ public:
                             double freq_min, double freq_max, int Nfreq,
                             bool use_centered_grid = true, int decimation_factor = 0,
                             bool persist = false);
+
+  dft_near2far add_dft_near2far(const volume_list *where, double freq_min, double freq_max, int Nfreq,
+                                int decimation_factor = 0, int Nperiods = 1);
+  dft_near2far add_dft_near2far(const volume_list *where, const std::vector<double> &freq,
+                                int decimation_factor = 0, int Nperiods = 1);
+  dft_near2far add_dft_near2far(const volume_list *where, const double *freq, size_t Nfreq,
+                                int decimation_factor = 0, int Nperiods = 1);
+  // trace-averaged permittivity / permeability at loc (src/monitor.cpp:172-194)
+  std::complex<double> get_eps(const vec &loc, double frequency = 0) const;
+  std::complex<double> get_mu(const vec &loc, double frequency = 0) const;
 
   std::complex<double> get_field(component c, const vec &loc, bool parallel = true);
   std::complex<double> get_field(component c, const ivec &iloc, bool parallel = true);

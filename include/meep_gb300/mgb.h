@@ -72,6 +72,26 @@ double mgb_last_source_time(const mgb_sim *s);
 int mgb_add_flux(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
                  int *handle);
 int mgb_flux(mgb_sim *s, int handle, double *out);
+/* near-to-far surfaces: regions as for mgb_add_flux; nperiods > 1 sums
+ * lattice images along periodic directions (fields::add_dft_near2far) */
+int mgb_add_near2far(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                     int nperiods, int *handle);
+/* far fields at npts points xyz[3 npts]: out[npts * nfreq * 6 * 2], point
+ * slowest, then frequency, then Ex..Hz, re/im interleaved */
+int mgb_near2far_points(mgb_sim *s, int handle, int npts, const double *xyz, double *out);
+/* get_farfields_array over volume(center, size) at `resolution`: with out
+ * NULL only dims[0..2] (points per direction, 1 for absent ones) and *rank;
+ * else out receives 12 * N * nfreq doubles in the reference's layout
+ * ((component * 2 + re/im) * N + point) * nfreq + frequency */
+int mgb_near2far_array(mgb_sim *s, int handle, const double center[3], const double size[3], double resolution,
+                       double *out, int dims[3], int *rank);
+/* dft_near2far::flux through volume(center, size) with normal `direction` */
+int mgb_near2far_flux(mgb_sim *s, int handle, int direction, const double center[3], const double size[3],
+                      double resolution, double *out);
+/* dft_near2far::scale_dfts */
+int mgb_near2far_scale(mgb_sim *s, int handle, double re, double im);
+/* the homogeneous medium seen by the surfaces */
+int mgb_near2far_medium(mgb_sim *s, int handle, double *eps, double *mu);
 /* DFT fields of ncomp components over volume(center, size) */
 int mgb_add_dft_fields(mgb_sim *s, int ncomp, const int *components, const double center[3],
                        const double size[3], int nfreq, const double *freqs, int yee_grid, int decimation,

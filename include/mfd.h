@@ -125,6 +125,39 @@ int mfd_get_dft(mfd_sim *sim, int id, double *out, size_t *npts, size_t *nfreq);
  * src/dft.cpp:542-556. out has nfreq entries. */
 int mfd_flux(mfd_sim *sim, int npairs, const int *idE, const int *idH, double *out);
 
+/* Multiply the sums of monitor `id` by (s_re + i s_im).  Replaces
+ * dft_chunk::scale_dft src/dft.cpp:402-406 (dft_near2far::scale_dfts
+ * src/near2far.cpp:124-126, dft_flux::scale_dfts). */
+int mfd_scale_dft(mfd_sim *sim, int id, double s_re, double s_im);
+
+/* ---- Near-to-far transform ----
+ * Far fields of equivalent current sheets.  Each of the nsheet monitors
+ * ids[i] holds the DFT of one tangential field on its own Yee grid (centered
+ * = 0) with the sheet's sign and surface weight in its scale and include
+ * weights on (how fields::add_dft_near2far src/near2far.cpp:569-651 adds
+ * them); src_comp[i] is the equivalent current it stands for (mfd component
+ * code of Ex..Ez or Hx..Hz); point k of the monitor box sits at
+ * (is_half[3i+d] + k_d) / a + rshift[3i+d] (the loop-start ivec / 2 of its
+ * first point and the lattice-image shift).  eps, mu: the homogeneous medium.
+ * periodic_dir[j] (0..2, or -1) with periodic_n[j] images on each side,
+ * periodic_k[j] phase per image and period[j] (the Nperiods sum of
+ * add_dft_near2far).  x: nx far points (x, y, z; z ignored in 2-D).  out:
+ * nx * nfreq * 6 complex values (re, im), far point slowest, then frequency,
+ * then Ex, Ey, Ez, Hx, Hy, Hz.  All monitors must have the same frequencies.
+ * 2-D (x, y) and 3-D grids.  Replaces dft_near2far::farfield_lowlevel
+ * src/near2far.cpp:334-378 for a list of far points. */
+int mfd_farfield(mfd_sim *sim, int nsheet, const int *ids, const int *src_comp, const double *is_half,
+                 const double *rshift, double eps, double mu, const int periodic_dir[2], const int periodic_n[2],
+                 const double periodic_k[2], const double period[2], int64_t nx, const double *x, double *out);
+
+/* The homogeneous-medium Green's function for n point pairs: out[12 i ..]
+ * = the 6 complex fields (Ex..Hz, re/im) at x[3i..] of a current f0 of
+ * component c0 (mfd code of Ex..Ez, Hx..Hz) at x0[3i..].  dim 3: green3d
+ * src/near2far.cpp:131-181; dim 2: green2d src/near2far.cpp:201-245 (x, y
+ * only; c0 of any direction).  No mfd_sim needed. */
+int mfd_green(int dim, int c0, double freq, double eps, double mu, double f0_re, double f0_im, int64_t n,
+              const double *x, const double *x0, double *out);
+
 /* ---- Differentiation: reverse-time adjoint of the leapfrog update ----
  * Design = the inverse-permittivity diagonal chi1inv of E components `comps`
  * over the point box lo..hi (inclusive, component-grid indices).

@@ -84,6 +84,11 @@ SIGNATURES = [
     ("mfd_get_field_im", C.c_int, [_P, C.c_int, _DP]),
     ("mfd_subpixel_rows", C.c_int, [C.c_int, C.c_int, C.c_int64, _DP, _DP, C.c_double, C.c_int, C.c_int,
                                     C.POINTER(mfd_object), C.c_double, _DP]),
+    ("mfd_scale_dft", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
+    ("mfd_farfield", C.c_int, [_P, C.c_int, _IP, _IP, _DP, _DP, C.c_double, C.c_double, _IP, _IP, _DP, _DP,
+                               C.c_int64, _DP, _DP]),
+    ("mfd_green", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                            C.c_int64, _DP, _DP, _DP]),
     ("mfd_flux_noalloc", C.c_int, [_P, _P, C.c_int64, C.c_int, _P, _P]),
     ("mfd_noalloc_last_error", C.c_char_p, []),
     ("mfd_kernel_launches", C.c_int64, [_P]),
@@ -141,6 +146,18 @@ class Engine:
         self.check(self.lib.mfd_subpixel_rows(dim, cdir, lo.shape[0], _dptr(lo), _dptr(hi), tol, maxeval,
                                               len(objects), objs, eps_default, _dptr(rows)))
         return rows
+
+
+    def green(self, dim, c0, freq, eps, mu, x, x0, f0=1.0 + 0.0j):
+        """Homogeneous-medium Green's function (mfd_green) for the point pairs
+        x[i], x0[i] (arrays n x 3) of a current f0 of component c0 (0..2 Ex..Ez,
+        3..5 Hx..Hz): (n, 6) complex fields Ex, Ey, Ez, Hx, Hy, Hz."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        x0 = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((x.shape[0], 6, 2))
+        self.check(self.lib.mfd_green(dim, c0, freq, eps, mu, complex(f0).real, complex(f0).imag, x.shape[0],
+                                      _dptr(x), _dptr(x0), _dptr(out)))
+        return out[..., 0] + 1j * out[..., 1]
 
 
 def _dptr(a):
@@ -287,6 +304,33 @@ class Sim:
         out = np.zeros(nfreq)
         self.eng.check(self.eng.lib.mfd_flux(self.h, len(idE), idE, idH, _dptr(out)))
         return out
+
+    def scale_dft(self, mid, s):
+        s = complex(s)
+        self.eng.check(self.eng.lib.mfd_scale_dft(self.h, mid, s.real, s.imag))
+
+    def farfield(self, sheets, x, eps=1.0, mu=1.0, periodic=None):
+        """Near-to-far transform (mfd_farfield).  sheets: list of (monitor id,
+        equivalent current component 0..5, is_half[3], rshift[3]); x: far points
+        (n x 3); periodic: up to two (direction, images per side, phase per
+        image, period).  Returns (n, nfreq, 6) complex Ex..Hz."""
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1, 3))
+        ids = (C.c_int * len(sheets))(*[int(s[0]) for s in sheets])
+        c0 = (C.c_int * len(sheets))(*[int(s[1]) for s in sheets])
+        ish = np.ascontiguousarray([v for s in sheets for v in s[2]], dtype=np.float64)
+        rsh = np.ascontiguousarray([v for s in sheets for v in s[3]], dtype=np.float64)
+        per = list(periodic or []) + [(-1, 0, 0.0, 0.0)] * 2
+        pd = (C.c_int * 2)(*[int(per[i][0]) for i in range(2)])
+        pn = (C.c_int * 2)(*[int(per[i][1]) for i in range(2)])
+        pk = np.ascontiguousarray([per[i][2] for i in range(2)], dtype=np.float64)
+        pp = np.ascontiguousarray([per[i][3] for i in range(2)], dtype=np.float64)
+        npts = C.c_size_t()
+        nf = C.c_size_t()
+        self.eng.check(self.eng.lib.mfd_get_dft(self.h, int(sheets[0][0]), None, C.byref(npts), C.byref(nf)))
+        out = np.zeros((x.shape[0], nf.value, 6, 2))
+        self.eng.check(self.eng.lib.mfd_farfield(self.h, len(sheets), ids, c0, _dptr(ish), _dptr(rsh), eps, mu, pd,
+                                                 pn, _dptr(pk), _dptr(pp), x.shape[0], _dptr(x), _dptr(out)))
+        return out[..., 0] + 1j * out[..., 1]
 
     def design(self, comps, lo, hi):
         """Declare the design: chi1inv of E components `comps` over the point

@@ -74,6 +74,8 @@ def build_engine(force=False, verbose=False):
                              "-o", os.path.join(objdir, "mfd_noalloc.o")])
     jobs.append(cu_common + ["--fmad=false", "-c", os.path.join(CSRC, "mfd_subpixel.cu"),
                              "-o", os.path.join(objdir, "mfd_subpixel.o")])
+    jobs.append(cu_common + ["-c", os.path.join(CSRC, "mfd_near2far.cu"),
+                             "-o", os.path.join(objdir, "mfd_near2far.o")])
     for src in ("mfd_plan.cpp", "mfd_capi.cpp", "sphere_quadrature.cpp"):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"] + INC +
                     ["-c", os.path.join(CSRC, src), "-o", os.path.join(objdir, src.replace(".cpp", ".o"))])
@@ -83,7 +85,7 @@ def build_engine(force=False, verbose=False):
         for o in outs:
             sys.stdout.write(o)
     objs = [os.path.join(objdir, f) for f in ("mfd_cuda_f64.o", "mfd_cuda_f32.o", "mfd_noalloc.o",
-                                               "mfd_subpixel.o", "mfd_plan.o", "mfd_capi.o",
+                                               "mfd_subpixel.o", "mfd_near2far.o", "mfd_plan.o", "mfd_capi.o",
                                                "sphere_quadrature.o")]
     _run([nvcc] + ARCH + ["-shared", "-o", so] + objs + ["-lcudart"])
     api = [os.path.join(CSRC, "meep_api.cpp"), os.path.join(CSRC, "meep_pyshim.cpp")]

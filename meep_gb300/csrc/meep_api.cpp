@@ -1033,7 +1033,7 @@ static int auto_decimation(fields &f, const double *freq, size_t Nfreq) {
 static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const double *freq,
                               size_t Nfreq, bool include_dV_and_interp_weights,
                               std::complex<double> stored_weight, dft_chunk *next,
-                              bool use_centered_grid, int decimation_factor) {
+                              bool use_centered_grid, int decimation_factor, int vc = -1) {
   fields::impl &I = *f.d;
   if (component_direction(c) > Z) return next;
   if (!I.components) meep::abort("allocate field components (by adding sources) before adding dft objects");
@@ -1072,9 +1072,12 @@ static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const
                   scale.imag(), use_centered_grid ? 1 : 0, Nfreq, freq, decimation_factor, &id));
   std::unique_ptr<dft_chunk> ch(new dft_chunk);
   ch->c = c;
+  ch->vc = vc < 0 ? int(c) : vc;
   ch->monitor_id = id;
+  ch->fld = &f;
   ch->is = L.is;
   ch->ie = L.ie;
+  ch->shift = img.shift;
   ch->omega.resize(Nfreq);
   for (size_t i = 0; i < Nfreq; i++)
     ch->omega[i] = 2 * pi * freq[i];
@@ -1346,6 +1349,329 @@ std::complex<double> fields::get_field(component c, const vec &loc, bool paralle
   for (int argh = 0; argh < 8 && w[argh]; argh++)
     res += w[argh] * get_field(c, ilocs[argh], false);
   return res;
+}
+
+/* ------------------------------------------------------- near-to-far */
+volume volume::operator|(const volume &a) const {
+  vec lo(dim), hi(dim);
+  LOOP_OVER_DIRECTIONS(dim, dd) {
+    lo.set_direction(dd, std::min(in_direction_min(dd), a.in_direction_min(dd)));
+    hi.set_direction(dd, std::max(in_direction_max(dd), a.in_direction_max(dd)));
+  }
+  return volume(lo, hi);
+}
+
+// volume::normal_direction (src/vec.cpp:227-262): the one empty direction
+static direction normal_direction(const volume &v) {
+  direction d = NO_DIRECTION;
+  switch (v.dim) {
+    case D1: d = Z; break;
+    case D2:
+      if (v.in_direction(X) == 0 && v.in_direction(Y) > 0) d = X;
+      else if (v.in_direction(X) > 0 && v.in_direction(Y) == 0) d = Y;
+      break;
+    case D3: {
+      const bool zx = v.in_direction(X) == 0, zy = v.in_direction(Y) == 0, zz = v.in_direction(Z) == 0;
+      if (zx && !zy && !zz) d = X;
+      else if (!zx && zy && !zz) d = Y;
+      else if (!zx && !zy && zz) d = Z;
+      break;
+    }
+    default: break;
+  }
+  return d;
+}
+
+void dft_chunk::scale_dft(std::complex<double> scale) {
+  for (dft_chunk *ch = this; ch; ch = ch->next_in_dft) {
+    if (ch->fld && ch->fld->d->sim) chk(mfd_scale_dft(ch->fld->d->sim, ch->monitor_id, scale.real(), scale.imag()));
+    for (size_t i = 0; i < ch->N * ch->omega.size(); ++i)
+      ch->dft[i] *= scale;
+  }
+}
+
+// fields::get_chi1inv(c, d, ivec) (src/monitor.cpp:135-154): vacuum outside
+// the cell
+static std::complex<double> field_chi1inv(const fields &f, component c, direction dd, const ivec &iloc) {
+  if (!f.gv.owns(iloc)) return dd == component_direction(c) ? 1.0 : 0.0;
+  return f.s->get_chi1inv(c, dd, iloc);
+}
+
+// fields::get_eps / get_mu (src/monitor.cpp:172-194): n / sum over the
+// grid's E (H) components of the interpolated diagonal chi1inv
+static std::complex<double> trace_average(const fields &f, bool electric, const vec &loc) {
+  std::complex<double> tr(0.0, 0.0);
+  int nc = 0;
+  const component cs[3] = {electric ? Ex : Hx, electric ? Ey : Hy, electric ? Ez : Hz};
+  for (component c : cs) {
+    if (!f.gv.has_field(c)) continue;
+    ivec ilocs[8];
+    double w[8];
+    std::complex<double> res(0.0, 0.0);
+    interpolate(f.gv, c, loc, ilocs, w);
+    for (int k = 0; k < 8 && w[k] != 0; k++)
+      res += w[k] * field_chi1inv(f, c, component_direction(c), ilocs[k]);
+    tr += res;
+    ++nc;
+  }
+  return std::complex<double>(nc, 0) / tr;
+}
+
+std::complex<double> fields::get_eps(const vec &loc, double frequency) const {
+  if (frequency != 0) meep::abort("frequency-dependent eps is not supported by the GB300 engine");
+  return trace_average(*this, true, loc);
+}
+
+std::complex<double> fields::get_mu(const vec &loc, double frequency) const {
+  if (frequency != 0) meep::abort("frequency-dependent mu is not supported by the GB300 engine");
+  return trace_average(*this, false, loc);
+}
+
+static bool approxeq(double a, double b) { return std::fabs(a - b) < 0.5e-11 * (std::fabs(a) + std::fabs(b)); }
+
+// fields::add_dft_near2far (src/near2far.cpp:569-651): per surface, the two
+// tangential E and H components as DFT chunks on their own Yee grids, each
+// standing for the equivalent current n x H (electric) or -n x E (magnetic)
+// of the perpendicular tangential component, with the sign of n x c
+dft_near2far fields::add_dft_near2far(const volume_list *where, const double *freq, size_t Nfreq,
+                                      int decimation_factor, int Nperiods) {
+  dft_chunk *F = nullptr;
+  double eps = 0, mu = 0;
+  volume everywhere = where->v;
+  direction periodic_d[2] = {NO_DIRECTION, NO_DIRECTION};
+  int periodic_n[2] = {0, 0};
+  double periodic_k[2] = {0, 0}, period[2] = {0, 0};
+  for (const volume_list *w = where; w; w = w->next) {
+    everywhere = everywhere | where->v; // (the reference unions the first surface with itself)
+    direction nd = w->c >= Sx ? component_direction(derived_component(w->c)) : component_direction(component(w->c));
+    if (nd == NO_DIRECTION) nd = normal_direction(w->v);
+    if (nd == NO_DIRECTION) meep::abort("unknown dft_near2far normal");
+    const double weps = get_eps(w->v.center()).real();
+    const double wmu = get_mu(w->v.center()).real();
+    if (w != where && !(approxeq(eps, weps) && approxeq(mu, wmu)))
+      meep::abort("dft_near2far requires surfaces in a homogeneous medium");
+    eps = weps;
+    mu = wmu;
+    // transverse directions in cyclic order (sign s below)
+    direction fd[2];
+    switch (nd) {
+      case X: fd[0] = Y, fd[1] = Z; break;
+      case Y: fd[0] = Z, fd[1] = X; break;
+      case Z: fd[0] = X, fd[1] = Y; break;
+      default: meep::abort("invalid normal direction in dft_near2far!");
+    }
+    if (Nperiods > 1) {
+      for (int i = 0; i < 2; ++i) {
+        const double user_width = user_volume.num_direction(fd[i]) / a;
+        const bool has = gv.dim == D3 || (gv.dim == D2 && fd[i] != Z);
+        if (has && d->periodic[fd[i]] && float(w->v.in_direction(fd[i])) >= float(user_width)) {
+          periodic_d[i] = fd[i];
+          periodic_n[i] = Nperiods;
+          period[i] = user_width;
+          periodic_k[i] = 2 * pi * d->kvec[fd[i]] * period[i];
+        }
+      }
+    }
+    for (int i = 0; i < 2; ++i) {   // E or H
+      for (int j = 0; j < 2; ++j) { // first or second transverse component
+        const component c = direction_component(i == 0 ? Ex : Hx, fd[j]);
+        const component c0 = direction_component(i == 0 ? Hx : Ex, fd[1 - j]);
+        double sgn = j == 0 ? 1 : -1;
+        if (is_electric(c)) sgn = -sgn;
+        F = add_dft_one(*this, c, w->v, freq, Nfreq, true, sgn * w->weight, F, false, decimation_factor, int(c0));
+      }
+    }
+  }
+  return dft_near2far(F, freq, Nfreq, eps, mu, everywhere, periodic_d, periodic_n, periodic_k, period);
+}
+
+dft_near2far fields::add_dft_near2far(const volume_list *where, double freq_min, double freq_max, int Nfreq,
+                                      int decimation_factor, int Nperiods) {
+  std::vector<double> fr = linspace(freq_min, freq_max, Nfreq);
+  return add_dft_near2far(where, fr.data(), fr.size(), decimation_factor, Nperiods);
+}
+
+dft_near2far fields::add_dft_near2far(const volume_list *where, const std::vector<double> &freq,
+                                      int decimation_factor, int Nperiods) {
+  return add_dft_near2far(where, freq.data(), freq.size(), decimation_factor, Nperiods);
+}
+
+dft_near2far::dft_near2far(dft_chunk *F_, const double *freq_, size_t Nfreq, double eps_, double mu_,
+                           const volume &where_, const direction periodic_d_[2], const int periodic_n_[2],
+                           const double periodic_k_[2], const double period_[2])
+    : freq(freq_, freq_ + Nfreq), F(F_), eps(eps_), mu(mu_), where(where_) {
+  for (int i = 0; i < 2; ++i) {
+    periodic_d[i] = periodic_d_[i];
+    periodic_n[i] = periodic_n_[i];
+    periodic_k[i] = periodic_k_[i];
+    period[i] = period_[i];
+  }
+}
+
+void dft_near2far::scale_dfts(std::complex<double> scale) {
+  if (F) F->scale_dft(scale);
+}
+
+void dft_near2far::remove() {
+  // the chunks stay owned by their fields (and their device sums allocated);
+  // the list is only detached
+  F = nullptr;
+}
+
+void dft_near2far::farfields_at(const std::vector<vec> &pts, std::complex<double> *out) {
+  const size_t Nfreq = freq.size();
+  if (pts.empty() || Nfreq == 0) return;
+  if (!F) {
+    for (size_t i = 0; i < pts.size() * 6 * Nfreq; i++)
+      out[i] = 0.0;
+    return;
+  }
+  fields &f = *F->fld;
+  std::vector<int> ids, c0;
+  std::vector<double> is_half, rshift;
+  for (dft_chunk *ch = F; ch; ch = ch->next_in_dft) {
+    ids.push_back(ch->monitor_id);
+    c0.push_back(mfd_comp(component(ch->vc)));
+    if (ch->omega.size() != Nfreq) meep::abort("near2far chunk with a different number of frequencies");
+    const vec rs = ch->shift * (0.5 * f.gv.inva);
+    for (int q = 0; q < 3; q++) {
+      const direction dd = direction(q);
+      const bool has = f.gv.dim == D3 || (f.gv.dim == D2 && dd != Z);
+      is_half.push_back(has ? 0.5 * ch->is.in_direction(dd) : 0.0);
+      rshift.push_back(has ? rs.in_direction(dd) : 0.0);
+    }
+  }
+  std::vector<double> xs(3 * pts.size());
+  for (size_t k = 0; k < pts.size(); k++) {
+    if (pts[k].dim != f.gv.dim) meep::abort("far-field point dimensions differ from the grid's");
+    xs[3 * k] = pts[k].x();
+    xs[3 * k + 1] = pts[k].y();
+    xs[3 * k + 2] = pts[k].dim == D3 ? pts[k].z() : 0.0;
+  }
+  int pd[2], pn[2];
+  for (int i = 0; i < 2; i++) {
+    pd[i] = periodic_d[i] == NO_DIRECTION ? -1 : int(periodic_d[i]);
+    pn[i] = periodic_d[i] == NO_DIRECTION ? 0 : periodic_n[i];
+  }
+  chk(mfd_farfield(f.d->sim, (int)ids.size(), ids.data(), c0.data(), is_half.data(), rshift.data(), eps, mu, pd, pn,
+                   periodic_k, period, (int64_t)pts.size(), xs.data(), reinterpret_cast<double *>(out)));
+}
+
+void dft_near2far::farfield_lowlevel(std::complex<double> *EH, const vec &x, double greencyl_tol) {
+  (void)greencyl_tol;
+  if (x.dim != D3 && x.dim != D2) meep::abort("only 2d or 3d far-field computation is supported");
+  farfields_at(std::vector<vec>(1, x), EH);
+}
+
+std::complex<double> *dft_near2far::farfield(const vec &x, double greencyl_tol) {
+  std::complex<double> *EH = new std::complex<double>[6 * freq.size()];
+  farfield_lowlevel(EH, x, greencyl_tol);
+  return EH;
+}
+
+// dft_near2far::get_farfields_array (src/near2far.cpp:392-467): the grid of
+// far points over `where`, all evaluated in one engine call
+double *dft_near2far::get_farfields_array(const volume &where, int &rank, size_t *dims, size_t &N, double resolution,
+                                          double greencyl_tol) {
+  (void)greencyl_tol;
+  double dx[3] = {0, 0, 0};
+  direction dirs[3] = {X, Y, Z};
+  rank = 0;
+  N = dims[0] = dims[1] = dims[2] = 1;
+  LOOP_OVER_DIRECTIONS(where.dim, dd) {
+    dims[rank] = int(std::floor(where.in_direction(dd) * resolution));
+    if (dims[rank] <= 1) dims[rank] = 1;
+    else dx[rank] = where.in_direction(dd) / (dims[rank] - 1);
+    N *= dims[rank];
+    dirs[rank++] = dd;
+  }
+  const size_t Nfreq = freq.size();
+  if (N * Nfreq < 1) return NULL;
+  std::vector<vec> pts;
+  pts.reserve(N);
+  vec x(where.dim);
+  for (size_t i0 = 0; i0 < dims[0]; ++i0) {
+    x.set_direction(dirs[0], where.in_direction_min(dirs[0]) + i0 * dx[0]);
+    for (size_t i1 = 0; i1 < dims[1]; ++i1) {
+      x.set_direction(dirs[1], where.in_direction_min(dirs[1]) + i1 * dx[1]);
+      for (size_t i2 = 0; i2 < dims[2]; ++i2) {
+        x.set_direction(dirs[2], where.in_direction_min(dirs[2]) + i2 * dx[2]);
+        pts.push_back(x);
+      }
+    }
+  }
+  std::vector<std::complex<double>> EH1(pts.size() * 6 * Nfreq);
+  farfields_at(pts, EH1.data());
+  double *EH = new double[6 * 2 * N * Nfreq];
+  for (size_t idx = 0; idx < N; ++idx)
+    for (size_t i = 0; i < Nfreq; ++i)
+      for (int k = 0; k < 6; ++k) {
+        EH[((k * 2 + 0) * N + idx) * Nfreq + i] = EH1[(idx * Nfreq + i) * 6 + k].real();
+        EH[((k * 2 + 1) * N + idx) * Nfreq + i] = EH1[(idx * Nfreq + i) * 6 + k].imag();
+      }
+  int ireduced = 0;
+  for (int i = 0; i < rank; ++i)
+    if (dims[i] > 1) dims[ireduced++] = dims[i];
+  rank = ireduced;
+  return EH;
+}
+
+// dft_near2far::flux (src/near2far.cpp:517-567): Re(E x H*) . n summed over
+// the far-field grid times its area element
+double *dft_near2far::flux(direction df, const volume &where, double resolution) {
+  if (df > Z || (where.dim == D2 && df == Z) || (where.dim == D1 && df != Z))
+    meep::abort("cannot get flux for near2far: co-ordinate mismatch");
+  size_t dims[4] = {1, 1, 1, 1};
+  int rank = 0;
+  size_t N = 1;
+  double *EH = get_farfields_array(where, rank, dims, N, resolution);
+  const size_t Nfreq = freq.size();
+  double *F = new double[Nfreq];
+  for (size_t i = 0; i < Nfreq; ++i)
+    F[i] = 0;
+  std::complex<double> ff[6], cE[2], cH[2];
+  for (size_t idx = 0; idx < N; ++idx) {
+    for (size_t i = 0; i < Nfreq; ++i) {
+      for (int k = 0; k < 6; ++k)
+        ff[k] = std::complex<double>(EH[((k * 2 + 0) * N + idx) * Nfreq + i], EH[((k * 2 + 1) * N + idx) * Nfreq + i]);
+      switch (df) {
+        case X: cE[0] = ff[1], cE[1] = ff[2], cH[0] = ff[5], cH[1] = ff[4]; break;
+        case Y: cE[0] = ff[2], cE[1] = ff[0], cH[0] = ff[3], cH[1] = ff[5]; break;
+        default: cE[0] = ff[0], cE[1] = ff[1], cH[0] = ff[4], cH[1] = ff[3]; break;
+      }
+      for (int j = 0; j < 2; ++j)
+        F[i] += real(cE[j] * conj(cH[j])) * (1 - 2 * j);
+    }
+  }
+  double dV = 1;
+  LOOP_OVER_DIRECTIONS(where.dim, dd) {
+    const int n = int(std::floor(where.in_direction(dd) * resolution));
+    if (n > 1) dV *= where.in_direction(dd) / (n - 1);
+  }
+  for (size_t i = 0; i < Nfreq; ++i)
+    F[i] *= dV;
+  delete[] EH;
+  return F;
+}
+
+static void green_call(int dim, std::complex<double> *EH, const vec &x, double freq, double eps, double mu,
+                       const vec &x0, component c0, std::complex<double> f0) {
+  const double xa[3] = {x.x(), x.y(), dim == 3 ? x.z() : 0.0};
+  const double xb[3] = {x0.x(), x0.y(), dim == 3 ? x0.z() : 0.0};
+  if (!is_electric(c0) && !is_magnetic(c0)) meep::abort("unrecognized source type");
+  chk(mfd_green(dim, mfd_comp(c0), freq, eps, mu, f0.real(), f0.imag(), 1, xa, xb, reinterpret_cast<double *>(EH)));
+}
+
+void green3d(std::complex<double> *EH, const vec &x, double freq, double eps, double mu, const vec &x0,
+             component c0, std::complex<double> f0) {
+  if (x.dim != D3) meep::abort("wrong dimensionality in green3d");
+  green_call(3, EH, x, freq, eps, mu, x0, c0, f0);
+}
+
+void green2d(std::complex<double> *EH, const vec &x, double freq, double eps, double mu, const vec &x0,
+             component c0, std::complex<double> f0) {
+  if (x.dim != D2) meep::abort("wrong dimensionality in green2d");
+  green_call(2, EH, x, freq, eps, mu, x0, c0, f0);
 }
 
 } // namespace meep

@@ -164,7 +164,33 @@ struct mgb_sim {
   std::vector<std::unique_ptr<src_time>> srcs;
   std::vector<dft_flux> fluxes;
   std::vector<dft_fields> dfts;
+  std::vector<dft_near2far> n2fs;
 };
+
+// rows of (center[3], size[3], direction or -1, weight) as a volume_list;
+// regions are prepended, as the Python layer builds its volume_list
+static std::unique_ptr<volume_list> region_list(mgb_sim *s, int nreg, const double *regions) {
+  std::unique_ptr<volume_list> head;
+  for (int q = 0; q < nreg; q++) {
+    const double *r = regions + 8 * q;
+    volume v = mkvol(s->dim, r, r + 3);
+    int d = (int)r[6];
+    if (d < 0) {
+      // fields::normal_direction: the one present direction of zero extent
+      int nzero = 0;
+      for (int dd = 0; dd < 3; dd++) {
+        if ((s->dim == 1 && dd != 2) || (s->dim == 2 && dd == 2)) continue;
+        if (r[3 + dd] == 0.0) {
+          d = dd;
+          nzero++;
+        }
+      }
+      if (nzero != 1) throw std::runtime_error("meep: flux region needs a normal direction");
+    }
+    head.reset(new volume_list(v, (int)direction_component(Sx, (direction)d), r[7], head.release()));
+  }
+  return head;
+}
 
 extern "C" {
 
@@ -245,26 +271,7 @@ int mgb_add_flux(mgb_sim *s, int nreg, const double *regions, int nfreq, const d
                  int *handle) {
   try {
     if (!s || !regions || !freqs || !handle || nreg < 1) throw std::runtime_error("null argument");
-    // regions are prepended, as the Python layer builds its volume_list
-    std::unique_ptr<volume_list> head;
-    for (int q = 0; q < nreg; q++) {
-      const double *r = regions + 8 * q;
-      volume v = mkvol(s->dim, r, r + 3);
-      int d = (int)r[6];
-      if (d < 0) {
-        // fields::normal_direction: the one present direction of zero extent
-        int nzero = 0;
-        for (int dd = 0; dd < 3; dd++) {
-          if ((s->dim == 1 && dd != 2) || (s->dim == 2 && dd == 2)) continue;
-          if (r[3 + dd] == 0.0) {
-            d = dd;
-            nzero++;
-          }
-        }
-        if (nzero != 1) throw std::runtime_error("meep: flux region needs a normal direction");
-      }
-      head.reset(new volume_list(v, (int)direction_component(Sx, (direction)d), r[7], head.release()));
-    }
+    std::unique_ptr<volume_list> head = region_list(s, nreg, regions);
     s->fluxes.push_back(s->f->add_dft_flux(head.get(), freqs, (size_t)nfreq, true, true, decimation));
     *handle = (int)s->fluxes.size() - 1;
     return 0;
@@ -280,6 +287,116 @@ int mgb_flux(mgb_sim *s, int handle, double *out) {
     for (size_t i = 0; i < s->fluxes[handle].freq.size(); i++)
       out[i] = F[i];
     delete[] F;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+static dft_near2far &n2f_of(mgb_sim *s, int handle) {
+  if (!s || handle < 0 || handle >= (int)s->n2fs.size()) throw std::runtime_error("bad near2far handle");
+  return s->n2fs[handle];
+}
+
+static vec point_of(int dim, const double *p) {
+  if (dim == 1) return vec(p[2]);
+  if (dim == 2) return vec(p[0], p[1]);
+  return vec(p[0], p[1], p[2]);
+}
+
+int mgb_add_near2far(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                     int nperiods, int *handle) {
+  try {
+    if (!s || !regions || !freqs || !handle || nreg < 1) throw std::runtime_error("null argument");
+    std::unique_ptr<volume_list> head = region_list(s, nreg, regions);
+    s->n2fs.push_back(s->f->add_dft_near2far(head.get(), freqs, (size_t)nfreq, decimation, nperiods));
+    *handle = (int)s->n2fs.size() - 1;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_near2far_points(mgb_sim *s, int handle, int npts, const double *xyz, double *out) {
+  try {
+    dft_near2far &n = n2f_of(s, handle);
+    if (npts < 0 || (npts > 0 && (!xyz || !out))) throw std::runtime_error("null argument");
+    std::vector<vec> pts;
+    for (int i = 0; i < npts; i++)
+      pts.push_back(point_of(s->dim, xyz + 3 * i));
+    n.farfields_at(pts, reinterpret_cast<std::complex<double> *>(out));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_near2far_array(mgb_sim *s, int handle, const double center[3], const double size[3], double resolution,
+                       double *out, int dims[3], int *rank) {
+  try {
+    dft_near2far &n = n2f_of(s, handle);
+    if (!center || !size || !dims || !rank) throw std::runtime_error("null argument");
+    const volume v = mkvol(s->dim, center, size);
+    int r = 0;
+    size_t dd[3] = {1, 1, 1}, N = 1;
+    if (!out) {
+      // the grid only (get_farfields_array's sizing, no evaluation)
+      LOOP_OVER_DIRECTIONS(v.dim, q) {
+        size_t k = (size_t)int(std::floor(v.in_direction(q) * resolution));
+        dd[r++] = k <= 1 ? 1 : k;
+      }
+    }
+    else {
+      double *EH = n.get_farfields_array(v, r, dd, N, resolution);
+      if (EH) {
+        std::copy(EH, EH + 12 * N * n.freq.size(), out);
+        delete[] EH;
+      }
+      // get_farfields_array collapsed singleton directions; report the grid
+      r = 0;
+      dd[0] = dd[1] = dd[2] = 1;
+      LOOP_OVER_DIRECTIONS(v.dim, q) {
+        size_t k = (size_t)int(std::floor(v.in_direction(q) * resolution));
+        dd[r++] = k <= 1 ? 1 : k;
+      }
+    }
+    for (int q = 0; q < 3; q++)
+      dims[q] = (int)dd[q];
+    *rank = r;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_near2far_flux(mgb_sim *s, int handle, int direction, const double center[3], const double size[3],
+                      double resolution, double *out) {
+  try {
+    dft_near2far &n = n2f_of(s, handle);
+    if (!center || !size || !out || direction < 0 || direction > 2) throw std::runtime_error("bad argument");
+    double *F = n.flux(meep::direction(direction), mkvol(s->dim, center, size), resolution);
+    std::copy(F, F + n.freq.size(), out);
+    delete[] F;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_near2far_scale(mgb_sim *s, int handle, double re, double im) {
+  try {
+    n2f_of(s, handle).scale_dfts(std::complex<double>(re, im));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_near2far_medium(mgb_sim *s, int handle, double *eps, double *mu) {
+  try {
+    dft_near2far &n = n2f_of(s, handle);
+    if (eps) *eps = n.eps;
+    if (mu) *mu = n.mu;
     return 0;
   } catch (const std::exception &e) {
     return fail(e);

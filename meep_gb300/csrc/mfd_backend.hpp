@@ -18,6 +18,27 @@ struct SrcStepValues {
   std::complex<double> dip_e; // dipole  at (t+1)*dt        (integrated E sources)
 };
 
+// Near-to-far transform: one equivalent current sheet per DFT monitor.  The
+// monitor holds the DFT of one tangential field on its own Yee grid with the
+// sheet's sign, surface weight and dV folded in (fields::add_dft_near2far,
+// src/near2far.cpp:569-651); point k of the monitor box sits at
+// (is_half + k) * inva + rshift (IVEC_LOOP_LOC plus the lattice-image shift).
+struct N2FSheet {
+  int id;            // DFT monitor
+  int c0;            // equivalent current: 0..2 electric x, y, z; 3..5 magnetic
+  double is_half[3]; // half the loop-start ivec of the monitor's first point
+  double rshift[3];  // lattice-image shift of the points
+};
+struct N2FSpec {
+  int dim;         // 2 (green2d) or 3 (green3d)
+  double eps, mu;  // homogeneous medium around the sheets
+  double inva;     // grid spacing 1/a
+  int pdir[2];     // periodic image directions, -1 none
+  int pn[2];       // images -pn..pn along each
+  double pk[2];    // Bloch phase per image
+  double period[2];
+};
+
 class Backend {
 public:
   virtual ~Backend() {}
@@ -32,6 +53,13 @@ public:
   virtual void get_field_im(Plan &p, int c, double *out_dense) = 0;
   virtual void get_dft(Plan &p, int id, double *out) = 0;
   virtual void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) = 0;
+  // multiply the DFT sums of monitor id by s (dft_chunk::scale_dft)
+  virtual void scale_dft(Plan &p, int id, std::complex<double> s) = 0;
+  // far fields (6 complex values per far point and frequency, point-major,
+  // then frequency, then Ex..Hz, re/im interleaved) of the sheets at the nx
+  // points x (3 coordinates each)
+  virtual void farfield(Plan &p, const N2FSpec &s, const std::vector<N2FSheet> &sheets, int64_t nx, const double *x,
+                        double *out) = 0;
   virtual void synchronize() {}
   virtual long long launches() const { return 0; }
   virtual double last_step_ms() const { return 0.0; }
@@ -70,5 +98,8 @@ Backend *make_backend(const Plan &p);
 // mfd_subpixel_rows (arguments checked by the C ABI)
 void subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const double *hi, double tol, int maxeval,
                    int nobj, const mfd_object *objs, double eps_default, double *rows);
+// mfd_green (arguments checked by the C ABI)
+void green_eval(int dim, int c0, double freq, double eps, double mu, double f0re, double f0im, int64_t n,
+                const double *x, const double *x0, double *out);
 
 } // namespace mfd

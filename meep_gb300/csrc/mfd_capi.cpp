@@ -437,6 +437,75 @@ int mfd_flux(mfd_sim *s, int npairs, const int *idE, const int *idH, double *out
   MFD_CATCH
 }
 
+int mfd_scale_dft(mfd_sim *s, int id, double s_re, double s_im) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  Plan &p = *s->plan;
+  need(id >= 0 && id < (int)p.monitors.size(), "unknown monitor id");
+  if (s->setup_done) s->be->scale_dft(p, id, {s_re, s_im});
+  MFD_CATCH
+}
+
+int mfd_farfield(mfd_sim *s, int nsheet, const int *ids, const int *src_comp, const double *is_half,
+                 const double *rshift, double eps, double mu, const int periodic_dir[2], const int periodic_n[2],
+                 const double periodic_k[2], const double period[2], int64_t nx, const double *x, double *out) {
+  MFD_TRY
+  need(s && s->plan, "null simulation handle");
+  Plan &p = *s->plan;
+  need(nsheet >= 1 && ids && src_comp && is_half && rshift, "near2far needs at least one monitor");
+  need(nx >= 0 && (nx == 0 || (x && out)), "null far-point or output array");
+  need(periodic_dir && periodic_n && periodic_k && period, "null periodicity argument");
+  N2FSpec sp{};
+  if (p.present[0] && p.present[1] && p.present[2]) sp.dim = 3;
+  else if (p.present[0] && p.present[1] && !p.present[2]) sp.dim = 2;
+  else throw Error("meep: only 2d or 3d far-field computation is supported");
+  need(eps > 0 && mu > 0, "near2far medium must have eps > 0 and mu > 0");
+  sp.eps = eps;
+  sp.mu = mu;
+  sp.inva = p.inva;
+  for (int j = 0; j < 2; j++) {
+    need(periodic_dir[j] >= -1 && periodic_dir[j] < 3, "periodic direction out of range");
+    need(periodic_n[j] >= 0 && (periodic_dir[j] >= 0 || periodic_n[j] == 0), "bad periodic image count");
+    sp.pdir[j] = periodic_dir[j];
+    sp.pn[j] = periodic_n[j];
+    sp.pk[j] = periodic_k[j];
+    sp.period[j] = period[j];
+  }
+  std::vector<N2FSheet> sh(nsheet);
+  size_t nf = 0;
+  for (int i = 0; i < nsheet; i++) {
+    need(ids[i] >= 0 && ids[i] < (int)p.monitors.size(), "unknown monitor id");
+    need(src_comp[i] >= 0 && src_comp[i] < 6, "equivalent source must be an E or H component");
+    const Monitor &m = p.monitors[ids[i]];
+    need(!m.centered, "near2far monitors must be on the Yee grid (centered = 0)");
+    if (i == 0) nf = m.freq.size();
+    need(m.freq.size() == nf, "near2far monitors differ in frequencies");
+    sh[i].id = ids[i];
+    sh[i].c0 = src_comp[i];
+    for (int d = 0; d < 3; d++) {
+      sh[i].is_half[d] = is_half[3 * i + d];
+      sh[i].rshift[d] = rshift[3 * i + d];
+    }
+  }
+  if (nx == 0) return 0;
+  if (!s->setup_done) {
+    std::memset(out, 0, sizeof(double) * 12 * nf * (size_t)nx);
+    return 0;
+  }
+  s->be->farfield(p, sp, sh, nx, x, out);
+  MFD_CATCH
+}
+
+int mfd_green(int dim, int c0, double freq, double eps, double mu, double f0_re, double f0_im, int64_t n,
+              const double *x, const double *x0, double *out) {
+  MFD_TRY
+  need(dim == 2 || dim == 3, "wrong dimensionality in green's function (2 or 3)");
+  need(c0 >= 0 && c0 < 6, "unrecognized source type");
+  need(n >= 0 && (n == 0 || (x && x0 && out)), "null point array");
+  if (n > 0) green_eval(dim, c0, freq, eps, mu, f0_re, f0_im, n, x, x0, out);
+  MFD_CATCH
+}
+
 int64_t mfd_kernel_launches(const mfd_sim *s) { return s && s->be ? s->be->launches() : 0; }
 
 double mfd_last_step_ms(const mfd_sim *s) { return s && s->be ? s->be->last_step_ms() : 0.0; }

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "mfd_backend.hpp"
+#include "mfd_near2far.hpp"
 
 namespace mfd {
 namespace cuda_impl {
@@ -2335,6 +2336,35 @@ public:
     cuda_check(cudaMemcpyAsync(out, d_out, nf * sizeof(double), cudaMemcpyDeviceToHost, stream),
                "download flux");
     cuda_check(cudaStreamSynchronize(stream), "flux sync");
+    check_tc();
+  }
+
+  void scale_dft(Plan &p, int id, std::complex<double> sc) override {
+    dft_flush(p, id);
+    const Monitor &m = p.monitors[id];
+    scale_device(mons[id].acc, (long long)(m.npts * m.freq.size()), sc.real(), sc.imag(), stream, nlaunch);
+    cuda_check(cudaStreamSynchronize(stream), "scale sync");
+    check_tc();
+  }
+
+  void farfield(Plan &p, const N2FSpec &s, const std::vector<N2FSheet> &sheets, int64_t nx, const double *x,
+                double *out) override {
+    std::vector<N2FDevSheet> dev;
+    for (const N2FSheet &sh : sheets) {
+      dft_flush(p, sh.id);
+      const Monitor &m = p.monitors[sh.id];
+      N2FDevSheet d{};
+      d.dft = mons[sh.id].acc;
+      for (int q = 0; q < 3; q++) {
+        d.n[q] = m.hi[q] - m.lo[q] + 1;
+        d.is_half[q] = sh.is_half[q];
+        d.rshift[q] = sh.rshift[q];
+      }
+      d.c0 = sh.c0;
+      dev.push_back(d);
+    }
+    const std::vector<double> &fr = p.monitors[sheets[0].id].freq;
+    farfield_device(s, dev, (int)fr.size(), fr.data(), nx, x, out, stream, nlaunch);
     check_tc();
   }
 };

@@ -269,6 +269,10 @@ class FluxRegion:
         self.direction, self.weight = direction, complex(weight)
 
 
+# near-to-far surfaces are flux regions (python/simulation.py: Near2FarRegion = FluxRegion)
+Near2FarRegion = FluxRegion
+
+
 # ------------------------------------------------------------ step funcs
 def _num_args(f):
     import inspect
@@ -377,6 +381,13 @@ _SIGS = [
     ("mgb_get_epsilon_points", C.c_int, [_P, C.c_int, _DP, _DP]),
     ("mgb_yee_array", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     ("mgb_use_bloch", C.c_int, [_P, _DP]),
+    ("mgb_add_near2far", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("mgb_near2far_points", C.c_int, [_P, C.c_int, C.c_int, _DP, _DP]),
+    ("mgb_near2far_array", C.c_int, [_P, C.c_int, _DP, _DP, C.c_double, _DP, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]),
+    ("mgb_near2far_flux", C.c_int, [_P, C.c_int, C.c_int, _DP, _DP, C.c_double, _DP]),
+    ("mgb_near2far_scale", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
+    ("mgb_near2far_medium", C.c_int, [_P, C.c_int, _DP, _DP]),
 ]
 
 _LIBS = {}
@@ -409,6 +420,43 @@ class DftFlux:
 class DftFields:
     def __init__(self, sim, handle, freq, components):
         self.sim, self.handle, self.freq, self.components = sim, handle, list(freq), list(components)
+
+
+class DftNear2Far:
+    """Near-to-far transform object (python/simulation.py DftNear2Far): the
+    DFTs of the tangential fields on its regions, far fields by the
+    homogeneous-medium Green's function, evaluated on the GPU."""
+
+    def __init__(self, sim, handle, freq, nperiods, regions):
+        self.sim, self.handle, self.freq = sim, handle, list(freq)
+        self.nfreqs, self.nperiods, self.regions = len(self.freq), nperiods, list(regions)
+
+    def _medium(self):
+        e, m = C.c_double(), C.c_double()
+        self.sim._check(self.sim._lib.mgb_near2far_medium(self.sim._h, self.handle, C.byref(e), C.byref(m)))
+        return e.value, m.value
+
+    @property
+    def eps(self):
+        return self._medium()[0]
+
+    @property
+    def mu(self):
+        return self._medium()[1]
+
+    def flux(self, direction=None, where=None, resolution=None):
+        """Poynting flux in `direction` of the far fields on a grid over the
+        Volume `where` at `resolution` (a list of nfreq values)."""
+        out = np.zeros(self.nfreqs)
+        c_a, c_p = _arr(list(where.center))
+        z_a, z_p = _arr(list(where.size))
+        self.sim._check(self.sim._lib.mgb_near2far_flux(self.sim._h, self.handle, int(direction), c_p, z_p,
+                                                        float(resolution), out.ctypes.data_as(_DP)))
+        return list(out)
+
+    def scale_dfts(self, s):
+        s = complex(s)
+        self.sim._check(self.sim._lib.mgb_near2far_scale(self.sim._h, self.handle, s.real, s.imag))
 
 
 def _fix_dft_args(args, i):
@@ -566,6 +614,73 @@ class Simulation:
         flux = DftFlux(self, h.value, freq)
         self.dft_objects.append(flux)
         return flux
+
+    def add_near2far(self, *args, **kwargs):
+        """add_near2far(fcen, df, nfreq | freq, *Near2FarRegions, nperiods=1,
+        decimation_factor=0): the DFTs of the tangential fields on the regions
+        (python/simulation.py Simulation.add_near2far)."""
+        args = _fix_dft_args(args, 0)
+        freq, regions = list(np.asarray(args[0], dtype=np.float64)), args[1:]
+        nperiods = int(kwargs.get("nperiods", 1))
+        decimation = int(kwargs.get("decimation_factor", 0))
+        self.init_sim()
+        rows = []
+        for r in regions:
+            if r.weight.imag != 0:
+                raise NotImplementedError("meep: complex near2far weights are not supported")
+            rows += list(r.center) + list(r.size) + [r.direction, r.weight.real]
+        r_a, r_p = _arr(rows)
+        f_a, f_p = _arr(freq)
+        h = C.c_int()
+        self._check(self._lib.mgb_add_near2far(self._h, len(regions), r_p, len(freq), f_p, decimation, nperiods,
+                                               C.byref(h)))
+        n2f = DftNear2Far(self, h.value, freq, nperiods, regions)
+        self.dft_objects.append(n2f)
+        return n2f
+
+    def _farfields_at(self, near2far, points):
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros((pts.shape[0], near2far.nfreqs, 6, 2))
+        self._check(self._lib.mgb_near2far_points(self._h, near2far.handle, pts.shape[0], pts.ctypes.data_as(_DP),
+                                                  out.ctypes.data_as(_DP)))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def get_farfield(self, near2far, x, greencyl_tol=1e-3):
+        """Far fields at the Vector3 x: a list of 6 nfreq complex values
+        (Ex, Ey, Ez, Hx, Hy, Hz for each frequency in turn)."""
+        self.init_sim()
+        return list(self._farfields_at(near2far, [list(_v3(x))]).ravel())
+
+    def get_farfields_at(self, near2far, points):
+        """Far fields at many points (an n x 3 array) in one GPU call: an
+        array (n, nfreq, 6) of complex Ex..Hz (an extension of get_farfield)."""
+        self.init_sim()
+        return self._farfields_at(near2far, points)
+
+    def get_farfields(self, near2far, resolution=None, where=None, center=None, size=None, greencyl_tol=1e-3):
+        """Far fields on a grid over a volume at `resolution`: a dict of
+        arrays Ex..Hz shaped (points per non-singleton direction..., nfreq),
+        the frequency axis only when nfreq > 1 (python/simulation.py
+        get_farfields)."""
+        self.init_sim()
+        if where is not None:
+            center, size = where.center, where.size
+        c_a, c_p = _arr(list(_v3(center)))
+        z_a, z_p = _arr(list(_v3(size)))
+        dims = (C.c_int * 3)()
+        rank = C.c_int()
+        self._check(self._lib.mgb_near2far_array(self._h, near2far.handle, c_p, z_p, float(resolution), None, dims,
+                                                 C.byref(rank)))
+        npts = int(np.prod([dims[i] for i in range(3)]))
+        out = np.zeros(12 * npts * near2far.nfreqs)
+        self._check(self._lib.mgb_near2far_array(self._h, near2far.handle, c_p, z_p, float(resolution),
+                                                 out.ctypes.data_as(_DP), dims, C.byref(rank)))
+        shape = [dims[i] for i in range(rank.value) if dims[i] > 1]
+        if near2far.nfreqs > 1:
+            shape.append(near2far.nfreqs)
+        arr = out.reshape(12, -1)
+        names = ["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"]
+        return {n: (arr[2 * k] + 1j * arr[2 * k + 1]).reshape(shape) for k, n in enumerate(names)}
 
     def add_dft_fields(self, components, *args, where=None, center=None, size=None, yee_grid=False,
                        decimation_factor=0, persist=False):
@@ -745,3 +860,11 @@ def get_fluxes(f):
 
 def get_flux_freqs(f):
     return list(f.freq)
+
+
+def get_near2far_freqs(f):
+    return list(f.freq)
+
+
+def scale_near2far_fields(s, near2far):
+    near2far.scale_dfts(s)

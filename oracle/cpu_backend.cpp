@@ -15,9 +15,13 @@
 //   sources             fields_chunk::step_source src/step.cpp:295-318
 //   DFT                 dft_chunk::update_dft     src/dft.cpp:266-308
 //   flux                dft_flux::flux            src/dft.cpp:542-556
+//   scale_dft           dft_chunk::scale_dft      src/dft.cpp:402-406
+//   far fields          dft_near2far::farfield_lowlevel src/near2far.cpp:334-378
+//                       green3d / green2d         src/near2far.cpp:131-245
 // The per-chunk choice of formula is made per point from its chunk region
 // (Plan::region), see meep_gb300/csrc/mfd_plan.hpp.
 #include "geom_eval.hpp"
+#include "greens.hpp"
 #include "subpixel.hpp"
 #include <chrono>
 #include <cmath>
@@ -642,6 +646,64 @@ public:
           out[w] += real(E[k * nf + w] * conj(H[k * nf + w]));
     }
   }
+
+  void scale_dft(Plan &p, int id, std::complex<double> s) override {
+    for (auto &v : dft[id]) v *= s;
+    (void)p;
+  }
+
+  // the reference's loop: per far point, sheets in list order, then per
+  // frequency the sheet's points in order and their periodic images
+  void farfield(Plan &p, const N2FSpec &s, const std::vector<N2FSheet> &sheets, int64_t nx, const double *x,
+                double *out) override {
+    using mgb_green::cplx;
+    const size_t nf = p.monitors[sheets[0].id].freq.size();
+    const std::vector<double> &freq = p.monitors[sheets[0].id].freq;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t ix = 0; ix < nx; ix++) {
+      std::vector<std::complex<double>> EH(6 * nf, 0.0);
+      const double xf[3] = {x[3 * ix], x[3 * ix + 1], s.dim == 2 ? 0.0 : x[3 * ix + 2]};
+      for (const N2FSheet &sh : sheets) {
+        const Monitor &m = p.monitors[sh.id];
+        const std::vector<std::complex<double>> &a = dft[sh.id];
+        int n[3];
+        for (int d = 0; d < 3; d++)
+          n[d] = m.hi[d] - m.lo[d] + 1;
+        for (size_t i = 0; i < nf; ++i) {
+          size_t idx = 0;
+          for (int k0 = 0; k0 < n[0]; k0++)
+            for (int k1 = 0; k1 < n[1]; k1++)
+              for (int k2 = 0; k2 < n[2]; k2++, idx++) {
+                const int k[3] = {k0, k1, k2};
+                double x0[3];
+                for (int d = 0; d < 3; d++)
+                  x0[d] = (sh.is_half[d] + k[d]) * s.inva + sh.rshift[d];
+                if (s.dim == 2) x0[2] = 0.0;
+                const std::complex<double> J = a[nf * idx + i];
+                double xs[3] = {x0[0], x0[1], x0[2]};
+                for (int i0 = -s.pn[0]; i0 <= s.pn[0]; ++i0) {
+                  if (s.pdir[0] >= 0) xs[s.pdir[0]] = x0[s.pdir[0]] + i0 * s.period[0];
+                  const double phase0 = i0 * s.pk[0];
+                  for (int i1 = -s.pn[1]; i1 <= s.pn[1]; ++i1) {
+                    if (s.pdir[1] >= 0) xs[s.pdir[1]] = x0[s.pdir[1]] + i1 * s.period[1];
+                    const double phase = phase0 + i1 * s.pk[1];
+                    const std::complex<double> cphase = std::polar(1.0, phase);
+                    cplx E6[6];
+                    if (s.dim == 2) mgb_green::green2d(E6, xf, freq[i], s.eps, s.mu, xs, sh.c0, {J.real(), J.imag()});
+                    else mgb_green::green3d(E6, xf, freq[i], s.eps, s.mu, xs, sh.c0, {J.real(), J.imag()});
+                    for (int j = 0; j < 6; ++j)
+                      EH[i * 6 + j] += std::complex<double>(E6[j].re, E6[j].im) * cphase;
+                  }
+                }
+              }
+        }
+      }
+      for (size_t q = 0; q < 6 * nf; q++) {
+        out[(ix * 6 * nf + q) * 2] = EH[q].real();
+        out[(ix * 6 * nf + q) * 2 + 1] = EH[q].imag();
+      }
+    }
+  }
 };
 
 } // namespace
@@ -663,6 +725,20 @@ void subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const doub
 #pragma omp parallel for schedule(dynamic, 64)
   for (int64_t i = 0; i < npix; i++)
     mgb_subpixel::eff_chi1inv_row(dim, cdir, lo + 3 * i, hi + 3 * i, tol, maxeval, sq, chi, rows + 3 * i);
+}
+
+// mfd_green on the host
+void green_eval(int dim, int c0, double freq, double eps, double mu, double f0re, double f0im, int64_t n,
+                const double *x, const double *x0, double *out) {
+  for (int64_t i = 0; i < n; i++) {
+    mgb_green::cplx EH[6];
+    if (dim == 2) mgb_green::green2d(EH, x + 3 * i, freq, eps, mu, x0 + 3 * i, c0, {f0re, f0im});
+    else mgb_green::green3d(EH, x + 3 * i, freq, eps, mu, x0 + 3 * i, c0, {f0re, f0im});
+    for (int c = 0; c < 6; c++) {
+      out[12 * i + 2 * c] = EH[c].re;
+      out[12 * i + 2 * c + 1] = EH[c].im;
+    }
+  }
 }
 
 } // namespace mfd

@@ -874,6 +874,218 @@ static void case_py_aniso3d(Writer &w) {
   w.rec("chi_EzY", global_chi1inv(s, gv, Ez, Y));
 }
 
+/* Near-to-far transform (src/near2far.cpp), after the reference's
+   tests/near2far.cpp check_2d_3d: eps = 2 everywhere, two point sources at
+   the origin (c0, and c1 with amplitude 0.7654321), a closed box of near2far
+   surfaces at +-xmax/4, scale_dfts(sqrt(2 pi) / dt); here with Gaussian
+   pulses run until they have left the cell instead of solve_cw, and no
+   mirror symmetry.  Records: far fields at 20 points beyond the cell (the
+   reference test's points), a far-field array over a line (2-D) or plane
+   (3-D) and its flux. */
+static double two_eps(const vec &) { return 2.0; }
+
+static void write_n2f(Writer &w, dft_near2far &n2f, const std::vector<vec> &pts, const volume &arr, direction df,
+                      double res) {
+  const size_t nf = n2f.freq.size();
+  std::vector<double> sums;
+  for (dft_chunk *ch = n2f.F; ch; ch = ch->next_in_dft)
+    for (size_t i = 0; i < ch->N * nf; i++) {
+      sums.push_back(ch->dft[i].real());
+      sums.push_back(ch->dft[i].imag());
+    }
+  w.rec("n2f_dft", sums);
+  w.scalar("n2f_eps", n2f.eps);
+  w.scalar("n2f_mu", n2f.mu);
+  std::vector<double> ff;
+  for (const vec &x : pts) {
+    complex<double> *EH = n2f.farfield(x);
+    for (size_t i = 0; i < 6 * nf; i++) {
+      ff.push_back(EH[i].real());
+      ff.push_back(EH[i].imag());
+    }
+    delete[] EH;
+  }
+  w.rec("ff", ff);
+  std::vector<double> xs;
+  for (const vec &x : pts)
+    for (int d = 0; d < 3; d++)
+      xs.push_back(d < 2 || x.dim == D3 ? x.in_direction(direction(d)) : 0.0);
+  w.rec("ff_points", xs);
+  int rank = 0;
+  size_t dims[3] = {1, 1, 1}, N = 1;
+  double *EH = n2f.get_farfields_array(arr, rank, dims, N, res);
+  w.rec("ffarr", std::vector<double>(EH, EH + 12 * N * nf));
+  w.rec("ffarr_dims", std::vector<double>{double(rank), double(dims[0]), double(dims[1]), double(dims[2])});
+  delete[] EH;
+  double *F = n2f.flux(df, arr, res);
+  w.rec("ffflux", std::vector<double>(F, F + nf));
+  delete[] F;
+}
+
+static void case_n2f(Writer &w, ndim dim, component c0, component c1, int steps) {
+  const double dpml = 1, xmax = dim == D2 ? 4 : 3, a = dim == D2 ? 20 : 10;
+  grid_volume gv = dim == D2 ? vol2d(xmax + 2 * dpml, xmax + 2 * dpml, a)
+                             : vol3d(xmax + 2 * dpml, xmax + 2 * dpml, xmax + 2 * dpml, a);
+  gv.center_origin();
+  structure s(gv, two_eps, pml(dpml), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  const double w0 = dim == D2 ? 0.3 : 0.5;
+  // same pulse for both; a current (not integrated) source where it is
+  // magnetic, the only kind this engine takes on H
+  gaussian_src_time src(w0, dim == D2 ? 0.2 : 0.3), srcm(w0, dim == D2 ? 0.2 : 0.3);
+  srcm.is_integrated = false;
+  f.add_point_source(c0, is_magnetic(c0) ? srcm : src, zero_vec(dim));
+  f.add_point_source(c1, is_magnetic(c1) ? srcm : src, zero_vec(dim), 0.7654321);
+  const double L = xmax / 4;
+  volume_list *vl;
+  if (dim == D2)
+    vl = new volume_list(
+        volume(vec(-L, +L), vec(+L, +L)), Sy, 1.0,
+        new volume_list(volume(vec(+L, +L), vec(+L, -L)), Sx, 1.0,
+                        new volume_list(volume(vec(-L, -L), vec(+L, -L)), Sy, -1.0,
+                                        new volume_list(volume(vec(-L, -L), vec(-L, +L)), Sx, -1.0))));
+  else
+    vl = new volume_list(
+        volume(vec(+L, -L, -L), vec(+L, +L, +L)), Sx, +1.,
+        new volume_list(
+            volume(vec(-L, -L, -L), vec(-L, +L, +L)), Sx, -1.,
+            new volume_list(
+                volume(vec(-L, +L, -L), vec(+L, +L, +L)), Sy, +1.,
+                new volume_list(volume(vec(-L, -L, -L), vec(+L, -L, +L)), Sy, -1.,
+                                new volume_list(volume(vec(-L, -L, +L), vec(+L, +L, +L)), Sz, +1.,
+                                                new volume_list(volume(vec(-L, -L, -L), vec(+L, +L, -L)),
+                                                                Sz, -1.))))));
+  std::vector<double> fr = {w0 - 0.05, w0, w0 + 0.05};
+  dft_near2far n2f = f.add_dft_near2far(vl, fr.data(), fr.size(), 0, 1);
+  delete vl;
+  for (int i = 0; i < steps; i++)
+    f.step();
+  w.scalar("t", f.time());
+  n2f.scale_dfts(std::sqrt(2 * pi) / f.dt);
+  sync_dfts(f);
+  const int N = 20;
+  const double dx = 0.75 * (xmax / 4) / N;
+  std::vector<vec> pts;
+  for (int i = 0; i < N; ++i) {
+    const double sx = xmax + dx * i;
+    pts.push_back(dim == D2 ? vec(sx, 0.5 * sx) : vec(sx, 0.5 * sx, 0.3 * sx));
+  }
+  if (dim == D2) write_n2f(w, n2f, pts, volume(vec(6, -3), vec(6, 3)), X, 4.0);
+  else write_n2f(w, n2f, pts, volume(vec(4, -2, -2), vec(4, 2, 2)), X, 3.0);
+}
+
+// periodic in x (Bloch), PML in y: a near2far line spanning the cell width,
+// summed over 2 * 3 + 1 lattice images with the Bloch phase
+static double eps15(const vec &) { return 1.5; }
+
+static void case_n2f_periodic2d(Writer &w, int steps) {
+  grid_volume gv = vol2d(2.0, 6.0, 20.0);
+  gv.center_origin();
+  structure s(gv, eps15, pml(1.0, Y), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_bloch(X, 0.15);
+  gaussian_src_time src(0.6, 0.4), srcm(0.6, 0.4);
+  srcm.is_integrated = false;
+  f.add_point_source(Ez, src, vec(0.2, -1.0));
+  f.add_point_source(Hx, srcm, vec(-0.3, -0.8), complex<double>(0.3, 0.2));
+  volume_list vl(volume(vec(-1.0, 1.0), vec(1.0, 1.0)), Sy, 1.0);
+  std::vector<double> fr = {0.5, 0.6, 0.7};
+  dft_near2far n2f = f.add_dft_near2far(&vl, fr.data(), fr.size(), 0, 3);
+  for (int i = 0; i < steps; i++)
+    f.step();
+  w.scalar("t", f.time());
+  sync_dfts(f);
+  std::vector<vec> pts;
+  for (int i = 0; i < 12; ++i)
+    pts.push_back(vec(-1.5 + 0.27 * i, 3.0 + 0.4 * i));
+  write_n2f(w, n2f, pts, volume(vec(-2, 5), vec(2, 5)), Y, 5.0);
+  w.scalar("n2f_periodic_n", n2f.periodic_n[1]);
+  w.scalar("n2f_periodic_k", n2f.periodic_k[1]);
+}
+
+/* Script (the reference's python/tests/test_antenna_radiation.py
+   test_poynting_theorem at resolution 20, no mirror symmetry, a fixed run
+   time instead of stop_when_fields_decayed):
+     sim = mp.Simulation(cell_size=mp.Vector3(6, 6), resolution=20, boundary_layers=[mp.PML(1)],
+                         sources=[mp.Source(mp.GaussianSource(1.0, fwidth=0.4), center=mp.Vector3(),
+                                            component=mp.Ez)], eps_averaging=False)
+     n2f = sim.add_near2far(1.0, 0, 1, <the four sides of the 4 x 4 box, weights +1, -1, +1, -1>)
+     box = sim.add_flux(1.0, 0, 1, <the same four regions>)
+     sim.run(until_after_sources=40)
+     near = mp.get_fluxes(box)[0]
+     ff = [sim.get_farfield(n2f, mp.Vector3(1000 * sin(a), 1000 * cos(a))) for 12 angles a in [0, pi/2)]
+     square = [n2f.flux(d, mp.Volume(center=..., size=...), 20) for the four sides of a 20 x 20 square]
+     arr = sim.get_farfields(n2f, resolution=2, center=mp.Vector3(0, 6), size=mp.Vector3(10, 0)) */
+static void case_py_n2f(Writer &w) {
+  grid_volume gv = vol2d(6, 6, 20);
+  gv.center_origin();
+  structure s(gv, one_eps, pml(1.0), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  const double fcen = 1.0, df = 0.4, sxy = 4;
+  double width = std::max(0.0, 1 / df);
+  gaussian_src_time src(fcen, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, volume(vec(0, 0), vec(0, 0)), complex<double>(1.0, 0.0));
+  // regions in script order; the Python layer prepends each to the list
+  struct Reg {
+    vec c, sz;
+    double wgt;
+  } regs[4] = {{vec(0, 0.5 * sxy), vec(sxy, 0), 1.0},
+               {vec(0, -0.5 * sxy), vec(sxy, 0), -1.0},
+               {vec(0.5 * sxy, 0), vec(0, sxy), 1.0},
+               {vec(-0.5 * sxy, 0), vec(0, sxy), -1.0}};
+  auto vlist = [&]() {
+    volume_list *vl = nullptr;
+    for (const Reg &r : regs) {
+      volume v(r.c - r.sz * 0.5, r.c + r.sz * 0.5);
+      vl = new volume_list(v, r.sz.x() == 0 ? Sx : Sy, r.wgt, vl);
+    }
+    return vl;
+  };
+  std::vector<double> fr = {fcen};
+  volume_list *l1 = vlist();
+  dft_near2far n2f = f.add_dft_near2far(l1, fr.data(), fr.size(), 0, 1);
+  delete l1;
+  volume_list *l2 = vlist();
+  dft_flux box = f.add_dft_flux(l2, fr.data(), fr.size(), true, true, 0);
+  delete l2;
+  py_run_until_after_sources(f, 40);
+  sync_dfts(f);
+  double *F = box.flux();
+  w.scalar("near_flux", F[0]);
+  delete[] F;
+  w.scalar("t", f.time());
+  std::vector<double> ff;
+  for (int i = 0; i < 12; i++) {
+    const double ang = 0.5 * pi / 12 * i, r = 1000 / fcen;
+    complex<double> *EH = n2f.farfield(vec(r * std::sin(ang), r * std::cos(ang)));
+    for (int j = 0; j < 6; j++) {
+      ff.push_back(EH[j].real());
+      ff.push_back(EH[j].imag());
+    }
+    delete[] EH;
+  }
+  w.rec("ff", ff);
+  const double rr = 20 / fcen;
+  const direction dirs[4] = {Y, Y, X, X};
+  const vec cen[4] = {vec(0, 0.5 * rr), vec(0, -0.5 * rr), vec(0.5 * rr, 0), vec(-0.5 * rr, 0)};
+  const vec siz[4] = {vec(rr, 0), vec(rr, 0), vec(0, rr), vec(0, rr)};
+  std::vector<double> sq;
+  for (int k = 0; k < 4; k++) {
+    double *Fk = n2f.flux(dirs[k], volume(cen[k] - siz[k] * 0.5, cen[k] + siz[k] * 0.5), 20);
+    sq.push_back(Fk[0]);
+    delete[] Fk;
+  }
+  w.rec("square_flux", sq);
+  int rank = 0;
+  size_t dims[3] = {1, 1, 1}, N = 1;
+  double *EH = n2f.get_farfields_array(volume(vec(-5, 6), vec(5, 6)), rank, dims, N, 2.0);
+  w.rec("ffarr", std::vector<double>(EH, EH + 12 * N));
+  delete[] EH;
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -917,6 +1129,16 @@ int main(int argc, char **argv) {
     case_py_aniso3d(w);
   else if (cs == "aniso1d")
     case_aniso1d(w, steps > 0 ? steps : 400);
+  else if (cs == "n2f_tm2d")
+    case_n2f(w, D2, Ez, Hx, steps > 0 ? steps : 2800);
+  else if (cs == "n2f_te2d")
+    case_n2f(w, D2, Ex, Hz, steps > 0 ? steps : 2800);
+  else if (cs == "n2f3d")
+    case_n2f(w, D3, Ez, Hx, steps > 0 ? steps : 900);
+  else if (cs == "py_n2f")
+    case_py_n2f(w);
+  else if (cs == "n2f_periodic2d")
+    case_n2f_periodic2d(w, steps > 0 ? steps : 1600);
   else {
     fprintf(stderr, "unknown case %s\n", cs.c_str());
     return 2;

@@ -1,0 +1,258 @@
+"""Near-to-far transform (dft_near2far, src/near2far.cpp).
+
+Cases of tests/golden/golden_driver.cpp run by the reference core (fixtures)
+and by the meep:: drop-in over the oracle (CPU) or the CUDA engine (GPU):
+  n2f_tm2d        2-D, eps = 2, Ez + Hx point pulses at the origin, a closed
+                  box of four near2far lines (the geometry of the reference's
+                  tests/near2far.cpp check_2d_3d)
+  n2f_te2d        the same with Ex + Hz (in-plane currents: the H0 - H2
+                  branch of green2d)
+  n2f3d           3-D, Ez + Hx, a closed box of six planes
+  n2f_periodic2d  Bloch-periodic in x, PML in y, one line spanning the cell,
+                  Nperiods = 3 (seven lattice images with the Bloch phase)
+Records: the raw near2far DFT sums after scale_dfts, far fields at 20 points
+(dft_near2far::farfield), get_farfields_array over a line or plane, and
+dft_near2far::flux through it."""
+import numpy as np
+import pytest
+
+from harness import GPU_DRIVER, ORACLE_DRIVER, golden, relerr, run_driver
+
+CASES = ["n2f_tm2d", "n2f_te2d", "n2f3d", "n2f_periodic2d"]
+SKIP = ("t", "realnum_bytes")
+
+
+def _green(path, dim, c0, freq, eps, mu, x, x0, f0=1.0 + 0.0j):
+    from meep_gb300 import _lib
+    return _lib.Engine(path).green(dim, c0, freq, eps, mu, x, x0, f0)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_fp64_matches_reference(case, oracle_lib, tmp_path):
+    """CPU restatement: DFT sums, far fields, far-field arrays and far-field
+    flux bit-identical to the reference FP64 build (same Green's function
+    arithmetic, same glibc sin/cos/jn/yn, same summation order)."""
+    ref = golden(case, "f64")
+    out = run_driver(ORACLE_DRIVER[64], case, tmp_path)
+    for k, v in ref.items():
+        if k in SKIP:
+            continue
+        assert np.array_equal(np.asarray(out[k]), np.asarray(v)), (case, k, relerr(out[k], v))
+
+
+# (case, dim, c0, c1 as mfd component codes Ex..Ez = 0..2, Hx..Hz = 3..5, freqs, resolution)
+PHYS = [("n2f_tm2d", 2, 2, 3, [0.25, 0.3, 0.35], 20.0), ("n2f_te2d", 2, 0, 5, [0.25, 0.3, 0.35], 20.0),
+        ("n2f3d", 3, 2, 3, [0.45, 0.5, 0.55], 10.0)]
+
+
+@pytest.mark.parametrize("case,dim,c0,c1,freqs,res", PHYS)
+def test_far_fields_are_dipole_fields(case, dim, c0, c1, freqs, res, oracle_lib, tmp_path):
+    """Physics, after the reference's NEAR2FAR check: the far fields of the
+    box around two point sources equal a0 G(c0) + a1 G(c1) with the analytic
+    homogeneous-medium Green's functions, within the reference test's
+    tolerance 0.05 * 30 / resolution (observed 3e-5 to 1e-4 in 2-D, 0.3-0.5%
+    in 3-D at resolution 10); the amplitude ratio is that of the sources."""
+    out = run_driver(ORACLE_DRIVER[64], case, tmp_path)
+    pts = np.asarray(out["ff_points"]).reshape(-1, 3)
+    nf = len(freqs)
+    ff = np.asarray(out["ff"]).reshape(len(pts), nf, 6, 2)
+    ff = ff[..., 0] + 1j * ff[..., 1]
+    zero = np.zeros_like(pts)
+    for i, fr in enumerate(freqs):
+        A = np.stack([_green(oracle_lib, dim, c, fr, 2.0, 1.0, pts, zero).ravel() for c in (c0, c1)], 1)
+        y = ff[:, i, :].ravel()
+        coef = np.linalg.lstsq(A, y, rcond=None)[0]
+        res_rel = np.linalg.norm(A @ coef - y) / np.linalg.norm(y)
+        assert res_rel < 0.05 * 30 / res, (case, fr, res_rel)
+        assert abs(abs(coef[1] / coef[0]) - 0.7654321) < 0.05, (case, fr, coef)
+
+
+def test_green_function_cases(oracle_lib):
+    """Host Green's functions: reciprocity of the electric 3-D dipole
+    (G_ij(x, x0) = G_ji(x0, x)), far-field decay 1/r (3-D) and 1/sqrt(r)
+    (2-D), and transversality of E and H to r far away (3-D)."""
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=(50, 3))
+    x0 = rng.normal(size=(50, 3))
+    for i in range(3):
+        for j in range(3):
+            gij = _green(oracle_lib, 3, j, 0.7, 2.0, 1.3, x, x0)[:, i]
+            gji = _green(oracle_lib, 3, i, 0.7, 2.0, 1.3, x0, x)[:, j]
+            assert np.allclose(gij, gji, rtol=1e-12, atol=1e-14)
+    d = np.array([[0.6, 0.48, 0.64]])
+    for c in range(6):
+        near = _green(oracle_lib, 3, c, 0.5, 1.0, 1.0, 1e3 * d, 0 * d)
+        far = _green(oracle_lib, 3, c, 0.5, 1.0, 1.0, 2e3 * d, 0 * d)
+        assert np.allclose(np.abs(far), 0.5 * np.abs(near), rtol=2e-3)
+        E, H = far[0, :3], far[0, 3:]
+        assert abs(np.dot(E, d[0])) < 1e-3 * np.linalg.norm(E) and abs(np.dot(H, d[0])) < 1e-3 * np.linalg.norm(H)
+    d2 = np.array([[0.6, 0.8, 0.0]])
+    for c in range(6):
+        near = _green(oracle_lib, 2, c, 0.5, 1.0, 1.0, 1e3 * d2, 0 * d2)
+        far = _green(oracle_lib, 2, c, 0.5, 1.0, 1.0, 4e3 * d2, 0 * d2)
+        assert np.allclose(np.abs(far), 0.5 * np.abs(near), rtol=2e-3, atol=1e-12)
+
+
+def test_errors(oracle_lib):
+    """The C ABI refuses what the reference aborts on: a Green's function of
+    a dimension other than 2 or 3, an equivalent source that is not an E or
+    H component."""
+    from meep_gb300 import _lib
+    eng = _lib.Engine(oracle_lib)
+    x = np.ones((1, 3))
+    with pytest.raises(_lib.MeepError, match="dimensionality"):
+        eng.green(1, 0, 0.5, 1.0, 1.0, x, 0 * x)
+    with pytest.raises(_lib.MeepError, match="source type"):
+        eng.green(3, 6, 0.5, 1.0, 1.0, x, 0 * x)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_gpu_fp64_matches_reference(case, gpu_drivers, tmp_path):
+    """CUDA engine, FP64: DFT sums within 1e-10 of the reference (observed
+    bit-identical); far fields, arrays and flux from the GPU far-field kernel
+    within 1e-11 (inf-norm relative: CUDA's sin/cos/jn/yn and the warp-tree
+    summation order differ from glibc's and the reference's in the last bits)."""
+    ref = golden(case, "f64")
+    out = run_driver(GPU_DRIVER[64], case, tmp_path)
+    for k, v in ref.items():
+        if k in SKIP:
+            continue
+        tol = 1e-10 if k == "n2f_dft" else 1e-11
+        assert relerr(out[k], v) <= tol, (case, k, relerr(out[k], v))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_gpu_fp32_close_to_reference_fp64(case, gpu_drivers, tmp_path):
+    """FP32 fields (DFT sums in double): far fields no worse than 3x the
+    reference's own FP32 build, or 1e-5."""
+    ref = golden(case, "f64")
+    ref32 = golden(case, "f32")
+    out = run_driver(GPU_DRIVER[32], case, tmp_path)
+    for k, v in ref.items():
+        if k in SKIP:
+            continue
+        e = relerr(out[k], v)
+        assert e <= max(3 * relerr(ref32[k], v), 1e-5), (case, k, e, relerr(ref32[k], v))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gpu_green_matches_host(dim, engine_lib, oracle_lib):
+    """mfd_green on the GPU vs the host restatement, every source component,
+    random point pairs from 0.05 to 50 wavelengths apart: within 1e-12 of
+    the largest field (CUDA's sin/cos/jn/yn, contracted products)."""
+    rng = np.random.default_rng(11 + dim)
+    x = rng.normal(size=(4000, 3)) * np.exp(rng.uniform(-3, 3.9, size=(4000, 1)))
+    x0 = rng.normal(size=(4000, 3))
+    if dim == 2:
+        x[:, 2] = x0[:, 2] = 0
+    for c0 in range(6):
+        g = _green(engine_lib, dim, c0, 0.7, 2.5, 1.2, x, x0, 0.3 - 0.8j)
+        h = _green(oracle_lib, dim, c0, 0.7, 2.5, 1.2, x, x0, 0.3 - 0.8j)
+        scale = np.abs(h).max(axis=1, keepdims=True)
+        assert np.all(np.abs(g - h) <= 1e-12 * scale + 1e-300), (dim, c0, float((np.abs(g - h) / scale).max()))
+
+
+def script_n2f(lib, res=20, until=40, nang=12):
+    """The reference's python/tests/test_antenna_radiation.py
+    test_poynting_theorem (no mirror symmetry; a fixed run time instead of
+    stop_when_fields_decayed), through the Python front end."""
+    import math
+    import meep_gb300 as mp
+    sxy, dpml, fcen, df = 4, 1, 1.0, 0.4
+    sim = mp.Simulation(cell_size=mp.Vector3(sxy + 2 * dpml, sxy + 2 * dpml), resolution=res,
+                        boundary_layers=[mp.PML(dpml)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(fcen, fwidth=df), center=mp.Vector3(),
+                                           component=mp.Ez)], _library=lib)
+    regions = [mp.Near2FarRegion(mp.Vector3(y=0.5 * sxy), size=mp.Vector3(sxy)),
+               mp.Near2FarRegion(mp.Vector3(y=-0.5 * sxy), size=mp.Vector3(sxy), weight=-1),
+               mp.Near2FarRegion(mp.Vector3(0.5 * sxy), size=mp.Vector3(y=sxy)),
+               mp.Near2FarRegion(mp.Vector3(-0.5 * sxy), size=mp.Vector3(y=sxy), weight=-1)]
+    n2f = sim.add_near2far(fcen, 0, 1, *regions)
+    box = sim.add_flux(fcen, 0, 1, *[mp.FluxRegion(r.center, size=r.size, weight=r.weight.real) for r in regions])
+    sim.run(until_after_sources=until)
+    r = 1000 / fcen
+    ff = [sim.get_farfield(n2f, mp.Vector3(r * math.sin(a), r * math.cos(a)))
+          for a in 0.5 * math.pi / nang * np.arange(nang)]
+    rr = 20 / fcen
+    sides = [(mp.Y, mp.Vector3(y=0.5 * rr), mp.Vector3(rr)), (mp.Y, mp.Vector3(y=-0.5 * rr), mp.Vector3(rr)),
+             (mp.X, mp.Vector3(0.5 * rr), mp.Vector3(y=rr)), (mp.X, mp.Vector3(-0.5 * rr), mp.Vector3(y=rr))]
+    square = [n2f.flux(d, mp.Volume(center=c, size=s), 20)[0] for d, c, s in sides]
+    arr = sim.get_farfields(n2f, resolution=2, center=mp.Vector3(0, 6), size=mp.Vector3(10, 0))
+    return {"near_flux": mp.get_fluxes(box)[0], "t": sim.meep_time(), "ff": np.asarray(ff), "square": square,
+            "arr": arr, "freqs": mp.get_near2far_freqs(n2f), "eps": n2f.eps}
+
+
+def _radial_flux(ff):
+    E, H = np.conj(ff[:, :3]), ff[:, 3:]
+    Px = np.real(E[:, 1] * H[:, 2] - E[:, 2] * H[:, 1])
+    Py = np.real(E[:, 2] * H[:, 0] - E[:, 0] * H[:, 2])
+    return np.sqrt(Px ** 2 + Py ** 2)
+
+
+def _check_py_n2f(out, ref, tol):
+    assert abs(out["near_flux"] - ref["near_flux"][0]) <= tol * abs(ref["near_flux"][0])
+    g = np.asarray(ref["ff"]).reshape(-1, 6, 2)
+    assert relerr(np.stack([out["ff"].real, out["ff"].imag], -1), g) <= tol
+    assert relerr(out["square"], ref["square_flux"]) <= tol
+    a = np.asarray(ref["ffarr"]).reshape(6, 2, -1)
+    for k, n in enumerate(["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"]):
+        assert out["arr"][n].shape == (a.shape[2],)
+        assert np.abs(out["arr"][n] - (a[k, 0] + 1j * a[k, 1])).max() <= tol * np.abs(a).max() + 1e-300, n
+
+
+def _oracle_meep(oracle_lib):
+    import os
+    return os.path.join(os.path.dirname(oracle_lib), "liboracle_meep.so")
+
+
+def test_py_n2f_matches_reference(oracle_lib):
+    """The Python front end (add_near2far, get_farfield, get_farfields,
+    DftNear2Far.flux) over the oracle vs the reference core running the same
+    calls: within 1e-12 (the reference splits this cell into chunks at the
+    PML, so its sums run in another order)."""
+    out = script_n2f(_oracle_meep(oracle_lib))
+    ref = golden("py_n2f", "f64")
+    assert out["t"] == ref["t"][0] and out["freqs"] == [1.0] and out["eps"] == 1.0
+    _check_py_n2f(out, ref, 1e-12)
+
+
+def _poynting(out):
+    r = 1000.0
+    circle = 4 * np.sum(_radial_flux(out["ff"])) * 0.5 * np.pi * r / len(out["ff"])
+    s = out["square"]
+    return out["near_flux"], circle, s[0] - s[1] + s[2] - s[3]
+
+
+def test_py_n2f_poynting_theorem(oracle_lib):
+    """Physics (the reference's test_poynting_theorem, here at resolution 20):
+    the flux through the near-field box equals the far-field flux through a
+    circle of radius 1000 and through a 20 x 20 square within 1% (observed
+    0.3%; the reference's resolution-50 tolerance is checked on the GPU)."""
+    near, circle, square = _poynting(script_n2f(_oracle_meep(oracle_lib), nang=50))
+    assert abs(near - circle) < 0.01 * near, (near, circle)
+    assert abs(near - square) < 0.01 * near, (near, square)
+
+
+@pytest.mark.gpu
+def test_gpu_py_n2f(gpu_drivers):
+    """The Python front end on the CUDA engine: FP64 within 1e-11 of the
+    reference core; FP32 within 1e-5."""
+    from test_simulation_api import SINGLE_LIB
+    from meep_gb300.simulation import PRODUCT_LIB
+    ref = golden("py_n2f", "f64")
+    _check_py_n2f(script_n2f(PRODUCT_LIB), ref, 1e-11)
+    _check_py_n2f(script_n2f(SINGLE_LIB), ref, 1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_poynting_theorem_resolution50(gpu_drivers):
+    """The reference's test_poynting_theorem at its resolution 50 on the GPU:
+    near-field box flux and far-field circle flux equal to two decimal
+    places (assertAlmostEqual(places=2))."""
+    from meep_gb300.simulation import PRODUCT_LIB
+    near, circle, square = _poynting(script_n2f(PRODUCT_LIB, res=50, until=50, nang=50))
+    assert round(abs(near - circle), 2) == 0, (near, circle)
+    assert abs(near - square) < 0.01 * near, (near, square)
