@@ -140,9 +140,13 @@ def test_gpu_fp32_close_to_reference_fp64(case, gpu_drivers, tmp_path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("dim", [2, 3])
 def test_gpu_green_matches_host(dim, engine_lib, oracle_lib):
-    """mfd_green on the GPU vs the host restatement, every source component,
-    random point pairs from 0.05 to 50 wavelengths apart: within 1e-12 of
-    the largest field (CUDA's sin/cos/jn/yn, contracted products)."""
+    """mfd_green on the GPU (the device forms the far-field kernel sums:
+    rsqrt, hoisted medium factors, H2 from H0 and H1) vs the reference-order
+    host restatement, every source component, random point pairs from 0.05
+    to 50 wavelengths apart: within 1e-11 (3-D) / 1e-10 (2-D: CUDA's
+    j0/j1/y0/y1 at arguments up to ~1e3 were seen 6e-12 off glibc's) of the
+    largest field at each point.  The same forms on the host agree with the
+    reference order to 3e-13."""
     rng = np.random.default_rng(11 + dim)
     x = rng.normal(size=(4000, 3)) * np.exp(rng.uniform(-3, 3.9, size=(4000, 1)))
     x0 = rng.normal(size=(4000, 3))
@@ -152,7 +156,8 @@ def test_gpu_green_matches_host(dim, engine_lib, oracle_lib):
         g = _green(engine_lib, dim, c0, 0.7, 2.5, 1.2, x, x0, 0.3 - 0.8j)
         h = _green(oracle_lib, dim, c0, 0.7, 2.5, 1.2, x, x0, 0.3 - 0.8j)
         scale = np.abs(h).max(axis=1, keepdims=True)
-        assert np.all(np.abs(g - h) <= 1e-12 * scale + 1e-300), (dim, c0, float((np.abs(g - h) / scale).max()))
+        tol = 1e-10 if dim == 2 else 1e-11
+        assert np.all(np.abs(g - h) <= tol * scale + 1e-300), (dim, c0, float((np.abs(g - h) / scale).max()))
 
 
 def script_n2f(lib, res=20, until=40, nang=12):
