@@ -30,24 +30,41 @@ template <typename R> struct CurlRes {
   bool wfu, wfc;
 };
 
+// the field-sized operands of one component's step_curl branch, loaded up
+// front with predicated loads: no branch separates the loads of the three
+// components of a point, so they are all in flight together (loads inside
+// the branches would wait for each other, one memory round trip per branch)
+template <typename R> struct CurlIn {
+  R fu, fc, cnd, cndinv;
+};
+template <typename R>
+__device__ __forceinline__ CurlIn<R> curl_in(bool sg, bool su, bool hc, const R *fu, const R *fcnd, const R *cnd,
+                                             const R *cndinv, int i) {
+  CurlIn<R> v;
+  v.fu = su ? fu[i] : R(0);
+  v.fc = (sg && hc) ? fcnd[i] : R(0);
+  v.cnd = hc ? cnd[i] : R(0);
+  v.cndinv = hc ? cndinv[i] : R(0);
+  return v;
+}
+
 // step_curl branches for one point (src/step_generic.cpp:94-248)
 template <typename R>
 __device__ __forceinline__ CurlRes<R> curl_general(R fold, R X, R dtdx, R dt2, bool sg, bool su, bool hc,
                                                    const R *sig_s, const R *kap_s, const R *si_s, int ps,
                                                    const R *sig_u, const R *kap_u, const R *si_u, int pu,
-                                                   const R *fu, const R *fcnd, const R *cnd,
-                                                   const R *cndinv, int i) {
+                                                   const CurlIn<R> &v) {
   CurlRes<R> o;
   o.wfu = o.wfc = false;
   o.fu = o.fc = R(0);
   const R one = R(1);
   if (!sg) {
     if (!su) {
-      o.f = hc ? ((one - dt2 * cnd[i]) * fold - dtdx * X) * cndinv[i] : fold - dtdx * X;
+      o.f = hc ? ((one - dt2 * v.cnd) * fold - dtdx * X) * v.cndinv : fold - dtdx * X;
       return o;
     }
-    const R fprev = fu[i];
-    const R fun = hc ? ((one - dt2 * cnd[i]) * fprev - dtdx * X) * cndinv[i] : fprev - dtdx * X;
+    const R fprev = v.fu;
+    const R fun = hc ? ((one - dt2 * v.cnd) * fprev - dtdx * X) * v.cndinv : fprev - dtdx * X;
     o.fu = fun;
     o.wfu = true;
     o.f = si_u[pu] * ((kap_u[pu] - sig_u[pu]) * fold + fun - fprev);
@@ -56,8 +73,8 @@ __device__ __forceinline__ CurlRes<R> curl_general(R fold, R X, R dtdx, R dt2, b
   const R ks = kap_s[ps] - sig_s[ps], si = si_s[ps];
   if (!su) {
     if (hc) {
-      const R fcp = fcnd[i];
-      const R fcn = ((one - dt2 * cnd[i]) * fcp - dtdx * X) * cndinv[i];
+      const R fcp = v.fc;
+      const R fcn = ((one - dt2 * v.cnd) * fcp - dtdx * X) * v.cndinv;
       o.fc = fcn;
       o.wfc = true;
       o.f = (ks * fold + (fcn - fcp)) * si;
@@ -66,11 +83,11 @@ __device__ __forceinline__ CurlRes<R> curl_general(R fold, R X, R dtdx, R dt2, b
       o.f = (ks * fold - dtdx * X) * si;
     return o;
   }
-  const R fprev = fu[i];
+  const R fprev = v.fu;
   R fun;
   if (hc) {
-    const R fcp = fcnd[i];
-    const R fcn = ((one - dt2 * cnd[i]) * fcp - dtdx * X) * cndinv[i];
+    const R fcp = v.fc;
+    const R fcn = ((one - dt2 * v.cnd) * fcp - dtdx * X) * v.cndinv;
     o.fc = fcn;
     o.wfc = true;
     fun = (ks * fprev + (fcn - fcp)) * si;
@@ -149,31 +166,35 @@ __device__ __forceinline__ void b3_point(const FusedArgs<R> &a, const int k[3]) 
   if (hcx && F.s1[1]) hcx = chunk_has(a.cond_chunks[3][0], F.r0[0], F.r1[1], F.r1[2]);
   if (hcy && F.s1[2]) hcy = chunk_has(a.cond_chunks[3][1], F.r1[0], F.r0[1], F.r1[2]);
   if (hcz && F.s1[0]) hcz = chunk_has(a.cond_chunks[3][2], F.r1[0], F.r1[1], F.r0[2]);
-  const CurlRes<R> cx = curl_general(bx, Xx, dtdx, dt2, F.s1[1], F.s1[2], hcx, a.sig[1], a.kap[1], a.siginv[1], p1y,
-                                     a.sig[2], a.kap[2], a.siginv[2], p1z, a.fu[3][0], a.fcnd[3][0], a.cnd[3][0],
-                                     a.cndinv[3][0], i);
-  // By at (1,0,1): dsig = Z, dsigu = X
-  const CurlRes<R> cy = curl_general(by, Xy, dtdx, dt2, F.s1[2], F.s1[0], hcy, a.sig[2], a.kap[2], a.siginv[2], p1z,
-                                     a.sig[0], a.kap[0], a.siginv[0], p1x, a.fu[3][1], a.fcnd[3][1], a.cnd[3][1],
-                                     a.cndinv[3][1], i);
-  // Bz at (1,1,0): dsig = X, dsigu = Y
-  const CurlRes<R> cz = curl_general(bz, Xz, dtdx, dt2, F.s1[0], F.s1[1], hcz, a.sig[0], a.kap[0], a.siginv[0], p1x,
-                                     a.sig[1], a.kap[1], a.siginv[1], p1y, a.fu[3][2], a.fcnd[3][2], a.cnd[3][2],
-                                     a.cndinv[3][2], i);
+  // every field-sized operand of the point before any branch
+  const CurlIn<R> inx = curl_in(F.s1[1], F.s1[2], hcx, a.fu[3][0], a.fcnd[3][0], a.cnd[3][0], a.cndinv[3][0], i);
+  const CurlIn<R> iny = curl_in(F.s1[2], F.s1[0], hcy, a.fu[3][1], a.fcnd[3][1], a.cnd[3][1], a.cndinv[3][1], i);
+  const CurlIn<R> inz = curl_in(F.s1[0], F.s1[1], hcz, a.fu[3][2], a.fcnd[3][2], a.cnd[3][2], a.cndinv[3][2], i);
   // H through f_w inside the slab along its own direction (shift 0 there)
   const bool hx = a.fuse_h && F.s0[0] && vx, hy = a.fuse_h && F.s0[1] && vy, hz = a.fuse_h && F.s0[2] && vz;
+  const R fwx0 = hx ? a.fw[1][0][i] : R(0), hx0 = hx ? a.h[0][i] : R(0);
+  const R fwy0 = hy ? a.fw[1][1][i] : R(0), hy0 = hy ? a.h[1][i] : R(0);
+  const R fwz0 = hz ? a.fw[1][2][i] : R(0), hz0 = hz ? a.h[2][i] : R(0);
+  const CurlRes<R> cx = curl_general(bx, Xx, dtdx, dt2, F.s1[1], F.s1[2], hcx, a.sig[1], a.kap[1], a.siginv[1], p1y,
+                                     a.sig[2], a.kap[2], a.siginv[2], p1z, inx);
+  // By at (1,0,1): dsig = Z, dsigu = X
+  const CurlRes<R> cy = curl_general(by, Xy, dtdx, dt2, F.s1[2], F.s1[0], hcy, a.sig[2], a.kap[2], a.siginv[2], p1z,
+                                     a.sig[0], a.kap[0], a.siginv[0], p1x, iny);
+  // Bz at (1,1,0): dsig = X, dsigu = Y
+  const CurlRes<R> cz = curl_general(bz, Xz, dtdx, dt2, F.s1[0], F.s1[1], hcz, a.sig[0], a.kap[0], a.siginv[0], p1x,
+                                     a.sig[1], a.kap[1], a.siginv[1], p1y, inz);
   R nhx = R(0), nhy = R(0), nhz = R(0), fwx = R(0), fwy = R(0), fwz = R(0);
   if (hx) {
-    const R fwprev = a.fw[1][0][i], kk = a.kap[0][p0x], ss = a.sig[0][p0x];
-    nhx = a.h[0][i] + ((kk + ss) * cx.f - (kk - ss) * fwprev);
+    const R kk = a.kap[0][p0x], ss = a.sig[0][p0x];
+    nhx = hx0 + ((kk + ss) * cx.f - (kk - ss) * fwx0);
   }
   if (hy) {
-    const R fwprev = a.fw[1][1][i], kk = a.kap[1][p0y], ss = a.sig[1][p0y];
-    nhy = a.h[1][i] + ((kk + ss) * cy.f - (kk - ss) * fwprev);
+    const R kk = a.kap[1][p0y], ss = a.sig[1][p0y];
+    nhy = hy0 + ((kk + ss) * cy.f - (kk - ss) * fwy0);
   }
   if (hz) {
-    const R fwprev = a.fw[1][2][i], kk = a.kap[2][p0z], ss = a.sig[2][p0z];
-    nhz = a.h[2][i] + ((kk + ss) * cz.f - (kk - ss) * fwprev);
+    const R kk = a.kap[2][p0z], ss = a.sig[2][p0z];
+    nhz = hz0 + ((kk + ss) * cz.f - (kk - ss) * fwz0);
   }
   fwx = cx.f;
   fwy = cy.f;
@@ -269,6 +290,37 @@ __device__ __forceinline__ void e_store(const FusedArgs<R> &a, int dc, int i, co
   }
 }
 
+// the E operands of one component without poles, loaded up front
+template <typename R> struct EIn {
+  R us, fw, e;
+};
+template <typename R>
+__device__ __forceinline__ EIn<R> e_in(const FusedArgs<R> &a, int dc, int i, bool v, bool slabw) {
+  EIn<R> o;
+  o.us = v ? a.chi[dc][i] : R(0);
+  o.fw = (v && slabw) ? a.fw[0][dc][i] : R(0);
+  o.e = (v && slabw) ? a.e[dc][i] : R(0);
+  return o;
+}
+// e_general without poles, from preloaded operands (same arithmetic)
+template <typename R>
+__device__ __forceinline__ EShell<R> e_from(const FusedArgs<R> &a, int dc, R dn, bool slabw, int pw, const EIn<R> &in) {
+  EShell<R> o;
+  if (slabw) {
+    const R kk = a.kap[dc][pw], ss = a.sig[dc][pw];
+    const R fwn = (dn * in.us);
+    o.fw = fwn;
+    o.wfw = true;
+    o.e = in.e + ((kk + ss) * fwn - (kk - ss) * in.fw);
+  }
+  else {
+    o.e = (dn * in.us);
+    o.fw = R(0);
+    o.wfw = false;
+  }
+  return o;
+}
+
 template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
 __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3]) {
   const int sx = a.s[0], sy = a.s[1];
@@ -303,15 +355,23 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
   if (hcy && F.s0[2]) hcy = chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]);
   // Dz (0,0,1): dsig = X, dsigu = Y
   if (hcz && F.s0[0]) hcz = chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]);
+  const CurlIn<R> inx = curl_in(F.s0[1], F.s0[2], hcx, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i);
+  const CurlIn<R> iny = curl_in(F.s0[2], F.s0[0], hcy, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i);
+  const CurlIn<R> inz = curl_in(F.s0[0], F.s0[1], hcz, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i);
+  // without poles the E operands too (chi, and E and f_w inside the slab
+  // along the component's own direction)
+  EIn<R> ex, ey, ez;
+  if constexpr (!POLES) {
+    ex = e_in(a, 0, i, vx, F.s1[0]);
+    ey = e_in(a, 1, i, vy, F.s1[1]);
+    ez = e_in(a, 2, i, vz, F.s1[2]);
+  }
   const CurlRes<R> cx = curl_general(dx, Xx, dtdx, dt2, F.s0[1], F.s0[2], hcx, a.sig[1], a.kap[1], a.siginv[1], p0y,
-                                     a.sig[2], a.kap[2], a.siginv[2], p0z, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0],
-                                     a.cndinv[2][0], i);
+                                     a.sig[2], a.kap[2], a.siginv[2], p0z, inx);
   const CurlRes<R> cy = curl_general(dy, Xy, dtdx, dt2, F.s0[2], F.s0[0], hcy, a.sig[2], a.kap[2], a.siginv[2], p0z,
-                                     a.sig[0], a.kap[0], a.siginv[0], p0x, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1],
-                                     a.cndinv[2][1], i);
+                                     a.sig[0], a.kap[0], a.siginv[0], p0x, iny);
   const CurlRes<R> cz = curl_general(dz, Xz, dtdx, dt2, F.s0[0], F.s0[1], hcz, a.sig[0], a.kap[0], a.siginv[0], p0x,
-                                     a.sig[1], a.kap[1], a.siginv[1], p0y, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2],
-                                     a.cndinv[2][2], i);
+                                     a.sig[1], a.kap[1], a.siginv[1], p0y, inz);
   // E components share the D positions: f_w slab along their own direction at
   // shift 1.  Without poles all loads go first, then the stores; with poles
   // (four more arrays per pole and component) one component after the other
@@ -341,9 +401,9 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
     }
     return;
   }
-  if (vx) ox = e_general<R, POLES>(a, 0, i, cx.f, F.s1[0], p1x);
-  if (vy) oy = e_general<R, POLES>(a, 1, i, cy.f, F.s1[1], p1y);
-  if (vz) oz = e_general<R, POLES>(a, 2, i, cz.f, F.s1[2], p1z);
+  if (vx) ox = e_from(a, 0, cx.f, F.s1[0], p1x, ex);
+  if (vy) oy = e_from(a, 1, cy.f, F.s1[1], p1y, ey);
+  if (vz) oz = e_from(a, 2, cz.f, F.s1[2], p1z, ez);
   if (vx) {
     a.d[0][i] = cx.f;
     if (cx.wfu) a.fu[2][0][i] = cx.fu;
@@ -393,13 +453,16 @@ __device__ __forceinline__ void d3_point(const FusedArgs<R> &a, const int k[3]) 
   if (hcx && F.s0[1]) hcx = chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]);
   if (hcy && F.s0[2]) hcy = chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]);
   if (hcz && F.s0[0]) hcz = chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]);
+  const CurlIn<R> inx = curl_in(F.s0[1], F.s0[2], hcx, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i);
+  const CurlIn<R> iny = curl_in(F.s0[2], F.s0[0], hcy, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i);
+  const CurlIn<R> inz = curl_in(F.s0[0], F.s0[1], hcz, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i);
   const CurlRes<R> c[3] = {
       curl_general(dx, Xx, dtdx, dt2, F.s0[1], F.s0[2], hcx, a.sig[1], a.kap[1], a.siginv[1], p0y, a.sig[2],
-                   a.kap[2], a.siginv[2], p0z, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i),
+                   a.kap[2], a.siginv[2], p0z, inx),
       curl_general(dy, Xy, dtdx, dt2, F.s0[2], F.s0[0], hcy, a.sig[2], a.kap[2], a.siginv[2], p0z, a.sig[0],
-                   a.kap[0], a.siginv[0], p0x, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i),
+                   a.kap[0], a.siginv[0], p0x, iny),
       curl_general(dz, Xz, dtdx, dt2, F.s0[0], F.s0[1], hcz, a.sig[0], a.kap[0], a.siginv[0], p0x, a.sig[1],
-                   a.kap[1], a.siginv[1], p0y, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i)};
+                   a.kap[1], a.siginv[1], p0y, inz)};
   const bool v[3] = {vx, vy, vz};
 #pragma unroll
   for (int dc = 0; dc < 3; dc++) {
@@ -483,14 +546,18 @@ __global__ void __launch_bounds__(256, 8) e3_band_kernel(const FusedArgs<R> a, c
   if (band_coords(bd, k)) e3_point<R, POLES, FX, FY, FZ>(a, k);
 }
 
+// slab bands keep more operands in flight per point (every load issued
+// before the branches): 40 registers there (64 in FP64), 32 in the rows
 template <typename R, bool CND, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256, 8) b3_band_kernel(const FusedArgs<R> a, const Band bd) {
+__global__ void __launch_bounds__(256, (FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8)
+    b3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];
   if (band_coords(bd, k)) b3_point<R, CND, FX, FY, FZ>(a, k);
 }
 
 template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256, 8) de3_band_kernel(const FusedArgs<R> a, const Band bd) {
+__global__ void __launch_bounds__(256, (FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8)
+    de3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];
   if (band_coords(bd, k)) de3_point<R, CND, POLES, FX, FY, FZ>(a, k);
 }
