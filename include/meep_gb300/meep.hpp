@@ -559,8 +559,10 @@ public:
   int vc;     // equivalent source component (near2far), else c
   int monitor_id;
   fields *fld;
+  std::complex<double> extra_weight; // weight of the force sum (dft_force)
   dft_chunk()
-      : c(Ex), N(0), dft(nullptr), next_in_dft(nullptr), vc(Ex), monitor_id(-1), fld(nullptr) {}
+      : c(Ex), N(0), dft(nullptr), next_in_dft(nullptr), vc(Ex), monitor_id(-1), fld(nullptr),
+        extra_weight(1.0) {}
   ~dft_chunk() { delete[] dft; }
   // multiply the sums of this chunk and the chunks after it (device sums)
   void scale_dft(std::complex<double> scale);
@@ -617,6 +619,19 @@ public:
   direction periodic_d[2];
   int periodic_n[2];
   double periodic_k[2], period[2];
+};
+
+// Maxwell-stress force on surfaces (src/stress.cpp): created by
+// fields::add_dft_force
+class dft_force {
+public:
+  dft_force(dft_chunk *offdiag1, dft_chunk *offdiag2, dft_chunk *diag, const double *freq, size_t Nfreq,
+            const volume &where);
+  double *force(); // newly allocated, Nfreq values
+  void scale_dfts(std::complex<double> scale);
+  std::vector<double> freq;
+  dft_chunk *offdiag1, *offdiag2, *diag;
+  volume where;
 };
 
 // homogeneous-medium Green's functions (src/near2far.cpp:131-245), on the GPU
@@ -692,6 +707,10 @@ public:
                                 int decimation_factor = 0, int Nperiods = 1);
   dft_near2far add_dft_near2far(const volume_list *where, const double *freq, size_t Nfreq,
                                 int decimation_factor = 0, int Nperiods = 1);
+  dft_force add_dft_force(const volume_list *where, double freq_min, double freq_max, int Nfreq,
+                          int decimation_factor = 0);
+  dft_force add_dft_force(const volume_list *where, const std::vector<double> &freq, int decimation_factor = 0);
+  dft_force add_dft_force(const volume_list *where, const double *freq, size_t Nfreq, int decimation_factor = 0);
   // trace-averaged permittivity / permeability at loc (src/monitor.cpp:172-194)
   std::complex<double> get_eps(const vec &loc, double frequency = 0) const;
   std::complex<double> get_mu(const vec &loc, double frequency = 0) const;

@@ -72,6 +72,11 @@ double mgb_last_source_time(const mgb_sim *s);
 int mgb_add_flux(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
                  int *handle);
 int mgb_flux(mgb_sim *s, int handle, double *out);
+/* Maxwell-stress force (fields::add_dft_force): regions as for mgb_add_flux,
+ * direction = the force's direction; mgb_force gives nfreq values */
+int mgb_add_force(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                  int *handle);
+int mgb_force(mgb_sim *s, int handle, double *out);
 /* near-to-far surfaces: regions as for mgb_add_flux; nperiods > 1 sums
  * lattice images along periodic directions (fields::add_dft_near2far) */
 int mgb_add_near2far(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,

@@ -100,7 +100,9 @@ int mfd_add_source_points(mfd_sim *sim, int c, int src_id, size_t npts, const in
 /* DFT monitor on component c over the box lo[d]..hi[d] (point indices of the
  * component grid, inclusive).  w[d] holds hi[d]-lo[d]+1 per-point weights for
  * each present direction (the reference's IVEC_LOOP_WEIGHT factors), dV the
- * volume element, scale the complex stored weight.  centered != 0 averages the
+ * volume element, scale the complex stored weight.  include_weights: 0 none,
+ * 1 the weight product, 2 its square root (sqrt_dV_and_interp_weights, used
+ * by the diagonal stress-tensor terms of add_dft_force).  centered != 0 averages the
  * Yee values onto the centred grid (yee2cent_offsets).  Replaces
  * fields::add_dft src/dft.cpp:175-235 / dft_chunk src/dft.cpp:266-308.
  * Returns monitor id in *id. */

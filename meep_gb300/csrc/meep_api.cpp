@@ -1033,7 +1033,8 @@ static int auto_decimation(fields &f, const double *freq, size_t Nfreq) {
 static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const double *freq,
                               size_t Nfreq, bool include_dV_and_interp_weights,
                               std::complex<double> stored_weight, dft_chunk *next,
-                              bool use_centered_grid, int decimation_factor, int vc = -1) {
+                              bool use_centered_grid, int decimation_factor, int vc = -1,
+                              bool sqrt_dV_and_interp_weights = false, std::complex<double> extra_weight = 1.0) {
   fields::impl &I = *f.d;
   if (component_direction(c) > Z) return next;
   if (!I.components) meep::abort("allocate field components (by adding sources) before adding dft objects");
@@ -1068,11 +1069,13 @@ static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const
   std::complex<double> scale = stored_weight * img.phase *
                                (f.dt / std::sqrt(2.0 * pi) * decimation_factor);
   int id = -1;
-  chk(mfd_add_dft(I.sim, mc, lo, hi, wp, L.dV0, include_dV_and_interp_weights ? 1 : 0, scale.real(),
+  const int incl = include_dV_and_interp_weights ? (sqrt_dV_and_interp_weights ? 2 : 1) : 0;
+  chk(mfd_add_dft(I.sim, mc, lo, hi, wp, L.dV0, incl, scale.real(),
                   scale.imag(), use_centered_grid ? 1 : 0, Nfreq, freq, decimation_factor, &id));
   std::unique_ptr<dft_chunk> ch(new dft_chunk);
   ch->c = c;
   ch->vc = vc < 0 ? int(c) : vc;
+  ch->extra_weight = extra_weight;
   ch->monitor_id = id;
   ch->fld = &f;
   ch->is = L.is;
@@ -1672,6 +1675,90 @@ void green2d(std::complex<double> *EH, const vec &x, double freq, double eps, do
              component c0, std::complex<double> f0) {
   if (x.dim != D2) meep::abort("wrong dimensionality in green2d");
   green_call(2, EH, x, freq, eps, mu, x0, c0, f0);
+}
+
+/* -------------------------------------------------------- stress / force */
+// fields::add_dft_force (src/stress.cpp:139-196): on a surface with normal n,
+// the force along f is the Maxwell stress integral.  f != n: E_f E_n* +
+// H_f H_n* (offdiag1 with dV weights and the surface weight, offdiag2
+// without); f == n: (+1/2 along f, -1/2 across) |E_d|^2 + |H_d|^2 over every
+// field direction d, each chunk with the square root of its dV weight and
+// the +-1/2 as its extra weight.
+dft_force fields::add_dft_force(const volume_list *where, const double *freq, size_t Nfreq, int decimation_factor) {
+  dft_chunk *offdiag1 = nullptr, *offdiag2 = nullptr, *diag = nullptr;
+  if (!where) return dft_force(offdiag1, offdiag2, diag, freq, Nfreq, volume(gv.center()));
+  volume everywhere = where->v;
+  for (const volume_list *w = where; w; w = w->next) {
+    const direction nd = normal_direction(w->v);
+    if (nd == NO_DIRECTION) meep::abort("cannot determine dft_force normal");
+    const direction fd = w->c >= Sx ? component_direction(derived_component(w->c)) : component_direction(component(w->c));
+    if (fd == NO_DIRECTION) meep::abort("NO_DIRECTION dft_force is invalid");
+    if (fd > Z) meep::abort("coordinate-type mismatch in add_dft_force");
+    if (fd != nd) {
+      offdiag1 = add_dft_one(*this, direction_component(Ex, fd), w->v, freq, Nfreq, true, w->weight, offdiag1, true,
+                             decimation_factor);
+      offdiag2 = add_dft_one(*this, direction_component(Ex, nd), w->v, freq, Nfreq, false, 1.0, offdiag2, true,
+                             decimation_factor);
+      offdiag1 = add_dft_one(*this, direction_component(Hx, fd), w->v, freq, Nfreq, true, w->weight, offdiag1, true,
+                             decimation_factor);
+      offdiag2 = add_dft_one(*this, direction_component(Hx, nd), w->v, freq, Nfreq, false, 1.0, offdiag2, true,
+                             decimation_factor);
+    }
+    else
+      for (int q = X; q <= Z; q++) {
+        const direction d = direction(q);
+        const std::complex<double> weight1 = w->weight * (d == fd ? +0.5 : -0.5);
+        diag = add_dft_one(*this, direction_component(Ex, d), w->v, freq, Nfreq, true, 1.0, diag, false,
+                           decimation_factor, -1, true, weight1);
+        diag = add_dft_one(*this, direction_component(Hx, d), w->v, freq, Nfreq, true, 1.0, diag, false,
+                           decimation_factor, -1, true, weight1);
+      }
+    everywhere = everywhere | w->v;
+  }
+  return dft_force(offdiag1, offdiag2, diag, freq, Nfreq, everywhere);
+}
+
+dft_force fields::add_dft_force(const volume_list *where, double freq_min, double freq_max, int Nfreq,
+                                int decimation_factor) {
+  std::vector<double> fr = linspace(freq_min, freq_max, Nfreq);
+  return add_dft_force(where, fr.data(), fr.size(), decimation_factor);
+}
+
+dft_force fields::add_dft_force(const volume_list *where, const std::vector<double> &freq, int decimation_factor) {
+  return add_dft_force(where, freq.data(), freq.size(), decimation_factor);
+}
+
+dft_force::dft_force(dft_chunk *offdiag1_, dft_chunk *offdiag2_, dft_chunk *diag_, const double *freq_, size_t Nfreq,
+                     const volume &where_)
+    : freq(freq_, freq_ + Nfreq), offdiag1(offdiag1_), offdiag2(offdiag2_), diag(diag_), where(where_) {}
+
+// dft_force::force (src/stress.cpp:84-96): sum over chunk pairs of
+// Re(extra_weight F1 conj(F2)); each pair reduced on the GPU (mfd_flux)
+double *dft_force::force() {
+  const size_t nf = freq.size();
+  double *F = new double[nf];
+  for (size_t i = 0; i < nf; i++)
+    F[i] = 0;
+  std::vector<double> part(nf);
+  auto pairs = [&](dft_chunk *a, dft_chunk *b) {
+    for (; a && b; a = a->next_in_dft, b = b->next_in_dft) {
+      const int ia = a->monitor_id, ib = b->monitor_id;
+      chk(mfd_flux(a->fld->d->sim, 1, &ia, &ib, part.data()));
+      // Re(w z) with z = sum F1 conj(F2) real for the diagonal (F1 = F2) and
+      // w = 1 off the diagonal
+      for (size_t i = 0; i < nf; i++)
+        F[i] += a->extra_weight.real() * part[i];
+    }
+  };
+  pairs(offdiag1, offdiag2);
+  pairs(diag, diag);
+  return F;
+}
+
+void dft_force::scale_dfts(std::complex<double> scale) {
+  if (offdiag1) offdiag1->scale_dft(scale);
+  if (offdiag2) offdiag2->scale_dft(scale);
+  if (diag) diag->scale_dft(scale);
 }
 
 } // namespace meep

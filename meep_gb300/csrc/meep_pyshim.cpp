@@ -165,6 +165,7 @@ struct mgb_sim {
   std::vector<dft_flux> fluxes;
   std::vector<dft_fields> dfts;
   std::vector<dft_near2far> n2fs;
+  std::vector<dft_force> forces;
 };
 
 // rows of (center[3], size[3], direction or -1, weight) as a volume_list;
@@ -286,6 +287,31 @@ int mgb_flux(mgb_sim *s, int handle, double *out) {
     double *F = s->fluxes[handle].flux();
     for (size_t i = 0; i < s->fluxes[handle].freq.size(); i++)
       out[i] = F[i];
+    delete[] F;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_add_force(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                  int *handle) {
+  try {
+    if (!s || !regions || !freqs || !handle || nreg < 1) throw std::runtime_error("null argument");
+    std::unique_ptr<volume_list> head = region_list(s, nreg, regions);
+    s->forces.push_back(s->f->add_dft_force(head.get(), freqs, (size_t)nfreq, decimation));
+    *handle = (int)s->forces.size() - 1;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_force(mgb_sim *s, int handle, double *out) {
+  try {
+    if (!s || !out || handle < 0 || handle >= (int)s->forces.size()) throw std::runtime_error("bad force handle");
+    double *F = s->forces[handle].force();
+    std::copy(F, F + s->forces[handle].freq.size(), out);
     delete[] F;
     return 0;
   } catch (const std::exception &e) {

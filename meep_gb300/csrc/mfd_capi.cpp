@@ -193,7 +193,9 @@ int mfd_add_dft(mfd_sim *s, int c, const int lo[3], const int hi[3], const doubl
     }
   }
   m.dV = dV;
+  need(include_weights >= 0 && include_weights <= 2, "include_weights must be 0, 1 or 2");
   m.include_weights = include_weights != 0;
+  m.sqrt_weights = include_weights == 2;
   m.scale = {scale_re, scale_im};
   m.centered = centered != 0;
   m.freq.assign(freq, freq + nfreq);
@@ -296,8 +298,10 @@ int mfd_backward(mfd_sim *s, int nmon, const int *ids, const double *const *grad
   need(s->fwd_t0 >= 0, "call mfd_forward before mfd_backward");
   need(nmon >= 0 && (nmon == 0 || (ids && grads)), "invalid monitor gradients");
   Plan &p = *s->plan;
-  for (int q = 0; q < nmon; q++)
+  for (int q = 0; q < nmon; q++) {
     need(ids[q] >= 0 && ids[q] < (int)p.monitors.size(), "unknown monitor id");
+    need(!p.monitors[ids[q]].sqrt_weights, "monitors with square-root weights (force) have no adjoint here");
+  }
   Backend &be = *s->be;
   be.begin_steps();
   be.adjoint_begin(p, nmon, ids, grads);

@@ -411,6 +411,7 @@ template <typename R> struct DftArgs {
   const double *w[3];
   double dV;
   int include_weights;
+  int sqrt_w; // the square root of the weight product
   int dim;
   int lo[3], n[3];
   int ad0, ad1; // averaging directions (-1 none)
@@ -453,6 +454,7 @@ template <typename R> __device__ __forceinline__ R dft_point_value(const Geo &g,
     if (a.dim == 2) wgt = wy * (wx * (a.dV * 1.0));
     else if (a.dim == 3) wgt = wz * (wy * (a.dV * wx));
     else wgt = 1.0 * (1.0 * (a.dV * wz));
+    if (a.sqrt_w) wgt = sqrt(wgt);
   }
   if (a.ad1 >= 0) {
     int k1[3] = {k[0], k[1], k[2]}, k2[3] = {k[0], k[1], k[2]}, k3[3] = {k[0], k[1], k[2]};
@@ -1824,6 +1826,7 @@ public:
     }
     a.dV = m.dV;
     a.include_weights = m.include_weights;
+    a.sqrt_w = m.sqrt_weights;
     a.dim = p.g.dim;
     a.ad0 = a.ad1 = -1;
     if (m.centered)

@@ -87,6 +87,7 @@ struct Monitor {
   std::vector<double> w[3]; // per present direction
   double dV = 1.0;
   bool include_weights = true;
+  bool sqrt_weights = false; // the square root of the weight product (sqrt_dV_and_interp_weights)
   std::complex<double> scale{1, 0};
   bool centered = false;
   std::vector<double> freq;

@@ -269,8 +269,10 @@ class FluxRegion:
         self.direction, self.weight = direction, complex(weight)
 
 
-# near-to-far surfaces are flux regions (python/simulation.py: Near2FarRegion = FluxRegion)
+# near-to-far and force surfaces are flux regions (python/simulation.py:
+# Near2FarRegion = FluxRegion; a ForceRegion's direction is the force's)
 Near2FarRegion = FluxRegion
+ForceRegion = FluxRegion
 
 
 # ------------------------------------------------------------ step funcs
@@ -381,6 +383,8 @@ _SIGS = [
     ("mgb_get_epsilon_points", C.c_int, [_P, C.c_int, _DP, _DP]),
     ("mgb_yee_array", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     ("mgb_use_bloch", C.c_int, [_P, _DP]),
+    ("mgb_add_force", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
+    ("mgb_force", C.c_int, [_P, C.c_int, _DP]),
     ("mgb_add_near2far", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("mgb_near2far_points", C.c_int, [_P, C.c_int, C.c_int, _DP, _DP]),
     ("mgb_near2far_array", C.c_int, [_P, C.c_int, _DP, _DP, C.c_double, _DP, C.POINTER(C.c_int),
@@ -420,6 +424,11 @@ class DftFlux:
 class DftFields:
     def __init__(self, sim, handle, freq, components):
         self.sim, self.handle, self.freq, self.components = sim, handle, list(freq), list(components)
+
+
+class DftForce:
+    def __init__(self, sim, handle, freq):
+        self.sim, self.handle, self.freq = sim, handle, list(freq)
 
 
 class DftNear2Far:
@@ -615,6 +624,27 @@ class Simulation:
         self.dft_objects.append(flux)
         return flux
 
+    def add_force(self, *args, **kwargs):
+        """add_force(fcen, df, nfreq | freq, *ForceRegions, decimation_factor=0):
+        the Maxwell-stress force along each region's direction
+        (python/simulation.py Simulation.add_force)."""
+        args = _fix_dft_args(args, 0)
+        freq, regions = list(np.asarray(args[0], dtype=np.float64)), args[1:]
+        decimation = int(kwargs.get("decimation_factor", 0))
+        self.init_sim()
+        rows = []
+        for r in regions:
+            if r.weight.imag != 0:
+                raise NotImplementedError("meep: complex force weights are not supported")
+            rows += list(r.center) + list(r.size) + [r.direction, r.weight.real]
+        r_a, r_p = _arr(rows)
+        f_a, f_p = _arr(freq)
+        h = C.c_int()
+        self._check(self._lib.mgb_add_force(self._h, len(regions), r_p, len(freq), f_p, decimation, C.byref(h)))
+        force = DftForce(self, h.value, freq)
+        self.dft_objects.append(force)
+        return force
+
     def add_near2far(self, *args, **kwargs):
         """add_near2far(fcen, df, nfreq | freq, *Near2FarRegions, nperiods=1,
         decimation_factor=0): the DFTs of the tangential fields on the regions
@@ -761,7 +791,9 @@ class Simulation:
             n = self._steps_until(min(stops))
             self._check(self._lib.mgb_step(self._h, n))
         else:
-            while not (any(self.round_time() >= s for s in stops) or any(f(self) for f in funcs)):
+            # every condition is evaluated on every step, as the reference's
+            # list comprehension does (stateful conditions sample each step)
+            while not any([self.round_time() >= s for s in stops] + [f(self) for f in funcs]):
                 for func in step_funcs:
                     _eval_step_func(self, func, "step")
                 self._check(self._lib.mgb_step(self._h, 1))
@@ -779,7 +811,7 @@ class Simulation:
             if isinstance(c, numbers.Number):
                 new.append((ts - self.round_time()) + c)
             else:
-                new.append(lambda sim, c=c: sim.round_time() >= ts and c(sim))
+                new.append(lambda sim, c=c: c(sim) and sim.round_time() >= ts)
         self._run_until(new, step_funcs)
 
     def run(self, *step_funcs, until=None, until_after_sources=None):
@@ -868,3 +900,40 @@ def get_near2far_freqs(f):
 
 def scale_near2far_fields(s, near2far):
     near2far.scale_dfts(s)
+
+
+def stop_when_fields_decayed(dt=None, c=None, pt=None, decay_by=None, sampling_interval=1):
+    """Condition for Simulation.run: keep running in windows of dt time units
+    until the largest |c(pt)|^2 of the last window is below decay_by times
+    the largest of all earlier windows (python/simulation.py
+    stop_when_fields_decayed); the field is sampled every sampling_interval
+    steps."""
+    if dt is None or c is None or pt is None or decay_by is None:
+        raise ValueError("dt, c, pt, and decay_by are all required.")
+    if not isinstance(sampling_interval, numbers.Integral) or sampling_interval < 1:
+        raise ValueError("sampling_interval must be a positive integer.")
+    state = {"max_abs": 0, "cur_max": 0, "t0": 0}
+
+    def _stop(sim):
+        if sim.timestep() % sampling_interval == 0:
+            state["cur_max"] = max(state["cur_max"], abs(sim.get_field_point(c, pt)) ** 2)
+        if sim.round_time() <= dt + state["t0"]:
+            return False
+        old = state["cur_max"]
+        state["cur_max"] = 0
+        state["t0"] = sim.round_time()
+        state["max_abs"] = max(state["max_abs"], old)
+        return old <= state["max_abs"] * decay_by
+
+    return _stop
+
+
+def get_forces(f):
+    sim = f.sim
+    out = np.zeros(len(f.freq))
+    sim._check(sim._lib.mgb_force(sim._h, f.handle, out.ctypes.data_as(_DP)))
+    return list(out)
+
+
+def get_force_freqs(f):
+    return list(f.freq)

@@ -488,6 +488,7 @@ public:
             if (p.g.dim == 2) wgt = wy * (wx * (m.dV * 1.0));
             else if (p.g.dim == 3) wgt = wz * (wy * (m.dV * wx));
             else wgt = 1.0 * (1.0 * (m.dV * wz));
+            if (m.sqrt_weights) wgt = std::sqrt(wgt); // src/dft.cpp:279-280
           }
           R fv, fvi = R(0);
           if (cplx) {

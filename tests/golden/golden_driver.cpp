@@ -1086,6 +1086,77 @@ static void case_py_n2f(Writer &w) {
   delete[] EH;
 }
 
+// run(until_after_sources=stop_when_fields_decayed(dt, c, pt, decay_by))
+// (python/simulation.py:5275-5336 with _run_sources_until :2866-2885): the
+// condition samples |c(pt)|^2 on every step and stops once the largest value
+// of the last dt window is below decay_by times the largest before it, and
+// the sources are off
+static void py_run_until_after_sources_decayed(fields &f, double dt, component c, const vec &pt, double decay_by) {
+  double max_abs = 0, cur_max = 0, t0 = 0;
+  const double ts = f.last_source_time();
+  auto stop = [&]() {
+    const double a = std::abs(f.get_field(c, pt));
+    cur_max = std::max(cur_max, a * a);
+    if (f.round_time() <= dt + t0) return false;
+    const double old = cur_max;
+    cur_max = 0;
+    t0 = f.round_time();
+    max_abs = std::max(max_abs, old);
+    return old <= max_abs * decay_by;
+  };
+  while (!(stop() && f.round_time() >= ts))
+    f.step();
+}
+
+/* Script (the reference's python/tests/test_force.py test_force):
+     sim = mp.Simulation(resolution=20, cell_size=mp.Vector3(10, 10), boundary_layers=[mp.PML(1.0)],
+                         sources=[mp.Source(mp.GaussianSource(1.0, fwidth=1.0), center=mp.Vector3(),
+                                            component=mp.Ez)])
+     fr = mp.ForceRegion(center=mp.Vector3(0, 1.27), direction=mp.Y, size=mp.Vector3(4.38, 0))
+     force = sim.add_force(1.0, 0, 1, fr, decimation_factor=1)
+     force_decimated = sim.add_force(1.0, 0, 1, fr, decimation_factor=10)
+     sim.run(until_after_sources=mp.stop_when_fields_decayed(50, mp.Ez, mp.Vector3(), 1e-6))
+   (its golden master: get_forces(force)[0] = -0.11039089113393187) */
+static void case_py_force(Writer &w) {
+  grid_volume gv = vol2d(10, 10, 20);
+  gv.center_origin();
+  structure s(gv, one_eps, pml(1.0), identity(), 0, 0.5, true);
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 1.0);
+  gaussian_src_time src(1.0, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, volume(vec(0, 0), vec(0, 0)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = {1.0};
+  volume_list r(volume(vec(-2.19, 1.27), vec(2.19, 1.27)), Sy, 1.0);
+  dft_force force = f.add_dft_force(&r, fr.data(), fr.size(), 1);
+  dft_force force_dec = f.add_dft_force(&r, fr.data(), fr.size(), 10);
+  // and the test's fr_box: force along x on the four sides of a 2 x 2 box
+  // (diagonal stress terms on the x sides, off-diagonal on the y sides)
+  volume_list *box = nullptr;
+  const double bc[4][2] = {{1.0, 0}, {-1.0, 0}, {0, 1.0}, {0, -1.0}}, bw[4] = {1.0, -1.0, 1.0, -1.0};
+  for (int q = 0; q < 4; q++) {
+    const double hx = q < 2 ? 0.0 : 1.0, hy = q < 2 ? 1.0 : 0.0;
+    box = new volume_list(volume(vec(bc[q][0] - hx, bc[q][1] - hy), vec(bc[q][0] + hx, bc[q][1] + hy)), Sx, bw[q],
+                          box);
+  }
+  dft_force force_box = f.add_dft_force(box, fr.data(), fr.size(), 1);
+  delete box;
+  py_run_until_after_sources_decayed(f, 50, Ez, vec(0, 0), 1e-6);
+  sync_dfts(f);
+  double *F = force.force();
+  w.scalar("force", F[0]);
+  delete[] F;
+  F = force_dec.force();
+  w.scalar("force_dec", F[0]);
+  delete[] F;
+  F = force_box.force();
+  w.scalar("force_box", F[0]);
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ez", global_field(f, gv, Ez));
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -1135,6 +1206,8 @@ int main(int argc, char **argv) {
     case_n2f(w, D2, Ex, Hz, steps > 0 ? steps : 2800);
   else if (cs == "n2f3d")
     case_n2f(w, D3, Ez, Hx, steps > 0 ? steps : 900);
+  else if (cs == "py_force")
+    case_py_force(w);
   else if (cs == "py_n2f")
     case_py_n2f(w);
   else if (cs == "n2f_periodic2d")
