@@ -587,7 +587,14 @@ public:
   fields *f;
   dft_flux() : E(nullptr), H(nullptr), cE(Ex), cH(Hy), f(nullptr) {}
   double *flux();
+  void scale_dfts(std::complex<double> scale);
 };
+
+// the DFT sums of a chunk list as one array, chunk after chunk (the layout
+// of the reference's Python get_dft_data / load_dft_data helpers)
+size_t dft_data_size(dft_chunk *chunks);
+void get_dft_data(dft_chunk *chunks, std::complex<double> *data, size_t n);
+void load_dft_data(dft_chunk *chunks, const std::complex<double> *data, size_t n);
 
 /* Near-to-far transform (src/near2far.cpp): DFT chunks of the tangential
    fields on closed or open surfaces in a homogeneous medium; far fields by

@@ -72,6 +72,12 @@ double mgb_last_source_time(const mgb_sim *s);
 int mgb_add_flux(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
                  int *handle);
 int mgb_flux(mgb_sim *s, int handle, double *out);
+/* the DFT sums of a flux's E (part 0) or H (part 1) chunks as one array of
+ * *n complex values (re/im); out NULL gives only *n.  load replaces them
+ * (n must match); scale multiplies both (dft_flux::scale_dfts) */
+int mgb_flux_data(mgb_sim *s, int handle, int part, double *out, size_t *n);
+int mgb_load_flux_data(mgb_sim *s, int handle, int part, const double *in, size_t n);
+int mgb_flux_scale(mgb_sim *s, int handle, double re, double im);
 /* Maxwell-stress force (fields::add_dft_force): regions as for mgb_add_flux,
  * direction = the force's direction; mgb_force gives nfreq values */
 int mgb_add_force(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,

@@ -127,6 +127,12 @@ int mfd_get_dft(mfd_sim *sim, int id, double *out, size_t *npts, size_t *nfreq);
  * src/dft.cpp:542-556. out has nfreq entries. */
 int mfd_flux(mfd_sim *sim, int npairs, const int *idE, const int *idH, double *out);
 
+/* Replace the sums of monitor `id` by in (npts*nfreq*(re,im), the layout of
+ * mfd_get_dft).  Replaces the chunk loop of _load_dft_data
+ * python/meep.i:511-527 (Simulation.load_flux_data / load_minus_flux_data);
+ * sums accumulated by later steps add to these values. */
+int mfd_set_dft(mfd_sim *sim, int id, const double *in);
+
 /* Multiply the sums of monitor `id` by (s_re + i s_im).  Replaces
  * dft_chunk::scale_dft src/dft.cpp:402-406 (dft_near2far::scale_dfts
  * src/near2far.cpp:124-126, dft_flux::scale_dfts). */

@@ -1761,4 +1761,43 @@ void dft_force::scale_dfts(std::complex<double> scale) {
   if (diag) diag->scale_dft(scale);
 }
 
+/* ------------------------------------------------- DFT data save / load */
+void dft_flux::scale_dfts(std::complex<double> scale) {
+  if (E) E->scale_dft(scale);
+  if (H) H->scale_dft(scale);
+}
+
+size_t dft_data_size(dft_chunk *chunks) {
+  size_t n = 0;
+  for (dft_chunk *c = chunks; c; c = c->next_in_dft)
+    n += c->N * c->omega.size();
+  return n;
+}
+
+// _get_dft_data / _load_dft_data (python/meep.i:492-527): the chunks' sums
+// in list order
+void get_dft_data(dft_chunk *chunks, std::complex<double> *data, size_t n) {
+  if (n != dft_data_size(chunks))
+    meep::abort("Total dft_chunks size does not agree with size allocated for output array.\n");
+  size_t at = 0;
+  for (dft_chunk *c = chunks; c; c = c->next_in_dft) {
+    size_t np = 0, nf = 0;
+    chk(mfd_get_dft(c->fld->d->sim, c->monitor_id, reinterpret_cast<double *>(data + at), &np, &nf));
+    at += np * nf;
+  }
+}
+
+void load_dft_data(dft_chunk *chunks, const std::complex<double> *data, size_t n) {
+  if (n != dft_data_size(chunks))
+    meep::abort("Total dft_chunks size does not agree with size allocated for output array.\n");
+  size_t at = 0;
+  for (dft_chunk *c = chunks; c; c = c->next_in_dft) {
+    const size_t m = c->N * c->omega.size();
+    chk(mfd_set_dft(c->fld->d->sim, c->monitor_id, reinterpret_cast<const double *>(data + at)));
+    for (size_t i = 0; i < m; i++)
+      c->dft[i] = std::complex<realnum>(realnum(data[at + i].real()), realnum(data[at + i].imag()));
+    at += m;
+  }
+}
+
 } // namespace meep

@@ -294,6 +294,44 @@ int mgb_flux(mgb_sim *s, int handle, double *out) {
   }
 }
 
+static dft_chunk *flux_part(mgb_sim *s, int handle, int part) {
+  if (!s || handle < 0 || handle >= (int)s->fluxes.size() || part < 0 || part > 1)
+    throw std::runtime_error("bad flux handle");
+  return part == 0 ? s->fluxes[handle].E : s->fluxes[handle].H;
+}
+
+int mgb_flux_data(mgb_sim *s, int handle, int part, double *out, size_t *n) {
+  try {
+    dft_chunk *c = flux_part(s, handle, part);
+    if (!n) throw std::runtime_error("null argument");
+    *n = dft_data_size(c);
+    if (out) get_dft_data(c, reinterpret_cast<std::complex<double> *>(out), *n);
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_load_flux_data(mgb_sim *s, int handle, int part, const double *in, size_t n) {
+  try {
+    if (!in) throw std::runtime_error("null argument");
+    load_dft_data(flux_part(s, handle, part), reinterpret_cast<const std::complex<double> *>(in), n);
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_flux_scale(mgb_sim *s, int handle, double re, double im) {
+  try {
+    if (!s || handle < 0 || handle >= (int)s->fluxes.size()) throw std::runtime_error("bad flux handle");
+    s->fluxes[handle].scale_dfts(std::complex<double>(re, im));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
 int mgb_add_force(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
                   int *handle) {
   try {

@@ -53,6 +53,8 @@ public:
   virtual void get_field_im(Plan &p, int c, double *out_dense) = 0;
   virtual void get_dft(Plan &p, int id, double *out) = 0;
   virtual void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) = 0;
+  // replace the DFT sums of monitor id (npts * nfreq complex, re/im)
+  virtual void set_dft(Plan &p, int id, const double *in) = 0;
   // multiply the DFT sums of monitor id by s (dft_chunk::scale_dft)
   virtual void scale_dft(Plan &p, int id, std::complex<double> s) = 0;
   // far fields (6 complex values per far point and frequency, point-major,

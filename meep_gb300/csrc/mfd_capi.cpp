@@ -450,6 +450,18 @@ int mfd_scale_dft(mfd_sim *s, int id, double s_re, double s_im) {
   MFD_CATCH
 }
 
+int mfd_set_dft(mfd_sim *s, int id, const double *in) {
+  MFD_TRY
+  need(s && s->plan && in, "null argument");
+  Plan &p = *s->plan;
+  need(id >= 0 && id < (int)p.monitors.size(), "unknown monitor id");
+  // the sums live in the backend once it is set up: set it up now (the
+  // reference loads flux data before the run, after the sources and monitors)
+  ensure_setup(s);
+  s->be->set_dft(p, id, in);
+  MFD_CATCH
+}
+
 int mfd_farfield(mfd_sim *s, int nsheet, const int *ids, const int *src_comp, const double *is_half,
                  const double *rshift, double eps, double mu, const int periodic_dir[2], const int periodic_n[2],
                  const double periodic_k[2], const double period[2], int64_t nx, const double *x, double *out) {

@@ -2342,6 +2342,16 @@ public:
     check_tc();
   }
 
+  void set_dft(Plan &p, int id, const double *in) override {
+    dft_flush(p, id);
+    const Monitor &m = p.monitors[id];
+    cuda_check(cudaMemcpyAsync(mons[id].acc, in, m.npts * m.freq.size() * sizeof(double2), cudaMemcpyHostToDevice,
+                               stream),
+               "upload dft");
+    cuda_check(cudaStreamSynchronize(stream), "upload dft sync");
+    check_tc();
+  }
+
   void scale_dft(Plan &p, int id, std::complex<double> sc) override {
     dft_flush(p, id);
     const Monitor &m = p.monitors[id];

@@ -31,6 +31,7 @@ fields when it is nonzero), as in the reference.
     sim.run(until_after_sources=200)
     print(mp.get_fluxes(flux))
 """
+import collections
 import ctypes as C
 import math
 import numbers
@@ -383,6 +384,9 @@ _SIGS = [
     ("mgb_get_epsilon_points", C.c_int, [_P, C.c_int, _DP, _DP]),
     ("mgb_yee_array", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     ("mgb_use_bloch", C.c_int, [_P, _DP]),
+    ("mgb_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_size_t)]),
+    ("mgb_load_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.c_size_t]),
+    ("mgb_flux_scale", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
     ("mgb_add_force", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
     ("mgb_force", C.c_int, [_P, C.c_int, _DP]),
     ("mgb_add_near2far", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
@@ -424,6 +428,10 @@ class DftFlux:
 class DftFields:
     def __init__(self, sim, handle, freq, components):
         self.sim, self.handle, self.freq, self.components = sim, handle, list(freq), list(components)
+
+
+# python/simulation.py FluxData: the E and H DFT sums of a flux object
+FluxData = collections.namedtuple("FluxData", ["E", "H"])
 
 
 class DftForce:
@@ -623,6 +631,32 @@ class Simulation:
         flux = DftFlux(self, h.value, freq)
         self.dft_objects.append(flux)
         return flux
+
+    def _flux_part(self, flux, part):
+        n = C.c_size_t()
+        self._check(self._lib.mgb_flux_data(self._h, flux.handle, part, None, C.byref(n)))
+        out = np.zeros(2 * n.value)
+        self._check(self._lib.mgb_flux_data(self._h, flux.handle, part, out.ctypes.data_as(_DP), C.byref(n)))
+        return out[0::2] + 1j * out[1::2]
+
+    def get_flux_data(self, flux):
+        """The flux object's DFT sums as FluxData(E, H) (complex arrays, chunk
+        after chunk), for load_flux_data / load_minus_flux_data."""
+        return FluxData(E=self._flux_part(flux, 0), H=self._flux_part(flux, 1))
+
+    def load_flux_data(self, flux, fdata):
+        """Replace the flux object's DFT sums by fdata (from get_flux_data of a
+        simulation with the same cell and regions); later steps add to them."""
+        for part, arr in ((0, fdata.E), (1, fdata.H)):
+            arr = np.asarray(arr, dtype=np.complex128)
+            ri = np.ascontiguousarray(np.stack([arr.real, arr.imag], axis=-1).reshape(-1))
+            self._check(self._lib.mgb_load_flux_data(self._h, flux.handle, part, ri.ctypes.data_as(_DP), arr.size))
+
+    def load_minus_flux_data(self, flux, fdata):
+        """As load_flux_data, then negate: the loaded fields are subtracted
+        from what the run accumulates (the reflected-flux normalisation)."""
+        self.load_flux_data(flux, fdata)
+        scale_flux_fields(-1.0, flux)
 
     def add_force(self, *args, **kwargs):
         """add_force(fcen, df, nfreq | freq, *ForceRegions, decimation_factor=0):
@@ -937,3 +971,9 @@ def get_forces(f):
 
 def get_force_freqs(f):
     return list(f.freq)
+
+
+def scale_flux_fields(s, flux):
+    """Multiply the flux object's DFT sums by the complex number s."""
+    s = complex(s)
+    flux.sim._check(flux.sim._lib.mgb_flux_scale(flux.sim._h, flux.handle, s.real, s.imag))

@@ -648,6 +648,13 @@ public:
     }
   }
 
+  void set_dft(Plan &p, int id, const double *in) override {
+    std::vector<std::complex<double>> &a = dft[id];
+    for (size_t i = 0; i < a.size(); i++)
+      a[i] = std::complex<double>(in[2 * i], in[2 * i + 1]);
+    (void)p;
+  }
+
   void scale_dft(Plan &p, int id, std::complex<double> s) override {
     for (auto &v : dft[id]) v *= s;
     (void)p;

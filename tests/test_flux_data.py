@@ -1,0 +1,71 @@
+"""Flux data save / load (the reference's Python get_flux_data,
+load_flux_data, load_minus_flux_data, scale_flux_fields; C ABI mfd_set_dft).
+
+The usual reflection normalisation: run A without the scatterer and keep the
+reflection plane's DFT sums; run B with the scatterer after
+load_minus_flux_data, so that its plane accumulates the scattered fields
+only; run C with the scatterer and nothing loaded.  B's sums must equal C's
+minus A's, and B's flux must be the flux of those differences."""
+import os
+
+import numpy as np
+import pytest
+
+import meep_gb300 as mp
+
+
+def relerr(a, b):
+    """max |a - b| / max |b| over complex values"""
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def _run(lib, scatterer, load=None, minus=True):
+    geometry = [mp.Block(mp.Vector3(0.6, 1.2, mp.inf), center=mp.Vector3(1.0, 0.1),
+                         material=mp.Medium(epsilon=12))] if scatterer else []
+    sim = mp.Simulation(cell_size=mp.Vector3(8, 4), resolution=10, geometry=geometry,
+                        boundary_layers=[mp.PML(1.0)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(0.5, fwidth=0.3), component=mp.Ez,
+                                           center=mp.Vector3(-2.5), size=mp.Vector3(y=2))], _library=lib)
+    refl = sim.add_flux(0.5, 0.3, 5, mp.FluxRegion(center=mp.Vector3(-1.5), size=mp.Vector3(y=2)))
+    tran = sim.add_flux(0.5, 0.3, 5, mp.FluxRegion(center=mp.Vector3(2.5), size=mp.Vector3(y=2)))
+    if load is not None:
+        (sim.load_minus_flux_data if minus else sim.load_flux_data)(refl, load)
+    sim.run(until_after_sources=20)
+    return sim.get_flux_data(refl), np.array(mp.get_fluxes(refl)), np.array(mp.get_fluxes(tran))
+
+
+def _check(lib, tol):
+    a, fa, _ = _run(lib, False)
+    c, fc, tc = _run(lib, True)
+    b, fb, tb = _run(lib, True, load=a)
+    assert relerr(b.E, c.E - a.E) <= tol and relerr(b.H, c.H - a.H) <= tol
+    flux_of_diff = np.real(((c.E - a.E) * np.conj(c.H - a.H)).reshape(-1, 5)).sum(axis=0)
+    assert relerr(fb, flux_of_diff) <= tol
+    assert relerr(tb, tc) <= tol  # the transmission plane is untouched
+    # the incident flux is positive at the reflection plane; the scattered
+    # flux there runs back towards the source
+    assert np.all(fa > 0) and np.all(fb < 0)
+    # load_flux_data (no negation) then scale by -1 is load_minus_flux_data
+    d, fd, _ = _run(lib, True, load=a, minus=False)
+    assert relerr(d.E, c.E + a.E) <= tol
+
+
+def test_flux_data_on_oracle(oracle_lib):
+    _check(os.path.join(os.path.dirname(oracle_lib), "liboracle_meep.so"), 1e-12)
+
+
+def test_load_rejects_wrong_size(oracle_lib):
+    lib = os.path.join(os.path.dirname(oracle_lib), "liboracle_meep.so")
+    a, _, _ = _run(lib, False)
+    with pytest.raises(RuntimeError, match="does not agree"):
+        _run(lib, True, load=mp.FluxData(E=a.E[:-1], H=a.H))
+
+
+@pytest.mark.gpu
+def test_flux_data_on_gpu(engine_lib):
+    """The same workflow on the CUDA engine (FP64 and FP32 fields)."""
+    from meep_gb300.simulation import PRODUCT_LIB
+    _check(PRODUCT_LIB, 1e-12)
+    _check(os.path.join(os.path.dirname(PRODUCT_LIB), "libmeep_gb300_single.so"), 1e-6)
