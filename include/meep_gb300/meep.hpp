@@ -628,6 +628,21 @@ public:
   double periodic_k[2], period[2];
 };
 
+// electric and magnetic energy density spectra in volumes (src/dft.cpp
+// dft_energy): created by fields::add_dft_energy
+class dft_energy {
+public:
+  dft_energy(dft_chunk *E, dft_chunk *H, dft_chunk *D, dft_chunk *B, const double *freq, size_t Nfreq,
+             const volume &where);
+  double *electric(); // newly allocated, Nfreq values
+  double *magnetic();
+  double *total();
+  void scale_dfts(std::complex<double> scale);
+  std::vector<double> freq;
+  dft_chunk *E, *H, *D, *B;
+  volume where;
+};
+
 // Maxwell-stress force on surfaces (src/stress.cpp): created by
 // fields::add_dft_force
 class dft_force {
@@ -714,6 +729,10 @@ public:
                                 int decimation_factor = 0, int Nperiods = 1);
   dft_near2far add_dft_near2far(const volume_list *where, const double *freq, size_t Nfreq,
                                 int decimation_factor = 0, int Nperiods = 1);
+  dft_energy add_dft_energy(const volume_list *where, double freq_min, double freq_max, int Nfreq,
+                            int decimation_factor = 0);
+  dft_energy add_dft_energy(const volume_list *where, const std::vector<double> &freq, int decimation_factor = 0);
+  dft_energy add_dft_energy(const volume_list *where, const double *freq, size_t Nfreq, int decimation_factor = 0);
   dft_force add_dft_force(const volume_list *where, double freq_min, double freq_max, int Nfreq,
                           int decimation_factor = 0);
   dft_force add_dft_force(const volume_list *where, const std::vector<double> &freq, int decimation_factor = 0);

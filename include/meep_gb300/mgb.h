@@ -78,6 +78,11 @@ int mgb_flux(mgb_sim *s, int handle, double *out);
 int mgb_flux_data(mgb_sim *s, int handle, int part, double *out, size_t *n);
 int mgb_load_flux_data(mgb_sim *s, int handle, int part, const double *in, size_t n);
 int mgb_flux_scale(mgb_sim *s, int handle, double re, double im);
+/* energy spectra (fields::add_dft_energy) over regions as for mgb_add_flux;
+ * mgb_energy: which 0 electric, 1 magnetic, 2 total, nfreq values */
+int mgb_add_energy(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                   int *handle);
+int mgb_energy(mgb_sim *s, int handle, int which, double *out);
 /* Maxwell-stress force (fields::add_dft_force): regions as for mgb_add_flux,
  * direction = the force's direction; mgb_force gives nfreq values */
 int mgb_add_force(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,

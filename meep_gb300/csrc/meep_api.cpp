@@ -1800,4 +1800,69 @@ void load_dft_data(dft_chunk *chunks, const std::complex<double> *data, size_t n
   }
 }
 
+/* ---------------------------------------------------------------- energy */
+// fields::add_dft_energy (src/dft.cpp:725-750): E, D, H, B of every field
+// direction on the centred grid, the dV weights on E and H
+dft_energy fields::add_dft_energy(const volume_list *where, const double *freq, size_t Nfreq, int decimation_factor) {
+  dft_chunk *E = nullptr, *D = nullptr, *H = nullptr, *B = nullptr;
+  if (!where) return dft_energy(E, H, D, B, freq, Nfreq, volume(gv.center()));
+  const volume firstvol(where->v);
+  for (const volume_list *w = where; w; w = w->next)
+    for (int q = X; q <= Z; q++) {
+      const direction d = direction(q);
+      E = add_dft_one(*this, direction_component(Ex, d), w->v, freq, Nfreq, true, 1.0, E, true, decimation_factor);
+      D = add_dft_one(*this, direction_component(Dx, d), w->v, freq, Nfreq, false, 1.0, D, true, decimation_factor);
+      H = add_dft_one(*this, direction_component(Hx, d), w->v, freq, Nfreq, true, 1.0, H, true, decimation_factor);
+      B = add_dft_one(*this, direction_component(Bx, d), w->v, freq, Nfreq, false, 1.0, B, true, decimation_factor);
+    }
+  return dft_energy(E, H, D, B, freq, Nfreq, firstvol);
+}
+
+dft_energy fields::add_dft_energy(const volume_list *where, double freq_min, double freq_max, int Nfreq,
+                                  int decimation_factor) {
+  std::vector<double> fr = linspace(freq_min, freq_max, Nfreq);
+  return add_dft_energy(where, fr.data(), fr.size(), decimation_factor);
+}
+
+dft_energy fields::add_dft_energy(const volume_list *where, const std::vector<double> &freq, int decimation_factor) {
+  return add_dft_energy(where, freq.data(), freq.size(), decimation_factor);
+}
+
+dft_energy::dft_energy(dft_chunk *E_, dft_chunk *H_, dft_chunk *D_, dft_chunk *B_, const double *freq_, size_t Nfreq,
+                       const volume &where_)
+    : freq(freq_, freq_ + Nfreq), E(E_), H(H_), D(D_), B(B_), where(where_) {}
+
+// 0.5 sum Re(conj(F1) F2) over the chunk pairs (src/dft.cpp:681-711): the
+// real part equals that of F1 conj(F2), the GPU flux reduction
+static double *energy_sum(const std::vector<double> &freq, dft_chunk *a, dft_chunk *b) {
+  const size_t nf = freq.size();
+  double *F = new double[nf];
+  for (size_t i = 0; i < nf; i++)
+    F[i] = 0;
+  std::vector<double> part(nf);
+  for (; a && b; a = a->next_in_dft, b = b->next_in_dft) {
+    const int ia = a->monitor_id, ib = b->monitor_id;
+    chk(mfd_flux(a->fld->d->sim, 1, &ia, &ib, part.data()));
+    for (size_t i = 0; i < nf; i++)
+      F[i] += 0.5 * part[i];
+  }
+  return F;
+}
+
+double *dft_energy::electric() { return energy_sum(freq, E, D); }
+double *dft_energy::magnetic() { return energy_sum(freq, H, B); }
+
+double *dft_energy::total() {
+  double *Fe = electric(), *Fm = magnetic();
+  for (size_t i = 0; i < freq.size(); i++)
+    Fe[i] += Fm[i];
+  delete[] Fm;
+  return Fe;
+}
+
+void dft_energy::scale_dfts(std::complex<double> scale) {
+  for (dft_chunk *c : {E, D, H, B})
+    if (c) c->scale_dft(scale);
+}
+
 } // namespace meep

@@ -166,6 +166,7 @@ struct mgb_sim {
   std::vector<dft_fields> dfts;
   std::vector<dft_near2far> n2fs;
   std::vector<dft_force> forces;
+  std::vector<dft_energy> energies;
 };
 
 // rows of (center[3], size[3], direction or -1, weight) as a volume_list;
@@ -326,6 +327,33 @@ int mgb_flux_scale(mgb_sim *s, int handle, double re, double im) {
   try {
     if (!s || handle < 0 || handle >= (int)s->fluxes.size()) throw std::runtime_error("bad flux handle");
     s->fluxes[handle].scale_dfts(std::complex<double>(re, im));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_add_energy(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,
+                   int *handle) {
+  try {
+    if (!s || !regions || !freqs || !handle || nreg < 1) throw std::runtime_error("null argument");
+    std::unique_ptr<volume_list> head = region_list(s, nreg, regions);
+    s->energies.push_back(s->f->add_dft_energy(head.get(), freqs, (size_t)nfreq, decimation));
+    *handle = (int)s->energies.size() - 1;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_energy(mgb_sim *s, int handle, int which, double *out) {
+  try {
+    if (!s || !out || handle < 0 || handle >= (int)s->energies.size() || which < 0 || which > 2)
+      throw std::runtime_error("bad energy handle");
+    dft_energy &e = s->energies[handle];
+    double *F = which == 0 ? e.electric() : which == 1 ? e.magnetic() : e.total();
+    std::copy(F, F + e.freq.size(), out);
+    delete[] F;
     return 0;
   } catch (const std::exception &e) {
     return fail(e);

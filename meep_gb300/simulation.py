@@ -274,6 +274,7 @@ class FluxRegion:
 # Near2FarRegion = FluxRegion; a ForceRegion's direction is the force's)
 Near2FarRegion = FluxRegion
 ForceRegion = FluxRegion
+EnergyRegion = FluxRegion
 
 
 # ------------------------------------------------------------ step funcs
@@ -387,6 +388,8 @@ _SIGS = [
     ("mgb_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_size_t)]),
     ("mgb_load_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.c_size_t]),
     ("mgb_flux_scale", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
+    ("mgb_add_energy", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
+    ("mgb_energy", C.c_int, [_P, C.c_int, C.c_int, _DP]),
     ("mgb_add_force", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
     ("mgb_force", C.c_int, [_P, C.c_int, _DP]),
     ("mgb_add_near2far", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
@@ -432,6 +435,16 @@ class DftFields:
 
 # python/simulation.py FluxData: the E and H DFT sums of a flux object
 FluxData = collections.namedtuple("FluxData", ["E", "H"])
+
+
+class DftEnergy:
+    def __init__(self, sim, handle, freq):
+        self.sim, self.handle, self.freq = sim, handle, list(freq)
+
+    def _get(self, which):
+        out = np.zeros(len(self.freq))
+        self.sim._check(self.sim._lib.mgb_energy(self.sim._h, self.handle, which, out.ctypes.data_as(_DP)))
+        return list(out)
 
 
 class DftForce:
@@ -657,6 +670,25 @@ class Simulation:
         from what the run accumulates (the reflected-flux normalisation)."""
         self.load_flux_data(flux, fdata)
         scale_flux_fields(-1.0, flux)
+
+    def add_energy(self, *args, **kwargs):
+        """add_energy(fcen, df, nfreq | freq, *EnergyRegions, decimation_factor=0):
+        electric and magnetic energy spectra in the regions
+        (python/simulation.py Simulation.add_energy)."""
+        args = _fix_dft_args(args, 0)
+        freq, regions = list(np.asarray(args[0], dtype=np.float64)), args[1:]
+        decimation = int(kwargs.get("decimation_factor", 0))
+        self.init_sim()
+        rows = []
+        for r in regions:
+            rows += list(r.center) + list(r.size) + [r.direction, r.weight.real]
+        r_a, r_p = _arr(rows)
+        f_a, f_p = _arr(freq)
+        h = C.c_int()
+        self._check(self._lib.mgb_add_energy(self._h, len(regions), r_p, len(freq), f_p, decimation, C.byref(h)))
+        energy = DftEnergy(self, h.value, freq)
+        self.dft_objects.append(energy)
+        return energy
 
     def add_force(self, *args, **kwargs):
         """add_force(fcen, df, nfreq | freq, *ForceRegions, decimation_factor=0):
@@ -977,3 +1009,19 @@ def scale_flux_fields(s, flux):
     """Multiply the flux object's DFT sums by the complex number s."""
     s = complex(s)
     flux.sim._check(flux.sim._lib.mgb_flux_scale(flux.sim._h, flux.handle, s.real, s.imag))
+
+
+def get_electric_energy(f):
+    return f._get(0)
+
+
+def get_magnetic_energy(f):
+    return f._get(1)
+
+
+def get_total_energy(f):
+    return f._get(2)
+
+
+def get_energy_freqs(f):
+    return list(f.freq)

@@ -1157,6 +1157,60 @@ static void case_py_force(Writer &w) {
   w.rec("Ez", global_field(f, gv, Ez));
 }
 
+/* Script (the reference's python/tests/test_dft_energy.py with a line source
+   across the guide instead of the eigenmode source, resolution 10, 50 time
+   units after the sources):
+     sim = mp.Simulation(resolution=10, cell_size=mp.Vector3(10, 5), eps_averaging=False,
+                         geometry=[mp.Block(size=mp.Vector3(mp.inf, 1, mp.inf), material=mp.Medium(epsilon=12))],
+                         boundary_layers=[mp.PML(1)],
+                         sources=[mp.Source(mp.GaussianSource(0.15, fwidth=0.03), component=mp.Ez,
+                                            center=mp.Vector3(-3), size=mp.Vector3(y=5))])
+     flux = sim.add_flux(0.15, 0, 1, mp.FluxRegion(center=mp.Vector3(3), size=mp.Vector3(y=5)), decimation_factor=1)
+     energy = sim.add_energy(0.15, 0, 1, mp.EnergyRegion(center=mp.Vector3(3), size=mp.Vector3(y=5)),
+                             decimation_factor=1)
+     energy_decimated = (the same with decimation_factor=10)
+     sim.run(until_after_sources=50) */
+static void case_py_energy(Writer &w) {
+  const double inf = 1.0e20;
+  grid_volume gv = vol2d(10, 5, 10);
+  gv.center_origin();
+  PyGeom g;
+  g.dim = 2;
+  g.meds = {{{1, 1, 1}, 0, {0, 0}}, {{12, 12, 12}, 0, {0, 0}}};
+  g.objs = {{0, {0, 0, 0}, {inf, 1, inf}, 0, 1}};
+  structure s(gv, g, pml(1.0), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.03);
+  gaussian_src_time src(0.15, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, volume(vec(-3, -2.5), vec(-3, 2.5)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = {0.15};
+  volume_list r(volume(vec(3, -2.5), vec(3, 2.5)), Sx, 1.0);
+  dft_flux flux = f.add_dft_flux(&r, fr.data(), fr.size(), true, true, 1);
+  dft_energy energy = f.add_dft_energy(&r, fr.data(), fr.size(), 1);
+  dft_energy energy_dec = f.add_dft_energy(&r, fr.data(), fr.size(), 10);
+  py_run_until_after_sources(f, 50);
+  sync_dfts(f);
+  double *F = flux.flux();
+  w.scalar("flux", F[0]);
+  delete[] F;
+  dft_energy *es[2] = {&energy, &energy_dec};
+  const char *names[2] = {"", "_dec"};
+  for (int q = 0; q < 2; q++) {
+    F = es[q]->electric();
+    w.scalar(std::string("electric") + names[q], F[0]);
+    delete[] F;
+    F = es[q]->magnetic();
+    w.scalar(std::string("magnetic") + names[q], F[0]);
+    delete[] F;
+    F = es[q]->total();
+    w.scalar(std::string("total") + names[q], F[0]);
+    delete[] F;
+  }
+  w.scalar("t", f.time());
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -1206,6 +1260,8 @@ int main(int argc, char **argv) {
     case_n2f(w, D2, Ex, Hz, steps > 0 ? steps : 2800);
   else if (cs == "n2f3d")
     case_n2f(w, D3, Ez, Hx, steps > 0 ? steps : 900);
+  else if (cs == "py_energy")
+    case_py_energy(w);
   else if (cs == "py_force")
     case_py_force(w);
   else if (cs == "py_n2f")
