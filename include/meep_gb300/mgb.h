@@ -78,6 +78,11 @@ int mgb_flux(mgb_sim *s, int handle, double *out);
 int mgb_flux_data(mgb_sim *s, int handle, int part, double *out, size_t *n);
 int mgb_load_flux_data(mgb_sim *s, int handle, int part, const double *in, size_t n);
 int mgb_flux_scale(mgb_sim *s, int handle, double re, double im);
+/* the same for any DFT object: kind 0 flux (parts E, H), 1 force (offdiag1,
+ * offdiag2, diag), 2 near2far (F), 3 energy (E, D, H, B) */
+int mgb_dft_data(mgb_sim *s, int kind, int handle, int part, double *out, size_t *n);
+int mgb_load_dft_data(mgb_sim *s, int kind, int handle, int part, const double *in, size_t n);
+int mgb_scale_dft_data(mgb_sim *s, int kind, int handle, int part, double re, double im);
 /* energy spectra (fields::add_dft_energy) over regions as for mgb_add_flux;
  * mgb_energy: which 0 electric, 1 magnetic, 2 total, nfreq values */
 int mgb_add_energy(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,

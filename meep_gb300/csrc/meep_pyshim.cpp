@@ -295,10 +295,64 @@ int mgb_flux(mgb_sim *s, int handle, double *out) {
   }
 }
 
-static dft_chunk *flux_part(mgb_sim *s, int handle, int part) {
-  if (!s || handle < 0 || handle >= (int)s->fluxes.size() || part < 0 || part > 1)
-    throw std::runtime_error("bad flux handle");
-  return part == 0 ? s->fluxes[handle].E : s->fluxes[handle].H;
+// the chunk lists of a DFT object: kind 0 flux (E, H), 1 force (offdiag1,
+// offdiag2, diag), 2 near2far (F), 3 energy (E, D, H, B)
+static dft_chunk *chunk_list(mgb_sim *s, int kind, int handle, int part) {
+  if (!s) throw std::runtime_error("null handle");
+  auto bad = [] { return std::runtime_error("bad dft object handle or part"); };
+  switch (kind) {
+    case 0:
+      if (handle < 0 || handle >= (int)s->fluxes.size() || part < 0 || part > 1) throw bad();
+      return part == 0 ? s->fluxes[handle].E : s->fluxes[handle].H;
+    case 1: {
+      if (handle < 0 || handle >= (int)s->forces.size() || part < 0 || part > 2) throw bad();
+      dft_force &f = s->forces[handle];
+      return part == 0 ? f.offdiag1 : part == 1 ? f.offdiag2 : f.diag;
+    }
+    case 2:
+      if (handle < 0 || handle >= (int)s->n2fs.size() || part != 0) throw bad();
+      return s->n2fs[handle].F;
+    case 3: {
+      if (handle < 0 || handle >= (int)s->energies.size() || part < 0 || part > 3) throw bad();
+      dft_energy &e = s->energies[handle];
+      return part == 0 ? e.E : part == 1 ? e.D : part == 2 ? e.H : e.B;
+    }
+    default: throw bad();
+  }
+}
+
+static dft_chunk *flux_part(mgb_sim *s, int handle, int part) { return chunk_list(s, 0, handle, part); }
+
+int mgb_dft_data(mgb_sim *s, int kind, int handle, int part, double *out, size_t *n) {
+  try {
+    dft_chunk *c = chunk_list(s, kind, handle, part);
+    if (!n) throw std::runtime_error("null argument");
+    *n = dft_data_size(c);
+    if (out) get_dft_data(c, reinterpret_cast<std::complex<double> *>(out), *n);
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_load_dft_data(mgb_sim *s, int kind, int handle, int part, const double *in, size_t n) {
+  try {
+    if (!in) throw std::runtime_error("null argument");
+    load_dft_data(chunk_list(s, kind, handle, part), reinterpret_cast<const std::complex<double> *>(in), n);
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_scale_dft_data(mgb_sim *s, int kind, int handle, int part, double re, double im) {
+  try {
+    dft_chunk *c = chunk_list(s, kind, handle, part);
+    if (c) c->scale_dft(std::complex<double>(re, im));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
 }
 
 int mgb_flux_data(mgb_sim *s, int handle, int part, double *out, size_t *n) {

@@ -388,6 +388,9 @@ _SIGS = [
     ("mgb_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_size_t)]),
     ("mgb_load_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.c_size_t]),
     ("mgb_flux_scale", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
+    ("mgb_dft_data", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP, C.POINTER(C.c_size_t)]),
+    ("mgb_load_dft_data", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP, C.c_size_t]),
+    ("mgb_scale_dft_data", C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double]),
     ("mgb_add_energy", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
     ("mgb_energy", C.c_int, [_P, C.c_int, C.c_int, _DP]),
     ("mgb_add_force", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
@@ -435,6 +438,8 @@ class DftFields:
 
 # python/simulation.py FluxData: the E and H DFT sums of a flux object
 FluxData = collections.namedtuple("FluxData", ["E", "H"])
+ForceData = collections.namedtuple("ForceData", ["offdiag1", "offdiag2", "diag"])
+NearToFarData = collections.namedtuple("NearToFarData", ["F"])
 
 
 class DftEnergy:
@@ -689,6 +694,45 @@ class Simulation:
         energy = DftEnergy(self, h.value, freq)
         self.dft_objects.append(energy)
         return energy
+
+    # force and near2far data (python/simulation.py get_force_data,
+    # load_force_data, load_minus_force_data, get_near2far_data, ...)
+    def _dft_parts(self, kind, obj, nparts):
+        out = []
+        for part in range(nparts):
+            n = C.c_size_t()
+            self._check(self._lib.mgb_dft_data(self._h, kind, obj.handle, part, None, C.byref(n)))
+            a = np.zeros(2 * n.value)
+            self._check(self._lib.mgb_dft_data(self._h, kind, obj.handle, part, a.ctypes.data_as(_DP), C.byref(n)))
+            out.append(a[0::2] + 1j * a[1::2])
+        return out
+
+    def _load_parts(self, kind, obj, arrays, minus):
+        for part, arr in enumerate(arrays):
+            arr = np.asarray(arr, dtype=np.complex128)
+            ri = np.ascontiguousarray(np.stack([arr.real, arr.imag], axis=-1).reshape(-1))
+            self._check(self._lib.mgb_load_dft_data(self._h, kind, obj.handle, part, ri.ctypes.data_as(_DP),
+                                                    arr.size))
+            if minus:
+                self._check(self._lib.mgb_scale_dft_data(self._h, kind, obj.handle, part, -1.0, 0.0))
+
+    def get_force_data(self, force):
+        return ForceData(*self._dft_parts(1, force, 3))
+
+    def load_force_data(self, force, fdata):
+        self._load_parts(1, force, [fdata.offdiag1, fdata.offdiag2, fdata.diag], False)
+
+    def load_minus_force_data(self, force, fdata):
+        self._load_parts(1, force, [fdata.offdiag1, fdata.offdiag2, fdata.diag], True)
+
+    def get_near2far_data(self, near2far):
+        return NearToFarData(*self._dft_parts(2, near2far, 1))
+
+    def load_near2far_data(self, near2far, n2fdata):
+        self._load_parts(2, near2far, [n2fdata.F], False)
+
+    def load_minus_near2far_data(self, near2far, n2fdata):
+        self._load_parts(2, near2far, [n2fdata.F], True)
 
     def add_force(self, *args, **kwargs):
         """add_force(fcen, df, nfreq | freq, *ForceRegions, decimation_factor=0):

@@ -69,3 +69,37 @@ def test_flux_data_on_gpu(engine_lib):
     from meep_gb300.simulation import PRODUCT_LIB
     _check(PRODUCT_LIB, 1e-12)
     _check(os.path.join(os.path.dirname(PRODUCT_LIB), "libmeep_gb300_single.so"), 1e-6)
+
+
+def _run_fn(lib, scatterer, fload=None, nload=None):
+    geometry = [mp.Block(mp.Vector3(0.6, 1.2, mp.inf), center=mp.Vector3(0.3, 0.1),
+                         material=mp.Medium(epsilon=12))] if scatterer else []
+    sim = mp.Simulation(cell_size=mp.Vector3(8, 6), resolution=10, geometry=geometry,
+                        boundary_layers=[mp.PML(1.0)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(0.5, fwidth=0.3), component=mp.Ez,
+                                           center=mp.Vector3(-2.5), size=mp.Vector3(y=2))], _library=lib)
+    force = sim.add_force(0.5, 0.3, 3, mp.ForceRegion(center=mp.Vector3(1.5), size=mp.Vector3(y=2), direction=mp.X),
+                          mp.ForceRegion(center=mp.Vector3(0.3, 1.5), size=mp.Vector3(2), direction=mp.X))
+    n2f = sim.add_near2far(0.5, 0.3, 3, mp.Near2FarRegion(center=mp.Vector3(2.5), size=mp.Vector3(y=3)))
+    if fload is not None:
+        sim.load_minus_force_data(force, fload)
+    if nload is not None:
+        sim.load_minus_near2far_data(n2f, nload)
+    sim.run(until_after_sources=10)
+    ff = sim.get_farfields_at(n2f, [[30.0, 5.0, 0.0], [40.0, -10.0, 0.0]])
+    return sim.get_force_data(force), sim.get_near2far_data(n2f), ff
+
+
+def test_force_and_near2far_data_on_oracle(oracle_lib):
+    """get/load_minus force and near2far data: the loaded-negated run holds
+    the difference of the separate runs' sums, and (the near-to-far transform
+    being linear in them) its far fields are the difference of theirs."""
+    lib = os.path.join(os.path.dirname(oracle_lib), "liboracle_meep.so")
+    fa, na, ffa = _run_fn(lib, False)
+    fc, nc, ffc = _run_fn(lib, True)
+    fb, nb, ffb = _run_fn(lib, True, fload=fa, nload=na)
+    for k in ("offdiag1", "offdiag2", "diag"):
+        assert getattr(fa, k).size > 0
+        assert relerr(getattr(fb, k), getattr(fc, k) - getattr(fa, k)) <= 1e-12, k
+    assert relerr(nb.F, nc.F - na.F) <= 1e-12
+    assert relerr(ffb, ffc - ffa) <= 1e-12
