@@ -628,6 +628,34 @@ public:
   double periodic_k[2], period[2];
 };
 
+// local density of states of the sources (src/dft_ldos.cpp): call
+// update(f) before every step and once after the last, as the reference's
+// dft_ldos step function does
+class dft_ldos {
+public:
+  dft_ldos(double freq_min, double freq_max, int Nfreq);
+  explicit dft_ldos(const std::vector<double> &freq);
+  dft_ldos(const double *freq, size_t Nfreq);
+  void update(fields &f);
+  double *ldos();                   // newly allocated, Nfreq values
+  std::complex<double> *F() const; // the DFT of sum E conj(J) (and H)
+  std::complex<double> *J() const; // the DFT of the first source's current
+  double overall_scale() const { return saved_overall_scale; }
+  std::vector<double> freq;
+
+private:
+  struct Mon {
+    int id;                      // engine DFT monitor over the points' box
+    std::vector<size_t> at;      // each point's index in the monitor box
+    std::vector<std::complex<double>> amp;
+  };
+  fields *fld = nullptr;
+  std::vector<Mon> mons;
+  std::vector<std::complex<double>> Jdft;
+  double Jsum = 1.0, saved_overall_scale = 1.0;
+  void attach(fields &f);
+};
+
 // electric and magnetic energy density spectra in volumes (src/dft.cpp
 // dft_energy): created by fields::add_dft_energy
 class dft_energy {

@@ -83,6 +83,12 @@ int mgb_flux_scale(mgb_sim *s, int handle, double re, double im);
 int mgb_dft_data(mgb_sim *s, int kind, int handle, int part, double *out, size_t *n);
 int mgb_load_dft_data(mgb_sim *s, int kind, int handle, int part, const double *in, size_t n);
 int mgb_scale_dft_data(mgb_sim *s, int kind, int handle, int part, double re, double im);
+/* local density of states (dft_ldos): create, update before every step and
+ * after the last (the dft_ldos step function), then ldos[nfreq] and the
+ * DFTs F, J (nfreq complex, re/im) */
+int mgb_ldos_create(mgb_sim *s, int nfreq, const double *freqs, int *handle);
+int mgb_ldos_update(mgb_sim *s, int handle);
+int mgb_ldos_results(mgb_sim *s, int handle, double *ldos, double *F, double *J);
 /* energy spectra (fields::add_dft_energy) over regions as for mgb_add_flux;
  * mgb_energy: which 0 electric, 1 magnetic, 2 total, nfreq values */
 int mgb_add_energy(mgb_sim *s, int nreg, const double *regions, int nfreq, const double *freqs, int decimation,

@@ -90,6 +90,13 @@ int mfd_add_continuous_src(mfd_sim *sim, double freq_re, double freq_im, double 
                            double start, double end, double slowness, int is_integrated,
                            int *id);
 
+/* Current of source time function src_id at `time` as fields::step takes it
+ * from src_time::update (the difference quotient (dipole(time + dt) -
+ * dipole(time)) / dt, src/sources.cpp); out = (re, im).  Host arithmetic, for
+ * callers that integrate the source spectrum (dft_ldos::update,
+ * src/dft_ldos.cpp:157-162). */
+int mfd_src_current(const mfd_sim *sim, int src_id, double time, double *out);
+
 /* Point list of a source on component c (an E or H component: the current is
  * applied to the D or B field of that direction).  idx are dense-array linear
  * indices, amp interleaved (re, im).  Replaces fields::add_volume_source /

@@ -86,6 +86,7 @@ SIGNATURES = [
                                     C.POINTER(mfd_object), C.c_double, _DP]),
     ("mfd_scale_dft", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
     ("mfd_set_dft", C.c_int, [_P, C.c_int, _DP]),
+    ("mfd_src_current", C.c_int, [_P, C.c_int, C.c_double, _DP]),
     ("mfd_farfield", C.c_int, [_P, C.c_int, _IP, _IP, _DP, _DP, C.c_double, C.c_double, _IP, _IP, _DP, _DP,
                                C.c_int64, _DP, _DP]),
     ("mfd_green", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,

@@ -1865,4 +1865,116 @@ void dft_energy::scale_dfts(std::complex<double> scale) {
     if (c) c->scale_dft(scale);
 }
 
+/* ------------------------------------------------------------------ LDOS */
+// dft_ldos (src/dft_ldos.cpp).  The reference adds E(t) conj(A) over every
+// source point to Fdft at each update; here each source's point list gets an
+// engine DFT monitor over its bounding box (no weights, the DFT's dt /
+// sqrt(2 pi) scale, every step), and ldos() forms sum conj(A) DFT(E) from
+// it: the same sum, the E samples at t dt (H at (t - 1/2) dt) with the same
+// phases (the t = 0 term of the reference is zero: the fields start at zero).
+// Jdft, the DFT of the first source's current, is accumulated on the host at
+// each update like the reference's.
+dft_ldos::dft_ldos(double freq_min, double freq_max, int Nfreq)
+    : freq(linspace(freq_min, freq_max, Nfreq)), Jdft(freq.size(), 0.0) {}
+dft_ldos::dft_ldos(const std::vector<double> &freq_) : freq(freq_), Jdft(freq.size(), 0.0) {}
+dft_ldos::dft_ldos(const double *freq_, size_t Nfreq) : freq(freq_, freq_ + Nfreq), Jdft(Nfreq, 0.0) {}
+
+void dft_ldos::attach(fields &f) {
+  fld = &f;
+  ensure_engine(f);
+  fields::impl &I = *f.d;
+  Dense dn(f.gv);
+  Jsum = 0.0;
+  for (const PendingSource &ps : I.pending) {
+    if (ps.idx.empty()) continue;
+    const int t = ps.c / 3, d = ps.c % 3;
+    if (t != MFD_E && t != MFD_H) continue;
+    // the field the reference reads for this source: E (or H) along its direction
+    const int mc = 3 * t + d;
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
+    for (int64_t di : ps.idx) {
+      int k[3];
+      dn.coords(di, k);
+      for (int q = 0; q < 3; q++) {
+        lo[q] = std::min(lo[q], k[q]);
+        hi[q] = std::max(hi[q], k[q]);
+      }
+    }
+    std::vector<double> ones[3];
+    const double *wp[3] = {nullptr, nullptr, nullptr};
+    for (int q = 0; q < 3; q++) {
+      ones[q].assign(hi[q] - lo[q] + 1, 1.0);
+      wp[q] = ones[q].data();
+    }
+    Mon m;
+    chk(mfd_add_dft(I.sim, mc, lo, hi, wp, 1.0, 0, f.dt / std::sqrt(2.0 * pi), 0.0, 0, freq.size(), freq.data(), 1,
+                    &m.id));
+    for (size_t j = 0; j < ps.idx.size(); j++) {
+      int k[3];
+      dn.coords(ps.idx[j], k);
+      m.at.push_back(((size_t)(k[0] - lo[0]) * (hi[1] - lo[1] + 1) + (k[1] - lo[1])) * (hi[2] - lo[2] + 1) +
+                     (k[2] - lo[2]));
+      m.amp.push_back(ps.amp[j]);
+      Jsum += std::abs(ps.amp[j]);
+    }
+    mons.push_back(std::move(m));
+  }
+  // correct for dV factors (src/dft_ldos.cpp:165-166)
+  double vol = 1.0;
+  LOOP_OVER_DIRECTIONS(f.gv.dim, q) vol *= f.gv.inva;
+  Jsum *= std::sqrt(vol);
+}
+
+void dft_ldos::update(fields &f) {
+  if (!fld) attach(f);
+  if (fld != &f) meep::abort("dft_ldos updated with another fields object");
+  // the first source's current as the last step left it: its value at the
+  // current time (none before the first step)
+  if (f.t == 0 || f.d->srcs.empty()) return;
+  double cur[2];
+  chk(mfd_src_current(f.d->sim, 0, f.time(), cur));
+  const std::complex<double> J = f.d->real_fields ? std::complex<double>(cur[0], 0.0) : std::complex<double>(cur[0], cur[1]);
+  const double scale = f.dt / std::sqrt(2 * pi);
+  for (size_t i = 0; i < freq.size(); ++i) {
+    const std::complex<double> Ephase = std::polar(1.0, 2 * pi * freq[i] * f.time()) * scale;
+    Jdft[i] += Ephase * J;
+  }
+}
+
+std::complex<double> *dft_ldos::F() const {
+  const size_t nf = freq.size();
+  std::complex<double> *out = new std::complex<double>[nf];
+  for (size_t i = 0; i < nf; i++)
+    out[i] = 0.0;
+  for (const Mon &m : mons) {
+    size_t np = 0, n2 = 0;
+    chk(mfd_get_dft(fld->d->sim, m.id, nullptr, &np, &n2));
+    std::vector<double> buf(2 * np * nf);
+    chk(mfd_get_dft(fld->d->sim, m.id, buf.data(), &np, &n2));
+    for (size_t j = 0; j < m.at.size(); j++)
+      for (size_t i = 0; i < nf; i++)
+        out[i] += std::complex<double>(buf[2 * (m.at[j] * nf + i)], buf[2 * (m.at[j] * nf + i) + 1]) * conj(m.amp[j]);
+  }
+  return out;
+}
+
+std::complex<double> *dft_ldos::J() const {
+  std::complex<double> *out = new std::complex<double>[freq.size()];
+  for (size_t i = 0; i < freq.size(); i++)
+    out[i] = Jdft[i];
+  return out;
+}
+
+// dft_ldos::ldos (src/dft_ldos.cpp:63-86)
+double *dft_ldos::ldos() {
+  saved_overall_scale = 4.0 / pi * -0.5 / (Jsum * Jsum);
+  std::complex<double> *Fd = F();
+  double *out = new double[freq.size()];
+  for (size_t i = 0; i < freq.size(); ++i)
+    out[i] = saved_overall_scale * real(Fd[i] * conj(Jdft[i])) /
+             (real(Jdft[i]) * real(Jdft[i]) + imag(Jdft[i]) * imag(Jdft[i]));
+  delete[] Fd;
+  return out;
+}
+
 } // namespace meep

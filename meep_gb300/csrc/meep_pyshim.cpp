@@ -167,6 +167,7 @@ struct mgb_sim {
   std::vector<dft_near2far> n2fs;
   std::vector<dft_force> forces;
   std::vector<dft_energy> energies;
+  std::vector<std::unique_ptr<dft_ldos>> ldoses;
 };
 
 // rows of (center[3], size[3], direction or -1, weight) as a volume_list;
@@ -381,6 +382,60 @@ int mgb_flux_scale(mgb_sim *s, int handle, double re, double im) {
   try {
     if (!s || handle < 0 || handle >= (int)s->fluxes.size()) throw std::runtime_error("bad flux handle");
     s->fluxes[handle].scale_dfts(std::complex<double>(re, im));
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_ldos_create(mgb_sim *s, int nfreq, const double *freqs, int *handle) {
+  try {
+    if (!s || !freqs || !handle || nfreq < 1) throw std::runtime_error("null argument");
+    // the reference's Python layer runs real fields unless a Bloch k makes
+    // them complex (fields::use_real_fields in Simulation._init_fields); the
+    // LDOS takes the real part of the source current for real fields
+    try {
+      s->f->use_real_fields();
+    } catch (const std::exception &) {
+    }
+    s->ldoses.emplace_back(new dft_ldos(freqs, (size_t)nfreq));
+    *handle = (int)s->ldoses.size() - 1;
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_ldos_update(mgb_sim *s, int handle) {
+  try {
+    if (!s || handle < 0 || handle >= (int)s->ldoses.size()) throw std::runtime_error("bad ldos handle");
+    s->ldoses[handle]->update(*s->f);
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int mgb_ldos_results(mgb_sim *s, int handle, double *ldos, double *F, double *J) {
+  try {
+    if (!s || handle < 0 || handle >= (int)s->ldoses.size()) throw std::runtime_error("bad ldos handle");
+    dft_ldos &l = *s->ldoses[handle];
+    const size_t nf = l.freq.size();
+    if (ldos) {
+      double *v = l.ldos();
+      std::copy(v, v + nf, ldos);
+      delete[] v;
+    }
+    for (int q = 0; q < 2; q++) {
+      double *dst = q == 0 ? F : J;
+      if (!dst) continue;
+      std::complex<double> *v = q == 0 ? l.F() : l.J();
+      for (size_t i = 0; i < nf; i++) {
+        dst[2 * i] = v[i].real();
+        dst[2 * i + 1] = v[i].imag();
+      }
+      delete[] v;
+    }
     return 0;
   } catch (const std::exception &e) {
     return fail(e);

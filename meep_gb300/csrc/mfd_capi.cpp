@@ -441,6 +441,17 @@ int mfd_flux(mfd_sim *s, int npairs, const int *idE, const int *idH, double *out
   MFD_CATCH
 }
 
+int mfd_src_current(const mfd_sim *s, int src_id, double time, double *out) {
+  MFD_TRY
+  need(s && s->plan && out, "null argument");
+  const Plan &p = *s->plan;
+  need(src_id >= 0 && src_id < (int)p.srcs.size(), "unknown source id");
+  const std::complex<double> c = p.srcs[src_id].current(time, p.dt);
+  out[0] = c.real();
+  out[1] = c.imag();
+  MFD_CATCH
+}
+
 int mfd_scale_dft(mfd_sim *s, int id, double s_re, double s_im) {
   MFD_TRY
   need(s && s->plan, "null simulation handle");

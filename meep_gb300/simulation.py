@@ -391,6 +391,9 @@ _SIGS = [
     ("mgb_dft_data", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP, C.POINTER(C.c_size_t)]),
     ("mgb_load_dft_data", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _DP, C.c_size_t]),
     ("mgb_scale_dft_data", C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double]),
+    ("mgb_ldos_create", C.c_int, [_P, C.c_int, _DP, C.POINTER(C.c_int)]),
+    ("mgb_ldos_update", C.c_int, [_P, C.c_int]),
+    ("mgb_ldos_results", C.c_int, [_P, C.c_int, _DP, _DP, _DP]),
     ("mgb_add_energy", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
     ("mgb_energy", C.c_int, [_P, C.c_int, C.c_int, _DP]),
     ("mgb_add_force", C.c_int, [_P, C.c_int, _DP, C.c_int, _DP, C.c_int, C.POINTER(C.c_int)]),
@@ -1069,3 +1072,49 @@ def get_total_energy(f):
 
 def get_energy_freqs(f):
     return list(f.freq)
+
+
+class Ldos:
+    """Frequencies of a local-density-of-states spectrum (python/simulation.py
+    Ldos(fcen, df, nfreq) or Ldos(freq)); pass it to dft_ldos(ldos=...)."""
+
+    def __init__(self, *args):
+        self.freq = list(np.asarray(_fix_dft_args(args, 0)[0], dtype=np.float64))
+        self.handle = None
+
+
+def get_ldos_freqs(l):
+    return list(l.freq)
+
+
+def dft_ldos(*args, **kwargs):
+    """Step function: the power spectrum of the sources normalised to the
+    LDOS (python/simulation.py dft_ldos).  After the run, sim.ldos_data holds
+    the spectrum and sim.ldos_Fdata / sim.ldos_Jdata the DFTs of E.J* and of
+    the source current."""
+    ldos = kwargs.get("ldos", None)
+    if ldos is None:
+        if not args and "freq" in kwargs:
+            args = (kwargs["freq"],)
+        elif not args:
+            args = (kwargs.get("fcen"), kwargs.get("df"), kwargs.get("nfreq"))
+        ldos = Ldos(*args)
+
+    def _ldos(sim, todo):
+        if ldos.handle is None:
+            h = C.c_int()
+            f_a, f_p = _arr(ldos.freq)
+            sim._check(sim._lib.mgb_ldos_create(sim._h, len(ldos.freq), f_p, C.byref(h)))
+            ldos.handle = h.value
+        if todo == "step":
+            sim._check(sim._lib.mgb_ldos_update(sim._h, ldos.handle))
+        else:
+            nf = len(ldos.freq)
+            out, F, J = np.zeros(nf), np.zeros(2 * nf), np.zeros(2 * nf)
+            sim._check(sim._lib.mgb_ldos_results(sim._h, ldos.handle, out.ctypes.data_as(_DP),
+                                                 F.ctypes.data_as(_DP), J.ctypes.data_as(_DP)))
+            sim.ldos_data = list(out)
+            sim.ldos_Fdata = list(F[0::2] + 1j * F[1::2])
+            sim.ldos_Jdata = list(J[0::2] + 1j * J[1::2])
+
+    return _ldos

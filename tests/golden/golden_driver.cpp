@@ -1211,6 +1211,60 @@ static void case_py_energy(Writer &w) {
   w.scalar("t", f.time());
 }
 
+/* Script (dft_ldos as in the reference's python/tests/test_ldos.py, here in
+   2-D Cartesian with a dielectric block beside an off-grid dipole):
+     sim = mp.Simulation(cell_size=mp.Vector3(6, 6), resolution=20, boundary_layers=[mp.PML(1)],
+                         eps_averaging=False,
+                         geometry=[mp.Block(mp.Vector3(1, 1, mp.inf), center=mp.Vector3(0.8),
+                                            material=mp.Medium(epsilon=4))],
+                         sources=[mp.Source(mp.GaussianSource(1.0, fwidth=0.2), component=mp.Ez,
+                                            center=mp.Vector3(0.1, 0.05))])
+     sim.run(mp.dft_ldos(1.0, 0.2, 5), until_after_sources=20)
+     sim.ldos_data, sim.ldos_Fdata, sim.ldos_Jdata */
+static void case_py_ldos(Writer &w) {
+  const double inf = 1.0e20;
+  grid_volume gv = vol2d(6, 6, 20);
+  gv.center_origin();
+  PyGeom g;
+  g.dim = 2;
+  g.meds = {{{1, 1, 1}, 0, {0, 0}}, {{4, 4, 4}, 0, {0, 0}}};
+  g.objs = {{0, {0.8, 0, 0}, {1, 1, inf}, 0, 1}};
+  structure s(gv, g, pml(1.0), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.2);
+  gaussian_src_time src(1.0, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, volume(vec(0.1, 0.05), vec(0.1, 0.05)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = np_linspace(1.0 - 0.5 * 0.2, 1.0 + 0.5 * 0.2, 5);
+  dft_ldos ldos(fr.data(), fr.size());
+  // run(step function, until_after_sources=20): the step function before
+  // every step and once after the last
+  const double ts = f.last_source_time();
+  const double until = (ts - f.round_time()) + 20, t0 = f.round_time();
+  while (!(f.round_time() >= t0 + until)) {
+    ldos.update(f);
+    f.step();
+  }
+  ldos.update(f);
+  double *L = ldos.ldos();
+  w.rec("ldos", std::vector<double>(L, L + fr.size()));
+  delete[] L;
+  complex<double> *F = ldos.F(), *J = ldos.J();
+  std::vector<double> vf, vj;
+  for (size_t i = 0; i < fr.size(); i++) {
+    vf.push_back(F[i].real());
+    vf.push_back(F[i].imag());
+    vj.push_back(J[i].real());
+    vj.push_back(J[i].imag());
+  }
+  delete[] F;
+  delete[] J;
+  w.rec("F", vf);
+  w.rec("J", vj);
+  w.scalar("t", f.time());
+}
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -1260,6 +1314,8 @@ int main(int argc, char **argv) {
     case_n2f(w, D2, Ex, Hz, steps > 0 ? steps : 2800);
   else if (cs == "n2f3d")
     case_n2f(w, D3, Ez, Hx, steps > 0 ? steps : 900);
+  else if (cs == "py_ldos")
+    case_py_ldos(w);
   else if (cs == "py_energy")
     case_py_energy(w);
   else if (cs == "py_force")

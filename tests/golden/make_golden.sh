@@ -7,7 +7,7 @@ set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 ROOT=$(cd "$HERE/../.." && pwd)
 make -C "$ROOT/oracle/ref" -j8 >/dev/null
-CASES=${CASES:-"known tm2d_small tm2d_small_dec1 vec3d_small disp3d_small tm2d_full aniso1d aniso_te2d aniso3d offdiag_te2d aniso_bloch2d py_tm2d py_disp3d py_aniso_te2d py_aniso3d n2f_tm2d n2f_te2d n2f3d n2f_periodic2d py_n2f py_force py_energy"}
+CASES=${CASES:-"known tm2d_small tm2d_small_dec1 vec3d_small disp3d_small tm2d_full aniso1d aniso_te2d aniso3d offdiag_te2d aniso_bloch2d py_tm2d py_disp3d py_aniso_te2d py_aniso3d n2f_tm2d n2f_te2d n2f3d n2f_periodic2d py_n2f py_force py_energy py_ldos"}
 for c in $CASES; do
   for p in f64 f32; do
     OMP_NUM_THREADS=${OMP_NUM_THREADS:-8} "$ROOT/oracle/_ref/fp${p#f}/golden_driver" "$c" "$HERE/$c.$p.bin"
