@@ -103,3 +103,25 @@ def test_force_and_near2far_data_on_oracle(oracle_lib):
         assert relerr(getattr(fb, k), getattr(fc, k) - getattr(fa, k)) <= 1e-12, k
     assert relerr(nb.F, nc.F - na.F) <= 1e-12
     assert relerr(ffb, ffc - ffa) <= 1e-12
+
+
+def test_abi_errors(oracle_lib):
+    """The C ABI refuses a 1-D far field, an unknown monitor for mfd_set_dft,
+    an unknown source for mfd_src_current, and an include_weights mode other
+    than 0, 1, 2, each with a message."""
+    import ctypes as C
+    from meep_gb300 import _lib
+    eng = _lib.Engine(oracle_lib)
+    s = _lib.Sim(eng, 1, (0, 0, 20), (0, 0, -20), 10.0, components=[0, 4, 6, 10])
+    w = [None, None, np.ones(3)]
+    mid = s.add_dft(0, [0, 0, 5], [0, 0, 7], w, centered=False, freqs=[0.5])
+    with pytest.raises(_lib.MeepError, match="only 2d or 3d"):
+        s.farfield([(mid, 4, [0, 0, 0], [0, 0, 0])], [[0, 0, 1.0]])
+    buf = np.zeros(6)
+    assert eng.lib.mfd_set_dft(s.h, 99, buf.ctypes.data_as(C.POINTER(C.c_double))) != 0
+    assert b"unknown monitor" in eng.lib.mfd_last_error()
+    out = np.zeros(2)
+    assert eng.lib.mfd_src_current(s.h, 0, 1.0, out.ctypes.data_as(C.POINTER(C.c_double))) != 0
+    assert b"unknown source" in eng.lib.mfd_last_error()
+    with pytest.raises(_lib.MeepError, match="include_weights"):
+        s.add_dft(0, [0, 0, 5], [0, 0, 7], w, include_weights=3, centered=False, freqs=[0.5])
