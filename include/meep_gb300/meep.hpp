@@ -560,9 +560,11 @@ public:
   int monitor_id;
   fields *fld;
   std::complex<double> extra_weight; // weight of the force sum (dft_force)
+  int decimation_factor;             // steps between accumulated samples (src/meep.hpp:1196)
   dft_chunk()
       : c(Ex), N(0), dft(nullptr), next_in_dft(nullptr), vc(Ex), monitor_id(-1), fld(nullptr),
-        extra_weight(1.0) {}
+        extra_weight(1.0), decimation_factor(1) {}
+  int get_decimation_factor() const { return decimation_factor; }
   ~dft_chunk() { delete[] dft; }
   // multiply the sums of this chunk and the chunks after it (device sums)
   void scale_dft(std::complex<double> scale);

@@ -22,7 +22,9 @@ LIB = os.path.join(PKG, "lib")
 INC = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "include", "meep_gb300"),
        "-I" + CSRC, "-I" + os.path.join(PKG, "workloads")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-REFERENCE = "/root/reference"
+# checkout of the reference (its src/ directory is compiled into oracle/_ref
+# by oracle/ref/Makefile); unset: the reference core is not built
+REFERENCE = os.environ.get("MEEP_REFERENCE", "")
 
 
 def _nvcc():
@@ -143,10 +145,12 @@ def build_oracle():
 
 
 def build_reference():
-    """Reference core, only where its sources are present (build container)."""
-    if not os.path.isdir(os.path.join(REFERENCE, "src")):
+    """Reference core, only where its sources are present: MEEP_REFERENCE
+    names the reference checkout (test infrastructure, never on the GPU
+    host)."""
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "src")):
         return None
-    _run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j8"])
+    _run(["make", "-C", os.path.join(ROOT, "oracle", "ref"), "-j8", "REF=" + REFERENCE])
     return os.path.join(ROOT, "oracle", "_ref")
 
 

@@ -1077,6 +1077,7 @@ static dft_chunk *add_dft_one(fields &f, component c, const volume &where, const
   ch->vc = vc < 0 ? int(c) : vc;
   ch->extra_weight = extra_weight;
   ch->monitor_id = id;
+  ch->decimation_factor = decimation_factor;
   ch->fld = &f;
   ch->is = L.is;
   ch->ie = L.ie;

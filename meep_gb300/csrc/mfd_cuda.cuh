@@ -623,6 +623,39 @@ static __global__ void flux_final_kernel(const double *partial, int nparts, int 
   }
 }
 
+// Divergence test of fields::step() (src/step.cpp:137-138): half the sum of
+// Re(conj(E_d) D_d) with both interpolated at the cell centre
+// (Plan::center_probe); a non-finite value sets a flag in host-mapped
+// memory, which the host reads without a copy in the stream.
+template <typename R> struct FiniteProbe {
+  const R *e[3], *d[3], *ei[3], *di[3];
+  int n[3];
+  long long idx[3][8];
+  double w[3][8];
+  int *flag;
+};
+template <typename R> __global__ void finite_probe_kernel(const FiniteProbe<R> p) {
+  double sum = 0.0;
+  for (int c = 0; c < 3; c++) {
+    if (!p.e[c]) continue;
+    double er = 0, dr = 0, ei = 0, di = 0;
+    for (int j = 0; j < p.n[c]; j++) {
+      const long long i = p.idx[c][j];
+      er += p.w[c][j] * double(p.e[c][i]);
+      dr += p.w[c][j] * double(p.d[c][i]);
+      if (p.ei[c]) {
+        ei += p.w[c][j] * double(p.ei[c][i]);
+        di += p.w[c][j] * double(p.di[c][i]);
+      }
+    }
+    sum += er * dr + ei * di;
+  }
+  if (!isfinite(sum * 0.5)) {
+    *(volatile int *)p.flag = 1;
+    __threadfence_system();
+  }
+}
+
 // ---------------------------------------------------------------- backend
 template <typename R> class CudaBackend : public Backend {
 public:
@@ -647,6 +680,7 @@ public:
   ~CudaBackend() override {
     for (void *ptr : allocs)
       cudaFree(ptr);
+    if (h_nonfinite) cudaFreeHost(h_nonfinite);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     for (int q = 0; q < NSIDE; q++) {
@@ -781,6 +815,37 @@ public:
     cuda_check(cudaStreamSynchronize(stream), "error flag sync");
     if (e) throw Error("tensor-core DFT contraction: an MMA completion wait timed out");
   }
+  // divergence test: every finite_every steps (MFD_FINITE_CHECK_EVERY, 0
+  // turns it off) the probe kernel checks the centre energy density; the
+  // flag is read at the start of every step and after every batch of steps,
+  // so a run stops within finite_every steps (plus the steps already queued)
+  // of the step the reference would stop at
+  int *h_nonfinite = nullptr, *d_nonfinite = nullptr;
+  int finite_every = 16;
+  void launch_finite_probe(const Plan &p) {
+    FiniteProbe<R> fp;
+    std::memset(&fp, 0, sizeof(fp));
+    for (int d = 0; d < 3; d++) {
+      const int ce = comp(MFD_E, d), cd = comp(MFD_D, d);
+      if (!f[ce] || !f[cd]) continue;
+      const Plan::ProbePoints pp = p.center_probe(d);
+      fp.e[d] = f[ce];
+      fp.d[d] = f[cd];
+      fp.ei[d] = cplx ? fim[ce] : nullptr;
+      fp.di[d] = cplx ? fim[cd] : nullptr;
+      fp.n[d] = pp.n;
+      for (int j = 0; j < pp.n; j++) {
+        fp.idx[d][j] = pp.idx[j];
+        fp.w[d][j] = pp.w[j];
+      }
+    }
+    fp.flag = d_nonfinite;
+    finite_probe_kernel<R><<<1, 1, 0, stream>>>(fp);
+    nlaunch++;
+  }
+  void check_finite() const {
+    if (h_nonfinite && *(volatile int *)h_nonfinite) throw Error("simulation fields are NaN or Inf");
+  }
   int fused_mask = -1; // component mask of an available fused kernel set, -1 none
   bool has_b_current = false;
   long long nlaunch = 0;
@@ -818,6 +883,10 @@ public:
 
   void setup(Plan &p) override {
     p.plan_offdiag();
+    if (const char *e = getenv("MFD_FINITE_CHECK_EVERY")) finite_every = std::max(0, atoi(e));
+    cuda_check(cudaHostAlloc((void **)&h_nonfinite, sizeof(int), cudaHostAllocMapped), "cudaHostAlloc");
+    *(volatile int *)h_nonfinite = 0;
+    cuda_check(cudaHostGetDevicePointer((void **)&d_nonfinite, h_nonfinite, 0), "cudaHostGetDevicePointer");
     for (int d = 0; d < 3; d++) {
       geo.N[d] = p.N[d];
       geo.T[d][0] = p.T[d][0];
@@ -913,6 +982,7 @@ public:
           }
     }
     setup_sources(p);
+    build_active_mask(p);
     if (p.any_offdiag)
       for (int d = 0; d < 3; d++) {
         if (!p.have[comp(MFD_E, d)]) continue;
@@ -936,6 +1006,40 @@ public:
     if (p.any_offdiag && p.g.dim != 3) fused_mask = -1;
     if (fused_mask >= 0) plan_boxes(p);
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
+  }
+
+  // activity bits per row segment of 32 z points (FusedArgs::amask) for
+  // the 3-D band kernels: poles with a nonzero sigma and D/B components with
+  // a nonzero conductivity somewhere in the segment
+  unsigned *d_amask = nullptr;
+  int amask_nseg = 0;
+  void build_active_mask(const Plan &p) {
+    if (p.g.dim != 3) return;
+    bool any = !poles.empty();
+    for (int d = 0; d < 3; d++)
+      any = any || cnd[comp(MFD_D, d)] || cnd[comp(MFD_B, d)];
+    if (!any) return;
+    const int nseg = (p.ext[2] + 31) / 32;
+    std::vector<unsigned> m((size_t)p.ext[0] * p.ext[1] * nseg, 0u);
+    auto mark = [&](const std::vector<double> &dense, unsigned bit) {
+      if (dense.empty()) return;
+      int64_t di = 0;
+      for (int k0 = 0; k0 < p.ext[0]; k0++)
+        for (int k1 = 0; k1 < p.ext[1]; k1++) {
+          unsigned *row = &m[((size_t)k0 * p.ext[1] + k1) * nseg];
+          for (int k2 = 0; k2 < p.ext[2]; k2++, di++)
+            if (dense[di] != 0.0) row[k2 >> 5] |= bit;
+        }
+    };
+    for (size_t q = 0; q < poles.size(); q++)
+      for (int d = 0; d < 3; d++)
+        if (poles[q].P[d]) mark(p.poles[q].sigma[d], 1u << (3 * q + d));
+    for (int d = 0; d < 3; d++) {
+      if (cnd[comp(MFD_D, d)]) mark(p.cond[comp(MFD_D, d)], 1u << (12 + d));
+      if (cnd[comp(MFD_B, d)]) mark(p.cond[comp(MFD_B, d)], 1u << (15 + d));
+    }
+    d_amask = dupload(m);
+    amask_nseg = nseg;
   }
 
   static constexpr int MASK3 = 0xFFF;
@@ -990,6 +1094,9 @@ public:
     a.dtdx = R(p.g.courant);
     a.dt2 = R(p.dt) * R(0.5);
     a.fuse_h = fuse_h;
+    a.amask = d_amask;
+    a.mext1 = p.ext[1];
+    a.mnseg = amask_nseg;
     for (int d = 0; d < 3; d++) {
       a.fmp[d] = fmp[d];
       a.noff[d] = p.offdiag[d].n;
@@ -1114,20 +1221,13 @@ public:
   }
   // launches one pass over rows + shell (the shell on the side streams)
   template <class F> void over_bands3(const Plan &p, F &&launch) {
-    constexpr bool F32 = std::is_same<R, float>::value;
     (void)p;
     fork();
     launch(band_rows, 0, stream);
-    if (F32) {
-      launch(band_xface, 1, side[0]);
-      launch(band_yface, 2, side[1]);
-    }
-    else {
-      launch(band_xface_zi, 4, side[0]);
-      launch(band_yface_zi, 5, side[1]);
-      launch(band_xzedge, 6, side[4]);
-      launch(band_yzedge, 7, side[5]);
-    }
+    launch(band_xface_zi, 4, side[0]);
+    launch(band_yface_zi, 5, side[1]);
+    launch(band_xzedge, 6, side[4]);
+    launch(band_yzedge, 7, side[5]);
     launch(band_xyedge, 3, side[3]);
     join();
   }
@@ -1237,6 +1337,15 @@ public:
       band_xyedge = Band{{sxo, syo, sza}};
       int zlo = std::min(p.T[2][0] + 1, p.N[2]), zhi = p.N[2] - p.T[2][1] - 1;
       zhi = std::max(zhi, zlo - 1);
+      if (std::is_same<R, float>::value) {
+        // FP32: the z interior rounded inwards to whole warps of 32 points
+        // (every warp of the face bands starts on a 128-byte line)
+        const int zl = (zlo + 31) / 32 * 32, zh = (zhi + 1) / 32 * 32 - 1;
+        if (zh >= zl) {
+          zlo = zl;
+          zhi = zh;
+        }
+      }
       const Span szr = span_run(zlo, zhi), szo = span_outside(p.N[2], zlo, zhi);
       band_xface_zi = Band{{sxo, syr, szr}};
       band_yface_zi = Band{{sxr, syo, szr}};
@@ -1389,16 +1498,12 @@ public:
       }
       else
         launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
-      if (F32) {
-        launch_b_band<true, false>(band_xface, a, cndB, zp, side[0]);
-        launch_b_band<false, true>(band_yface, a, cndB, zp, side[1]);
-      }
-      else {
-        launch_b_band<true, false, false>(band_xface_zi, a, cndB, zp, side[0]);
-        launch_b_band<false, true, false>(band_yface_zi, a, cndB, zp, side[1]);
-        launch_b_band<true, false>(band_xzedge, a, cndB, zp, side[4]);
-        launch_b_band<false, true>(band_yzedge, a, cndB, zp, side[5]);
-      }
+      // x and y slab faces: their z interior (no z flags; whole warps in
+      // FP32) and their z ends as separate launches
+      launch_b_band<true, false, false>(band_xface_zi, a, cndB, zp, side[0]);
+      launch_b_band<false, true, false>(band_yface_zi, a, cndB, zp, side[1]);
+      launch_b_band<true, false>(band_xzedge, a, cndB, zp, side[4]);
+      launch_b_band<false, true>(band_yzedge, a, cndB, zp, side[5]);
       launch_b_band<true, true>(band_xyedge, a, cndB, zp, side[3]);
       join();
     }
@@ -1452,16 +1557,10 @@ public:
       }
       else
         launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
-      if (F32) {
-        launch_de_band<true, false>(band_xface, a, cndD, zp, side[0]);
-        launch_de_band<false, true>(band_yface, a, cndD, zp, side[1]);
-      }
-      else {
-        launch_de_band<true, false, false>(band_xface_zi, a, cndD, zp, side[0]);
-        launch_de_band<false, true, false>(band_yface_zi, a, cndD, zp, side[1]);
-        launch_de_band<true, false>(band_xzedge, a, cndD, zp, side[4]);
-        launch_de_band<false, true>(band_yzedge, a, cndD, zp, side[5]);
-      }
+      launch_de_band<true, false, false>(band_xface_zi, a, cndD, zp, side[0]);
+      launch_de_band<false, true, false>(band_yface_zi, a, cndD, zp, side[1]);
+      launch_de_band<true, false>(band_xzedge, a, cndD, zp, side[4]);
+      launch_de_band<false, true>(band_yzedge, a, cndD, zp, side[5]);
       launch_de_band<true, true>(band_xyedge, a, cndD, zp, side[3]);
       join();
     }
@@ -1563,6 +1662,7 @@ public:
     if ((int)mons.size() <= id) mons.resize(id + 1);
     const Monitor &m = p.monitors[id];
     DMon &dm = mons[id];
+    bump(id);
     dm.acc = dzeros<double2>(m.npts * m.freq.size());
     dm.ph = dalloc<double2>(m.freq.size());
     dm.freq = dupload(m.freq);
@@ -1802,6 +1902,7 @@ public:
   void dft(Plan &p, int id, double time, int64_t tn) {
     const Monitor &m = p.monitors[id];
     DMon &dm = mons[id];
+    bump(id);
     int nf = (int)m.freq.size();
     DftArgs<R> a{};
     a.f = f[m.c];
@@ -1867,6 +1968,7 @@ public:
       dip.re[k] = vals[k].dip_e.real();
       dip.im[k] = vals[k].dip_e.imag();
     }
+    check_finite();
     if (fused_mask >= 0) fused_step(p, curb, curd, dip);
     else {
       // per part (real, then imaginary for complex fields): the B half-step,
@@ -1911,6 +2013,7 @@ public:
       double time = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? timeE - 0.5 * p.dt : timeE;
       dft(p, (int)id, time, tn);
     }
+    if (finite_every > 0 && tn % finite_every == 0) launch_finite_probe(p);
   }
 
   void begin_steps() override {
@@ -1924,10 +2027,14 @@ public:
     ms = fms;
     cuda_check(cudaGetLastError(), "kernel launch");
     check_tc();
+    check_finite();
   }
   double last_step_ms() const override { return ms; }
   long long launches() const override { return nlaunch; }
-  void synchronize() override { cuda_check(cudaStreamSynchronize(stream), "sync"); }
+  void synchronize() override {
+    cuda_check(cudaStreamSynchronize(stream), "sync");
+    check_finite();
+  }
 
   // ------------------------------------------------------------ adjoint
   std::vector<int> dcomps;       // design E components
@@ -2314,7 +2421,38 @@ public:
     check_tc();
   }
 
+  // Version of each monitor's sums, bumped by every change (a sample, set_dft,
+  // scale_dft).  flux() returns its previous result for the same monitor
+  // pairs while their versions are unchanged: the spectrum is a function of
+  // the sums alone, so a caller reading the flux after every step (with a
+  // decimated monitor) costs no device work or synchronisation on the steps
+  // that add no sample.
+  std::vector<unsigned long long> mon_ver;
+  struct FluxMemo {
+    std::vector<int> e, h;
+    std::vector<unsigned long long> v;
+    std::vector<double> out;
+  };
+  std::vector<FluxMemo> flux_memo;
+  unsigned long long &ver(int id) {
+    if ((size_t)id >= mon_ver.size()) mon_ver.resize(id + 1, 0);
+    return mon_ver[id];
+  }
+  void bump(int id) { ver(id)++; }
+
   void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) override {
+    FluxMemo key;
+    key.e.assign(idE, idE + npairs);
+    key.h.assign(idH, idH + npairs);
+    for (int q = 0; q < npairs; q++) {
+      key.v.push_back(ver(idE[q]));
+      key.v.push_back(ver(idH[q]));
+    }
+    for (const FluxMemo &m : flux_memo)
+      if (m.e == key.e && m.h == key.h && m.v == key.v) {
+        std::copy(m.out.begin(), m.out.end(), out);
+        return;
+      }
     for (int q = 0; q < npairs; q++) {
       dft_flush(p, idE[q]);
       dft_flush(p, idH[q]);
@@ -2340,10 +2478,14 @@ public:
                "download flux");
     cuda_check(cudaStreamSynchronize(stream), "flux sync");
     check_tc();
+    key.out.assign(out, out + nf);
+    if (flux_memo.size() >= 8) flux_memo.erase(flux_memo.begin());
+    flux_memo.push_back(std::move(key));
   }
 
   void set_dft(Plan &p, int id, const double *in) override {
     dft_flush(p, id);
+    bump(id);
     const Monitor &m = p.monitors[id];
     cuda_check(cudaMemcpyAsync(mons[id].acc, in, m.npts * m.freq.size() * sizeof(double2), cudaMemcpyHostToDevice,
                                stream),
@@ -2354,6 +2496,7 @@ public:
 
   void scale_dft(Plan &p, int id, std::complex<double> sc) override {
     dft_flush(p, id);
+    bump(id);
     const Monitor &m = p.monitors[id];
     scale_device(mons[id].acc, (long long)(m.npts * m.freq.size()), sc.real(), sc.imag(), stream, nlaunch);
     cuda_check(cudaStreamSynchronize(stream), "scale sync");

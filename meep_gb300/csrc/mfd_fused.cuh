@@ -44,6 +44,15 @@ template <typename R> struct FusedArgs {
   R *fmp[3];
   const R *chio[3][2];
   int noff[3], odir[3][2], osx[3][2];
+  // activity bits per run of 32 consecutive z points (row segment, aligned on
+  // z = 0, 32, ...): bit 3q+d pole q has a nonzero sigma on E_d somewhere in
+  // the segment, bit 12+d (15+d) D_d (B_d) has a nonzero conductivity there.
+  // A pole with zero sigma keeps P = P_prev = 0 and a zero conductivity
+  // leaves (1 - dt/2 sigma) f - dt curl and its condinv product unchanged, so
+  // the 3-D band kernels skip those loads outside the f_cond branch.  Null:
+  // everything active.
+  const unsigned *amask;
+  int mext1, mnseg;
   __device__ __forceinline__ R tbs(int d, int p) const { return sig[d][p]; }
   __device__ __forceinline__ R tbk(int d, int p) const { return kap[d][p]; }
   __device__ __forceinline__ R tbsi(int d, int p) const { return siginv[d][p]; }

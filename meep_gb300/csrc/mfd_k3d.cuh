@@ -141,6 +141,16 @@ __device__ __forceinline__ bool chunk_has(unsigned mask, int rx, int ry, int rz)
   return (mask >> (rx * 9 + ry * 3 + rz)) & 1u;
 }
 
+// activity bits of the row segment holding point k (FusedArgs::amask)
+constexpr int AM_DCOND = 12, AM_BCOND = 15;
+template <typename R> __device__ __forceinline__ unsigned seg_active(const FusedArgs<R> &a, const int k[3]) {
+  return a.amask ? __ldg(a.amask + ((size_t)k[0] * a.mext1 + k[1]) * a.mnseg + (k[2] >> 5)) : ~0u;
+}
+template <typename R>
+__device__ __forceinline__ bool pole_on(const FusedArgs<R> &a, unsigned am, int q, int dc) {
+  return q < a.npoles && a.P[q][dc] && ((am >> (3 * q + dc)) & 1u);
+}
+
 // B -= dtdx * curl E with PML / conductivity branches, then H inside the
 // slab along its own direction (update_eh through f_w)
 template <typename R, bool CND, bool FX, bool FY, bool FZ>
@@ -163,9 +173,10 @@ __device__ __forceinline__ void b3_point(const FusedArgs<R> &a, const int k[3]) 
   const int p0x = 2 * k[0], p1x = p0x + 1, p0y = 2 * k[1], p1y = p0y + 1, p0z = 2 * k[2], p1z = p0z + 1;
   // Bx at (0,1,1): dsig = Y, dsigu = Z
   bool hcx = CND && a.cnd[3][0] != nullptr, hcy = CND && a.cnd[3][1] != nullptr, hcz = CND && a.cnd[3][2] != nullptr;
-  if (hcx && F.s1[1]) hcx = chunk_has(a.cond_chunks[3][0], F.r0[0], F.r1[1], F.r1[2]);
-  if (hcy && F.s1[2]) hcy = chunk_has(a.cond_chunks[3][1], F.r1[0], F.r0[1], F.r1[2]);
-  if (hcz && F.s1[0]) hcz = chunk_has(a.cond_chunks[3][2], F.r1[0], F.r1[1], F.r0[2]);
+  const unsigned am = CND ? seg_active(a, k) : 0u;
+  if (hcx) hcx = F.s1[1] ? chunk_has(a.cond_chunks[3][0], F.r0[0], F.r1[1], F.r1[2]) : ((am >> (AM_BCOND + 0)) & 1u);
+  if (hcy) hcy = F.s1[2] ? chunk_has(a.cond_chunks[3][1], F.r1[0], F.r0[1], F.r1[2]) : ((am >> (AM_BCOND + 1)) & 1u);
+  if (hcz) hcz = F.s1[0] ? chunk_has(a.cond_chunks[3][2], F.r1[0], F.r1[1], F.r0[2]) : ((am >> (AM_BCOND + 2)) & 1u);
   // every field-sized operand of the point before any branch
   const CurlIn<R> inx = curl_in(F.s1[1], F.s1[2], hcx, a.fu[3][0], a.fcnd[3][0], a.cnd[3][0], a.cndinv[3][0], i);
   const CurlIn<R> iny = curl_in(F.s1[2], F.s1[0], hcy, a.fu[3][1], a.fcnd[3][1], a.cnd[3][1], a.cndinv[3][1], i);
@@ -239,13 +250,14 @@ template <typename R> struct EShell {
 // everything loaded and computed, nothing stored (so the loads of all three
 // components are in flight together)
 template <typename R, bool POLES>
-__device__ __forceinline__ EShell<R> e_general(const FusedArgs<R> &a, int dc, int i, R dn, bool slabw, int pw) {
+__device__ __forceinline__ EShell<R> e_general(const FusedArgs<R> &a, int dc, int i, R dn, bool slabw, int pw,
+                                               unsigned am) {
   EShell<R> o;
   R gs = dn;
   if (POLES) {
 #pragma unroll
     for (int q = 0; q < MAX_POLES; q++)
-      if (q < a.npoles && a.P[q][dc]) {
+      if (pole_on(a, am, q, dc)) {
         o.pc[q] = a.P[q][dc][i];
         gs -= o.pc[q];
       }
@@ -269,7 +281,7 @@ __device__ __forceinline__ EShell<R> e_general(const FusedArgs<R> &a, int dc, in
   if (POLES) {
 #pragma unroll
     for (int q = 0; q < MAX_POLES; q++)
-      if (q < a.npoles && a.P[q][dc])
+      if (pole_on(a, am, q, dc))
         o.pn[q] = a.pg1inv[q] * (o.pc[q] * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][dc][i] +
                                  a.pw0[q] * (a.ps[q][dc][i] * W));
   }
@@ -277,13 +289,13 @@ __device__ __forceinline__ EShell<R> e_general(const FusedArgs<R> &a, int dc, in
 }
 
 template <typename R, bool POLES>
-__device__ __forceinline__ void e_store(const FusedArgs<R> &a, int dc, int i, const EShell<R> &o) {
+__device__ __forceinline__ void e_store(const FusedArgs<R> &a, int dc, int i, const EShell<R> &o, unsigned am) {
   a.e[dc][i] = o.e;
   if (o.wfw) a.fw[0][dc][i] = o.fw;
   if (POLES) {
 #pragma unroll
     for (int q = 0; q < MAX_POLES; q++)
-      if (q < a.npoles && a.P[q][dc]) {
+      if (pole_on(a, am, q, dc)) {
         a.P[q][dc][i] = o.pn[q];
         a.PP[q][dc][i] = o.pc[q];
       }
@@ -349,12 +361,13 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
   const R dtdx = a.dtdx, dt2 = a.dt2;
   const int p0x = 2 * k[0], p1x = p0x + 1, p0y = 2 * k[1], p1y = p0y + 1, p0z = 2 * k[2], p1z = p0z + 1;
   bool hcx = CND && a.cnd[2][0] != nullptr, hcy = CND && a.cnd[2][1] != nullptr, hcz = CND && a.cnd[2][2] != nullptr;
+  const unsigned am = (CND || POLES) ? seg_active(a, k) : 0u;
   // Dx (1,0,0): dsig = Y (shift 0), dsigu = Z (shift 0)
-  if (hcx && F.s0[1]) hcx = chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]);
+  if (hcx) hcx = F.s0[1] ? chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]) : ((am >> (AM_DCOND + 0)) & 1u);
   // Dy (0,1,0): dsig = Z, dsigu = X
-  if (hcy && F.s0[2]) hcy = chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]);
+  if (hcy) hcy = F.s0[2] ? chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]) : ((am >> (AM_DCOND + 1)) & 1u);
   // Dz (0,0,1): dsig = X, dsigu = Y
-  if (hcz && F.s0[0]) hcz = chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]);
+  if (hcz) hcz = F.s0[0] ? chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]) : ((am >> (AM_DCOND + 2)) & 1u);
   const CurlIn<R> inx = curl_in(F.s0[1], F.s0[2], hcx, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i);
   const CurlIn<R> iny = curl_in(F.s0[2], F.s0[0], hcy, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i);
   const CurlIn<R> inz = curl_in(F.s0[0], F.s0[1], hcz, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i);
@@ -379,25 +392,25 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
   EShell<R> ox, oy, oz;
   if constexpr (POLES) {
     if (vx) {
-      ox = e_general<R, POLES>(a, 0, i, cx.f, F.s1[0], p1x);
+      ox = e_general<R, POLES>(a, 0, i, cx.f, F.s1[0], p1x, am);
       a.d[0][i] = cx.f;
       if (cx.wfu) a.fu[2][0][i] = cx.fu;
       if (cx.wfc) a.fcnd[2][0][i] = cx.fc;
-      e_store<R, POLES>(a, 0, i, ox);
+      e_store<R, POLES>(a, 0, i, ox, am);
     }
     if (vy) {
-      oy = e_general<R, POLES>(a, 1, i, cy.f, F.s1[1], p1y);
+      oy = e_general<R, POLES>(a, 1, i, cy.f, F.s1[1], p1y, am);
       a.d[1][i] = cy.f;
       if (cy.wfu) a.fu[2][1][i] = cy.fu;
       if (cy.wfc) a.fcnd[2][1][i] = cy.fc;
-      e_store<R, POLES>(a, 1, i, oy);
+      e_store<R, POLES>(a, 1, i, oy, am);
     }
     if (vz) {
-      oz = e_general<R, POLES>(a, 2, i, cz.f, F.s1[2], p1z);
+      oz = e_general<R, POLES>(a, 2, i, cz.f, F.s1[2], p1z, am);
       a.d[2][i] = cz.f;
       if (cz.wfu) a.fu[2][2][i] = cz.fu;
       if (cz.wfc) a.fcnd[2][2][i] = cz.fc;
-      e_store<R, POLES>(a, 2, i, oz);
+      e_store<R, POLES>(a, 2, i, oz, am);
     }
     return;
   }
@@ -408,19 +421,19 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
     a.d[0][i] = cx.f;
     if (cx.wfu) a.fu[2][0][i] = cx.fu;
     if (cx.wfc) a.fcnd[2][0][i] = cx.fc;
-    e_store<R, POLES>(a, 0, i, ox);
+    e_store<R, POLES>(a, 0, i, ox, am);
   }
   if (vy) {
     a.d[1][i] = cy.f;
     if (cy.wfu) a.fu[2][1][i] = cy.fu;
     if (cy.wfc) a.fcnd[2][1][i] = cy.fc;
-    e_store<R, POLES>(a, 1, i, oy);
+    e_store<R, POLES>(a, 1, i, oy, am);
   }
   if (vz) {
     a.d[2][i] = cz.f;
     if (cz.wfu) a.fu[2][2][i] = cz.fu;
     if (cz.wfc) a.fcnd[2][2][i] = cz.fc;
-    e_store<R, POLES>(a, 2, i, oz);
+    e_store<R, POLES>(a, 2, i, oz, am);
   }
 }
 
@@ -450,9 +463,10 @@ __device__ __forceinline__ void d3_point(const FusedArgs<R> &a, const int k[3]) 
   const R dtdx = a.dtdx, dt2 = a.dt2;
   const int p0x = 2 * k[0], p0y = 2 * k[1], p0z = 2 * k[2];
   bool hcx = CND && a.cnd[2][0] != nullptr, hcy = CND && a.cnd[2][1] != nullptr, hcz = CND && a.cnd[2][2] != nullptr;
-  if (hcx && F.s0[1]) hcx = chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]);
-  if (hcy && F.s0[2]) hcy = chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]);
-  if (hcz && F.s0[0]) hcz = chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]);
+  const unsigned am = seg_active(a, k);
+  if (hcx) hcx = F.s0[1] ? chunk_has(a.cond_chunks[2][0], F.r1[0], F.r0[1], F.r0[2]) : ((am >> (AM_DCOND + 0)) & 1u);
+  if (hcy) hcy = F.s0[2] ? chunk_has(a.cond_chunks[2][1], F.r0[0], F.r1[1], F.r0[2]) : ((am >> (AM_DCOND + 1)) & 1u);
+  if (hcz) hcz = F.s0[0] ? chunk_has(a.cond_chunks[2][2], F.r0[0], F.r0[1], F.r1[2]) : ((am >> (AM_DCOND + 2)) & 1u);
   const CurlIn<R> inx = curl_in(F.s0[1], F.s0[2], hcx, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i);
   const CurlIn<R> iny = curl_in(F.s0[2], F.s0[0], hcy, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i);
   const CurlIn<R> inz = curl_in(F.s0[0], F.s0[1], hcz, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i);
@@ -474,7 +488,7 @@ __device__ __forceinline__ void d3_point(const FusedArgs<R> &a, const int k[3]) 
       R g = c[dc].f;
 #pragma unroll
       for (int q = 0; q < MAX_POLES; q++)
-        if (q < a.npoles && a.P[q][dc]) g -= a.P[q][dc][i];
+        if (pole_on(a, am, q, dc)) g -= a.P[q][dc][i];
       a.fmp[dc][i] = g;
     }
   }
@@ -491,6 +505,7 @@ __device__ __forceinline__ void e3_point(const FusedArgs<R> &a, const int k[3]) 
   band_flags<R, FX, FY, FZ>(a, k, F);
   const bool v[3] = {k[1] >= 1 && k[2] >= 1, k[0] >= 1 && k[2] >= 1, k[0] >= 1 && k[1] >= 1};
   const int pw[3] = {2 * k[0] + 1, 2 * k[1] + 1, 2 * k[2] + 1};
+  const unsigned am = POLES ? seg_active(a, k) : 0u;
 #pragma unroll
   for (int dc = 0; dc < 3; dc++) {
     if (!v[dc]) continue;
@@ -524,13 +539,13 @@ __device__ __forceinline__ void e3_point(const FusedArgs<R> &a, const int k[3]) 
     if (POLES) {
 #pragma unroll
       for (int q = 0; q < MAX_POLES; q++)
-        if (q < a.npoles && a.P[q][dc]) {
+        if (pole_on(a, am, q, dc)) {
           o.pc[q] = a.P[q][dc][i];
           o.pn[q] = a.pg1inv[q] * (o.pc[q] * (R(2) - a.pw0d[q]) - a.pg1[q] * a.PP[q][dc][i] +
                                    a.pw0[q] * (a.ps[q][dc][i] * W));
         }
     }
-    e_store<R, POLES>(a, dc, i, o);
+    e_store<R, POLES>(a, dc, i, o, am);
   }
 }
 

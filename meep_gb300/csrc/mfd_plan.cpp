@@ -245,6 +245,40 @@ int64_t Plan::store_index_of_dense(int64_t di) const {
   return k[0] * stride[0] + k[1] * stride[1] + k[2] * stride[2];
 }
 
+Plan::ProbePoints Plan::center_probe(int d) const {
+  ProbePoints pp;
+  pp.n = 1;
+  pp.idx[0] = 0;
+  pp.w[0] = 1.0;
+  const int c = comp(MFD_E, d);
+  for (int e = 0; e < 3; e++) {
+    if (!present[e]) continue;
+    const int pc = N[e] - N[e] % 2; // icenter, relative to the low corner
+    const int s = shift[c][e];
+    int k0, nk;
+    if ((pc - s) % 2 == 0) {
+      k0 = (pc - s) / 2;
+      nk = 1;
+    }
+    else {
+      k0 = (pc - s - 1) / 2;
+      nk = 2;
+    }
+    ProbePoints q;
+    for (int i = 0; i < pp.n; i++)
+      for (int j = 0; j < nk; j++) {
+        const int k = k0 + j, pos = s + 2 * k;
+        // a point no chunk owns reads as zero (fields::get_field(c, ivec))
+        if (pos <= 0 || pos > 2 * N[e]) continue;
+        q.idx[q.n] = pp.idx[i] + k * stride[e];
+        q.w[q.n] = pp.w[i] * (nk == 2 ? 0.5 : 1.0);
+        q.n++;
+      }
+    pp = q;
+  }
+  return pp;
+}
+
 void Plan::dense_coords(int64_t di, int k[3]) const {
   k[2] = int(di % ext[2]);
   di /= ext[2];

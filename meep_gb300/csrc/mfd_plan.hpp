@@ -164,6 +164,23 @@ public:
     return 1;
   }
   bool in_slab(int d, int pos) const { return region(d, pos) != 1; }
+
+  // Divergence test of fields::step(): the reference aborts with "simulation
+  // fields are NaN or Inf" when get_field(D_EnergyDensity, gv.center()) is
+  // not finite (src/step.cpp:137-138), i.e. half the sum over the E
+  // components of E_d * D_d, each interpolated at the cell centre
+  // (src/monitor.cpp:76-91).  The centre is io + n rounded down to even
+  // (grid_volume::icenter, src/vec.cpp:1089-1101); a component reads the one
+  // or two Yee points around it per direction with weights 1 or 1/2, and
+  // drops zero weights (grid_volume::interpolate, src/vec.cpp:558-598).
+  // Returns the store indices and weights for E component direction d
+  // (the D component at the same Yee positions uses the same ones).
+  struct ProbePoints {
+    int n = 0;
+    int64_t idx[8] = {};
+    double w[8] = {};
+  };
+  ProbePoints center_probe(int d) const;
   int64_t dense_count() const { return ndense; }
   int64_t store_index_of_dense(int64_t di) const;
   void dense_coords(int64_t di, int k[3]) const;

@@ -15,7 +15,9 @@ the reference's default material-function method (sphere-quadrature normal,
 sampled means of eps and 1/eps, `subpixel_tol`, `subpixel_maxeval`): the
 reference's Python layer averages through libctl's analytic overlaps instead,
 so interface pixels differ from it at the level of the averaging tolerance.
-Averaging needs isotropic media.  Differences from the reference, raised as
+Averaging needs isotropic media.  Fields are double precision unless the
+environment sets MEEP_GB300_PRECISION=32 (the reference's single-precision
+build).  Differences from the reference, raised as
 errors where they would change results: no symmetries, no material functions
 (per-point Python callables).  `k_point` gives Bloch-periodic walls (complex
 fields when it is nonzero), as in the reference.
@@ -48,7 +50,21 @@ High, Low = 0, 1
 inf = 1.0e20
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-PRODUCT_LIB = os.path.join(_HERE, "lib", "libmeep_gb300.so")
+# The reference picks its floating-point type when it is built (realnum is
+# float with --enable-single); both builds ship here and MEEP_GB300_PRECISION
+# (64, the default, or 32) picks the one Simulation runs on.
+DOUBLE_LIB = os.path.join(_HERE, "lib", "libmeep_gb300.so")
+SINGLE_LIB = os.path.join(_HERE, "lib", "libmeep_gb300_single.so")
+
+
+def _product_lib():
+    prec = os.environ.get("MEEP_GB300_PRECISION", "64").strip()
+    if prec not in ("32", "64"):
+        raise ValueError("MEEP_GB300_PRECISION must be 32 or 64, not %r" % prec)
+    return SINGLE_LIB if prec == "32" else DOUBLE_LIB
+
+
+PRODUCT_LIB = DOUBLE_LIB
 
 
 class Vector3:
@@ -286,64 +302,100 @@ def _num_args(f):
         return 1
 
 
+# Step functions (the reference's python/simulation.py:5049-5160 semantics):
+# run() calls each with todo = "step" before every step and once with
+# todo = "finish" after the last.  A one-argument function f(sim) only sees
+# the steps; a two-argument f(sim, todo) sees both phases.  The combinators
+# below are small stateful callables that decide when to pass a phase on.
 def _eval_step_func(sim, func, todo):
-    n = _num_args(func)
-    if n == 1:
-        if todo == "step":
-            func(sim)
-    elif n == 2:
-        func(sim, todo)
-    else:
+    arity = _num_args(func)
+    if arity not in (1, 2):
         raise ValueError("Step function requires 1 or 2 arguments")
+    if arity == 2:
+        func(sim, todo)
+    elif todo == "step":
+        func(sim)
+
+
+class _Combinator:
+    """Base of the step-function combinators: forwards a phase to the
+    wrapped functions when `_due` says so."""
+
+    def __init__(self, funcs):
+        self.funcs = funcs
+
+    def _forward(self, sim, todo):
+        for func in self.funcs:
+            _eval_step_func(sim, func, todo)
+
+    def __call__(self, sim, todo):
+        raise NotImplementedError
+
+
+class _AtEvery(_Combinator):
+    # due once `interval` has passed since the last call that ran (half a
+    # time step of slack), and always at "finish"
+    def __init__(self, interval, funcs):
+        super().__init__(funcs)
+        self.interval = interval
+        self.last_run = 0.0
+
+    def __call__(self, sim, todo):
+        now = sim.round_time()
+        if todo != "finish" and now < self.last_run + self.interval - 0.5 * sim.fields_dt:
+            return
+        self._forward(sim, todo)
+        self.last_run = now
+
+
+class _AtEnd(_Combinator):
+    # only at "finish": one "step" call, then the "finish" call
+    def __call__(self, sim, todo):
+        if todo == "finish":
+            self._forward(sim, "step")
+            self._forward(sim, "finish")
+
+
+class _AtBeginning(_Combinator):
+    # only the first phase it sees
+    def __init__(self, funcs):
+        super().__init__(funcs)
+        self.done = False
+
+    def __call__(self, sim, todo):
+        if not self.done:
+            self._forward(sim, todo)
+            self.done = True
+
+
+class _AfterTime(_Combinator):
+    # every phase from `delay` after the first call on
+    def __init__(self, delay, funcs):
+        super().__init__(funcs)
+        self.delay = delay
+        self.start = None
+
+    def __call__(self, sim, todo):
+        if self.start is None:
+            self.start = sim.round_time()
+        if todo == "finish" or sim.round_time() >= self.start + self.delay:
+            self._forward(sim, todo)
 
 
 def at_every(dt, *step_funcs):
-    closure = {"tlast": 0.0}
-
-    def _every(sim, todo):
-        t = sim.round_time()
-        if todo == "finish" or t >= closure["tlast"] + dt + (-0.5 * sim.fields_dt):
-            for func in step_funcs:
-                _eval_step_func(sim, func, todo)
-            closure["tlast"] = t
-
-    return _every
+    return _AtEvery(dt, step_funcs)
 
 
 def at_end(*step_funcs):
-    def _end(sim, todo):
-        if todo == "finish":
-            for func in step_funcs:
-                _eval_step_func(sim, func, "step")
-            for func in step_funcs:
-                _eval_step_func(sim, func, "finish")
-
-    return _end
+    return _AtEnd(step_funcs)
 
 
 def at_beginning(*step_funcs):
-    closure = {"done": False}
-
-    def _beg(sim, todo):
-        if not closure["done"]:
-            for f in step_funcs:
-                _eval_step_func(sim, f, todo)
-            closure["done"] = True
-
-    return _beg
+    return _AtBeginning(step_funcs)
 
 
 def after_time(t, *step_funcs):
-    closure = {"t0": None}
-
-    def _after(sim, todo):
-        if closure["t0"] is None:
-            closure["t0"] = sim.round_time()
-        if todo == "finish" or sim.round_time() >= closure["t0"] + t:
-            for f in step_funcs:
-                _eval_step_func(sim, f, todo)
-
-    return _after
+    return _AfterTime(t, step_funcs)
 
 
 # ---------------------------------------------------------------- binding
@@ -553,7 +605,7 @@ class Simulation:
         self.k_point = _v3(k_point) if k_point not in (False, None) else False
         self.Courant = float(Courant)
         self.dft_objects = []
-        self._lib = _load(_library or PRODUCT_LIB)
+        self._lib = _load(_library or _product_lib())
         self._h = None
 
     # -------------------------------------------------------------- setup

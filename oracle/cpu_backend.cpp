@@ -597,6 +597,30 @@ public:
       update_dft(p, (int)id, time);
     }
     ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (!std::isfinite(center_energy(p))) throw Error("simulation fields are NaN or Inf");
+  }
+
+  // get_field(D_EnergyDensity, gv.center()) of fields::step()'s divergence
+  // test (src/step.cpp:137-138): half the sum of Re(conj(E_d) D_d) with both
+  // interpolated at the centre (Plan::center_probe)
+  double center_energy(const Plan &p) const {
+    double sum = 0.0;
+    for (int d = 0; d < 3; d++) {
+      const int ce = comp(MFD_E, d), cd = comp(MFD_D, d);
+      if (!p.have[ce] || !p.have[cd]) continue;
+      const Plan::ProbePoints pp = p.center_probe(d);
+      double er = 0, dr = 0, ei = 0, dimg = 0;
+      for (int j = 0; j < pp.n; j++) {
+        er += pp.w[j] * double(f[ce][pp.idx[j]]);
+        dr += pp.w[j] * double(f[cd][pp.idx[j]]);
+        if (cplx) {
+          ei += pp.w[j] * double(f_im[ce][pp.idx[j]]);
+          dimg += pp.w[j] * double(f_im[cd][pp.idx[j]]);
+        }
+      }
+      sum += er * dr + ei * dimg;
+    }
+    return sum * 0.5;
   }
 
   void begin_steps() override { ms = 0; }

@@ -187,6 +187,121 @@ static void case_disp3d(Writer &w, int nx, int ny, int nz, double res, double dp
   }
 }
 
+/* One z plane (point index kz along z) of component c: every `every`-th of
+   the (nx+1)(ny+1) points of its own Yee grid in x-slowest order. */
+static std::vector<double> plane_field(fields &f, const grid_volume &gv, component c, int kz, int every = 7) {
+  std::vector<double> out;
+  ivec p0 = gv.little_corner() + gv.iyee_shift(c);
+  long long n = 0;
+  for (int a = 0; a <= gv.nx(); a++)
+    for (int b = 0; b <= gv.ny(); b++) {
+      if (n++ % every) continue;
+      ivec p = p0;
+      p.set_direction(X, p0.in_direction(X) + 2 * a);
+      p.set_direction(Y, p0.in_direction(Y) + 2 * b);
+      p.set_direction(Z, p0.in_direction(Z) + 2 * kz);
+      out.push_back(real(f.get_field(c, p, false)));
+    }
+  return out;
+}
+
+/* Large DFT monitors in a few numbers: per frequency the sum of |F|^2 over
+   every point and the projection sum_k r_k F_k onto signs r_k = +-1 drawn
+   from a hash of the point's ivec coordinates (both complex sums, order
+   independent to rounding); plus the full spectra of every point whose
+   coordinates hash into one residue class mod `every` (coordinates, then
+   Re, Im per frequency). */
+static uint64_t coord_hash(const ivec &p) {
+  uint64_t h = 1469598103934665603ull;
+  LOOP_OVER_DIRECTIONS(p.dim, d) {
+    h ^= (uint64_t)(uint32_t)(p.in_direction(d) + 100000);
+    h *= 1099511628211ull;
+  }
+  return h ^ (h >> 29);
+}
+static void write_dft_summary(Writer &w, const std::string &name, dft_chunk *chunks, component c,
+                              const grid_volume &gv, int every) {
+  std::vector<double> norm2, proj, sample;
+  size_t nw = 0;
+  for (dft_chunk *ch = chunks; ch; ch = ch->next_in_dft) {
+    if (ch->c != c) continue;
+    nw = ch->omega.size();
+    if (norm2.empty()) {
+      norm2.assign(nw, 0.0);
+      proj.assign(2 * nw, 0.0);
+    }
+    int cnt[3] = {1, 1, 1};
+    direction ds[3];
+    int nd = 0;
+    LOOP_OVER_DIRECTIONS(gv.dim, d) {
+      ds[nd] = d;
+      cnt[nd] = (ch->ie.in_direction(d) - ch->is.in_direction(d)) / 2 + 1;
+      nd++;
+    }
+    size_t idx = 0;
+    for (int a = 0; a < cnt[0]; a++)
+      for (int b = 0; b < cnt[1]; b++)
+        for (int e = 0; e < cnt[2]; e++, idx++) {
+          ivec p = ch->is;
+          int k[3] = {a, b, e};
+          for (int q = 0; q < nd; q++)
+            p.set_direction(ds[q], ch->is.in_direction(ds[q]) + 2 * k[q]);
+          const uint64_t h = coord_hash(p);
+          const double r = (h & 1) ? 1.0 : -1.0;
+          const bool keep = (h >> 1) % (uint64_t)every == 0;
+          if (keep)
+            for (int q = 0; q < nd; q++)
+              sample.push_back(p.in_direction(ds[q]));
+          for (size_t q = 0; q < nw; q++) {
+            const complex<double> v(ch->dft[idx * nw + q]);
+            norm2[q] += std::norm(v);
+            proj[2 * q] += r * v.real();
+            proj[2 * q + 1] += r * v.imag();
+            if (keep) {
+              sample.push_back(v.real());
+              sample.push_back(v.imag());
+            }
+          }
+        }
+  }
+  w.rec(name + "_norm2", norm2);
+  w.rec(name + "_proj", proj);
+  w.rec(name + "_sample", sample);
+}
+
+/* The benchmark workloads at full size, a few hundred steps (until the
+   pulse has crossed the monitors): the 256^3 non-dispersive case (flux
+   spectrum from 10 decimated samples, field planes at the flux plane, the
+   grid centre and inside the low z PML) and the 384 x 384 x 192 dispersive
+   case (six full 64-step blocks of the 200-frequency DFT of Ez on the whole
+   plane, field planes at the DFT plane, the source plane and inside the low
+   z PML).  Planes are every 7th point, DFT spectra a hashed sample. */
+static void case_vec3d_full_trunc(Writer &w, int steps) {
+  auto wl = make_vec3d(256, 256, 256, 20.0, 0.8, 60, 42, 200, 50);
+  run_steps(*wl, steps);
+  write_flux(w, *wl);
+  w.scalar("t", wl->f->time());
+  const component cs[4] = {Ex, Ey, Hx, Hz};
+  const char *names[4] = {"Ex", "Ey", "Hx", "Hz"};
+  const int planes[3] = {192, 128, 6};
+  for (int i = 0; i < 4; i++)
+    for (int kz : planes)
+      w.rec(std::string(names[i]) + "_z" + std::to_string(kz), plane_field(*wl->f, wl->gv, cs[i], kz));
+}
+
+static void case_disp3d_full_trunc(Writer &w, int steps) {
+  auto wl = make_disp3d(384, 384, 192, 20.0, 0.8, 200, 1);
+  run_steps(*wl, steps);
+  w.scalar("t", wl->f->time());
+  write_dft_summary(w, "dft_Ez", wl->dftf->chunks, Ez, wl->gv, 1999);
+  const component cs[3] = {Ex, Ez, Hy};
+  const char *names[3] = {"Ex", "Ez", "Hy"};
+  const int planes[3] = {72, 144, 6};
+  for (int i = 0; i < 3; i++)
+    for (int kz : planes)
+      w.rec(std::string(names[i]) + "_z" + std::to_string(kz), plane_field(*wl->f, wl->gv, cs[i], kz));
+}
+
 /* Known answers from the reference's own test suite (tests/known_results.cpp)
    that lie on this path: 2-D TM metallic and PML, 3-D metallic, 1-D Lorentz
    polariton.  Same structures, sources and run lengths. */
@@ -1286,6 +1401,10 @@ int main(int argc, char **argv) {
     case_vec3d(w, 24, 20, 18, 20.0, 0.25, 6, 42, steps > 0 ? steps : 1200, 10, 9, true);
   else if (cs == "vec3d_full")
     case_vec3d(w, 256, 256, 256, 20.0, 0.8, 60, 42, steps > 0 ? steps : 1000, 200, 50, false);
+  else if (cs == "vec3d_full_trunc")
+    case_vec3d_full_trunc(w, steps > 0 ? steps : 600);
+  else if (cs == "disp3d_full_trunc")
+    case_disp3d_full_trunc(w, steps > 0 ? steps : 384);
   else if (cs == "disp3d_small")
     case_disp3d(w, 20, 18, 16, 20.0, 0.25, steps > 0 ? steps : 600, 7, true, 1);
   else if (cs == "known")

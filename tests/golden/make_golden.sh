@@ -1,8 +1,9 @@
 #!/bin/sh
 # Regenerates the golden fixtures in this directory from the reference core
-# built by oracle/ref/Makefile (needs the reference sources; run in the build
-# container, not on the GPU host).  Each case is written twice: by the FP64
-# (.f64.bin) and by the FP32 (.f32.bin) reference build.
+# built by oracle/ref/Makefile (needs the reference sources: set
+# MEEP_REFERENCE to the reference checkout; not on the GPU host).  Each case
+# is written twice: by the FP64 (.f64.bin) and by the FP32 (.f32.bin)
+# reference build.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 ROOT=$(cd "$HERE/../.." && pwd)

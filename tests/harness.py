@@ -30,10 +30,20 @@ def run_driver(exe, case, tmpdir, steps=None, threads=8):
 
 def relerr(a, b):
     """max |a - b| / max |b| (infinity-norm relative error, as the reference's
-    ApproxComparisonTestCase.assertClose does, python/tests/utils.py:10-29)."""
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    ApproxComparisonTestCase.assertClose does, python/tests/utils.py:10-29).
+    Complex inputs are compared as complex numbers (|a - b| is the modulus
+    of the difference), so the imaginary parts count."""
+    a = np.asarray(a)
+    b = np.asarray(b)
     assert a.shape == b.shape, (a.shape, b.shape)
+    if np.iscomplexobj(a) or np.iscomplexobj(b):
+        a = a.astype(np.complex128)
+        b = b.astype(np.complex128)
+    else:
+        a = a.astype(np.float64)
+        b = b.astype(np.float64)
+    if a.size == 0:
+        return 0.0
     m = np.abs(b).max()
     return float(np.abs(a - b).max() / m) if m > 0 else float(np.abs(a - b).max())
 
@@ -70,7 +80,8 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
-                   nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True):
+                   nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True,
+                   boxed=False):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -79,7 +90,10 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     sums after `steps` steps; `n` overrides the random grid size.  offdiag:
     off-diagonal inverse permittivities on 40% of the points (Ex: xy and xz,
     Ey: yz only, Ez: zy only -- the reference's 3x3, 2x2 and swapped 2x2
-    cases); ecur=False makes every E source integrated (no D current)."""
+    cases); ecur=False makes every E source integrated (no D current).
+    boxed: conductivities and pole strengths are zero outside random boxes
+    (separate ones per array), so long grids hold runs of points where a
+    pole or a conductivity is absent next to runs where it is present."""
     rng = np.random.default_rng(seed)
     nrand = n
     if dim == 2:
@@ -116,17 +130,29 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
             for d in dirs:
                 arr = np.where(rng.uniform(size=shape) < 0.4, rng.uniform(-0.08, 0.08, size=shape), 0.0)
                 sim.set_chi1inv(c, d, arr)
+    def box_mask():
+        m = np.zeros(shape, dtype=bool)
+        lo = [int(rng.integers(0, max(1, e // 2))) for e in shape]
+        hi = [lo[d] + int(rng.integers(1, shape[d] - lo[d] + 1)) for d in range(3)]
+        m[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] = True
+        return m
+
     if cond:
         for c in comps:
             if c // 3 == _lib.D:
                 arr = np.where(rng.uniform(size=shape) < 0.3, rng.uniform(0, 0.5, size=shape), 0.0)
+                if boxed:
+                    arr = np.where(box_mask(), rng.uniform(0, 0.5, size=shape), 0.0)
                 sim.set_conductivity(c, arr)
     if poles:
         for (w0, g, dr) in ((1e-5, 0.05, True), (0.8, 0.1, False)):
             sig = []
             for d in range(3):
                 c = _lib.comp(_lib.E, d)
-                sig.append(rng.uniform(0, 2.0, size=shape) if c in comps else None)
+                arr = rng.uniform(0, 2.0, size=shape) if c in comps else None
+                if boxed and arr is not None:
+                    arr = np.where(box_mask(), arr, 0.0)
+                sig.append(arr)
             sim.add_lorentzian(w0, g, dr, sig)
     ecomps = [c for c in comps if c // 3 == _lib.E]
     s_int = sim.add_gaussian_src(0.6, 2.0, integrated=True)

@@ -192,3 +192,18 @@ def test_integrated_source_planewave_on_oracle(oracle_meep_lib):
 @pytest.mark.gpu
 def test_integrated_source_planewave_on_gpu(engine_lib):
     assert abs(integrated_source_std(PRODUCT_LIB)) < 1e-8
+
+
+def test_precision_from_environment(monkeypatch):
+    """MEEP_GB300_PRECISION picks the drop-in build Simulation loads (the
+    reference picks realnum when it is built)."""
+    from meep_gb300 import simulation as sm
+    monkeypatch.delenv("MEEP_GB300_PRECISION", raising=False)
+    assert sm._product_lib() == sm.DOUBLE_LIB
+    monkeypatch.setenv("MEEP_GB300_PRECISION", "32")
+    assert sm._product_lib() == sm.SINGLE_LIB
+    monkeypatch.setenv("MEEP_GB300_PRECISION", "64")
+    assert sm._product_lib() == sm.DOUBLE_LIB
+    monkeypatch.setenv("MEEP_GB300_PRECISION", "16")
+    with pytest.raises(ValueError):
+        sm._product_lib()
