@@ -229,9 +229,10 @@ int mfd_subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const d
 
 /* Allocation-free flux reduction.  No counterpart in the reference: it is the
  * reduction of mfd_flux (sum_k Re(E conj H) per frequency) for callers that
- * must not allocate device memory when they call it -- code recording a CUDA
- * graph, hosts whose device memory belongs to another allocator, loops that
- * cannot take the device synchronisation of cudaMalloc/cudaFree.  Inputs are
+ * must not allocate device memory when they call it -- hosts whose device
+ * memory belongs to another allocator (a framework's caching pool, an FFI
+ * host that hands out pre-allocated buffers), loops that cannot take the
+ * device synchronisation of cudaMalloc/cudaFree.  Inputs are
  * device pointers to two DFT sum arrays laid out as this engine keeps them
  * (npts * nfreq complex doubles, point-major, i.e. mfd_get_dft's layout), the
  * output a device pointer to nfreq doubles; `stream` is a cudaStream_t (NULL
@@ -239,8 +240,10 @@ int mfd_subpixel_rows(int dim, int cdir, int64_t npix, const double *lo, const d
  * (MFD_NOALLOC_MAX_PARTS rows of MFD_NOALLOC_MAX_FREQ doubles) shared by every
  * call on a device: nfreq above MFD_NOALLOC_MAX_FREQ is rejected, and calls
  * that overlap on the GPU race on it.  The first call on a device looks up the
- * array's address (cudaGetSymbolAddress) with that device current; make it
- * before any stream capture.  Errors: mfd_noalloc_last_error(). */
+ * array's address (cudaGetSymbolAddress) with that device current and keeps
+ * it; make that first call before any stream capture.  The address belongs
+ * to the device's context: after cudaDeviceReset the library must be
+ * reloaded before it is called again.  Errors: mfd_noalloc_last_error(). */
 #define MFD_NOALLOC_MAX_FREQ 1024
 #define MFD_NOALLOC_MAX_PARTS 256
 int mfd_flux_noalloc(const double *dft_E, const double *dft_H, int64_t npts, int nfreq, double *flux_out,

@@ -1172,13 +1172,13 @@ public:
     else b3_band_kernel<R, false, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
     nlaunch++;
   }
-  template <bool FX, bool FY, bool POLES>
+  template <bool FX, bool FY, int NP>
   void launch_de_band_p(const Band &bd, const dim3 &g, const dim3 &blk, const FusedArgs<R> &a, bool cnd, bool zp,
                         cudaStream_t st) {
-    if (cnd && zp) de3_band_kernel<R, true, POLES, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
-    else if (cnd) de3_band_kernel<R, true, POLES, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
-    else if (zp) de3_band_kernel<R, false, POLES, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
-    else de3_band_kernel<R, false, POLES, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    if (cnd && zp) de3_band_kernel<R, true, NP, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else if (cnd) de3_band_kernel<R, true, NP, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
+    else if (zp) de3_band_kernel<R, false, NP, FX, FY, true><<<g, blk, 0, st>>>(a, bd);
+    else de3_band_kernel<R, false, NP, FX, FY, false><<<g, blk, 0, st>>>(a, bd);
   }
   // ZCAN: the band can hold z slab points (the z flags are computed when the
   // grid has a z PML)
@@ -1188,8 +1188,11 @@ public:
     dim3 g, blk;
     band_shape(bd, g, blk);
     if (g.x == 0) return;
-    if (a.npoles > 0) launch_de_band_p<FX, FY, true>(bd, g, blk, a, cnd, zp, st);
-    else launch_de_band_p<FX, FY, false>(bd, g, blk, a, cnd, zp, st);
+    // up to two poles in registers, more one component after the other
+    if (a.npoles == 1) launch_de_band_p<FX, FY, 1>(bd, g, blk, a, cnd, zp, st);
+    else if (a.npoles == 2) launch_de_band_p<FX, FY, 2>(bd, g, blk, a, cnd, zp, st);
+    else if (a.npoles > 2) launch_de_band_p<FX, FY, -1>(bd, g, blk, a, cnd, zp, st);
+    else launch_de_band_p<FX, FY, 0>(bd, g, blk, a, cnd, zp, st);
     nlaunch++;
   }
 
@@ -1272,9 +1275,8 @@ public:
   }
 
   dim3 core_grid() const {
-    const int nz = qcore.zend - qcore.lo[2];
-    if (qcore.n[0] <= 0 || qcore.n[1] <= 0 || nz <= 0) return dim3(0, 0, 0);
-    return dim3((unsigned)((nz / 4 + 31) / 32), (unsigned)((qcore.n[1] + 7) / 8), (unsigned)qcore.n[0]);
+    if (qcore.total <= 0) return dim3(0, 0, 0);
+    return dim3((unsigned)((qcore.total + 255) / 256), 1, 1);
   }
 
   static void add_box(BoxList &L, const int lo[3], const int hi[3], int dim, dim3 blk) {
@@ -1359,6 +1361,10 @@ public:
       qcore.n[1] = yhi - ylo + 1;
       qcore.lo[2] = (std::max(p.T[2][0] + 1, 1) + 3) / 4 * 4;
       qcore.zend = std::max((p.N[2] - p.T[2][1]) / 4 * 4, qcore.lo[2]);
+      qcore.nq = (qcore.zend - qcore.lo[2]) / 4;
+      qcore.total = qcore.nq > 0 && qcore.n[0] > 0 && qcore.n[1] > 0
+                        ? (long long)qcore.n[0] * qcore.n[1] * qcore.nq
+                        : 0;
       band_zend = Band{{span_run(xlo, xhi), span_run(ylo, yhi),
                         qcore.zend > qcore.lo[2] ? span_outside(p.N[2], qcore.lo[2], qcore.zend - 1)
                                                  : span_run(0, p.N[2] - 1)}};
@@ -1486,8 +1492,8 @@ public:
       if constexpr (F32) {
         const dim3 g = core_grid();
         if (g.x) {
-          if (cndB) b3q_core_kernel<true><<<g, dim3(32, 8, 1), 0, stream>>>(a, qcore);
-          else b3q_core_kernel<false><<<g, dim3(32, 8, 1), 0, stream>>>(a, qcore);
+          if (cndB) b3q_core_kernel<true><<<g, 256, 0, stream>>>(a, qcore);
+          else b3q_core_kernel<false><<<g, 256, 0, stream>>>(a, qcore);
           nlaunch++;
         }
         launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);

@@ -333,8 +333,84 @@ __device__ __forceinline__ EShell<R> e_from(const FusedArgs<R> &a, int dc, R dn,
   return o;
 }
 
-template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
+// The E operands of one component with NP poles held in registers (NP = 1
+// or 2), loaded with the curl operands before any store so that every load
+// of the point is in flight at once: chi, E and f_w in the component's own
+// slab, and for each pole active in the row segment P, P_prev and sigma.
+template <typename R, int NP> struct EPoleIn {
+  R us, fw, e;
+  R p[NP], pp[NP], s[NP];
+  bool on[NP];
+};
+template <typename R, int NP>
+__device__ __forceinline__ EPoleIn<R, NP> epole_in(const FusedArgs<R> &a, int dc, int i, bool v, bool slabw,
+                                                   unsigned am) {
+  EPoleIn<R, NP> o;
+  o.us = v ? a.chi[dc][i] : R(0);
+  o.fw = (v && slabw) ? a.fw[0][dc][i] : R(0);
+  o.e = (v && slabw) ? a.e[dc][i] : R(0);
+#pragma unroll
+  for (int q = 0; q < NP; q++) {
+    o.on[q] = v && pole_on(a, am, q, dc);
+    o.p[q] = o.on[q] ? a.P[q][dc][i] : R(0);
+    o.pp[q] = o.on[q] ? a.PP[q][dc][i] : R(0);
+    o.s[q] = o.on[q] ? a.ps[q][dc][i] : R(0);
+  }
+  return o;
+}
+// E = chi (D - sum P) (through f_w in the slab), then the new P of each pole
+// with W = f_w or E: the arithmetic of e_general in the same order
+template <typename R, int NP> struct EPoleOut {
+  R e, fw;
+  bool wfw;
+  R pn[NP];
+};
+template <typename R, int NP>
+__device__ __forceinline__ EPoleOut<R, NP> epole_from(const FusedArgs<R> &a, int dc, R dn, bool slabw, int pw,
+                                                      const EPoleIn<R, NP> &in) {
+  EPoleOut<R, NP> o;
+  R gs = dn;
+#pragma unroll
+  for (int q = 0; q < NP; q++)
+    if (in.on[q]) gs -= in.p[q];
+  R W;
+  if (slabw) {
+    const R kk = a.kap[dc][pw], ss = a.sig[dc][pw];
+    const R fwn = (gs * in.us);
+    o.fw = fwn;
+    o.wfw = true;
+    o.e = in.e + ((kk + ss) * fwn - (kk - ss) * in.fw);
+    W = fwn;
+  }
+  else {
+    o.e = (gs * in.us);
+    o.fw = R(0);
+    o.wfw = false;
+    W = o.e;
+  }
+#pragma unroll
+  for (int q = 0; q < NP; q++)
+    o.pn[q] = a.pg1inv[q] * (in.p[q] * (R(2) - a.pw0d[q]) - a.pg1[q] * in.pp[q] + a.pw0[q] * (in.s[q] * W));
+  return o;
+}
+template <typename R, int NP>
+__device__ __forceinline__ void epole_store(const FusedArgs<R> &a, int dc, int i, const EPoleIn<R, NP> &in,
+                                            const EPoleOut<R, NP> &o) {
+  a.e[dc][i] = o.e;
+  if (o.wfw) a.fw[0][dc][i] = o.fw;
+#pragma unroll
+  for (int q = 0; q < NP; q++)
+    if (in.on[q]) {
+      a.P[q][dc][i] = o.pn[q];
+      a.PP[q][dc][i] = in.p[q];
+    }
+}
+
+// NP: number of poles held in registers (0 none, 1 or 2), or -1 for any
+// number, updated one component after the other
+template <typename R, bool CND, int NP, bool FX, bool FY, bool FZ>
 __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3]) {
+  constexpr bool POLES = NP != 0;
   const int sx = a.s[0], sy = a.s[1];
   const int i = k[0] * sx + k[1] * sy + k[2];
   ShellFlags<R> F;
@@ -371,13 +447,21 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
   const CurlIn<R> inx = curl_in(F.s0[1], F.s0[2], hcx, a.fu[2][0], a.fcnd[2][0], a.cnd[2][0], a.cndinv[2][0], i);
   const CurlIn<R> iny = curl_in(F.s0[2], F.s0[0], hcy, a.fu[2][1], a.fcnd[2][1], a.cnd[2][1], a.cndinv[2][1], i);
   const CurlIn<R> inz = curl_in(F.s0[0], F.s0[1], hcz, a.fu[2][2], a.fcnd[2][2], a.cnd[2][2], a.cndinv[2][2], i);
-  // without poles the E operands too (chi, and E and f_w inside the slab
-  // along the component's own direction)
+  // without poles, or with poles held in registers, the E operands too
+  // (chi, E and f_w inside the slab along the component's own direction,
+  // the poles' P, P_prev and sigma)
   EIn<R> ex, ey, ez;
   if constexpr (!POLES) {
     ex = e_in(a, 0, i, vx, F.s1[0]);
     ey = e_in(a, 1, i, vy, F.s1[1]);
     ez = e_in(a, 2, i, vz, F.s1[2]);
+  }
+  constexpr int NPR = NP > 0 ? NP : 1;
+  EPoleIn<R, NPR> qx, qy, qz;
+  if constexpr (NP > 0) {
+    qx = epole_in<R, NP>(a, 0, i, vx, F.s1[0], am);
+    qy = epole_in<R, NP>(a, 1, i, vy, F.s1[1], am);
+    qz = epole_in<R, NP>(a, 2, i, vz, F.s1[2], am);
   }
   const CurlRes<R> cx = curl_general(dx, Xx, dtdx, dt2, F.s0[1], F.s0[2], hcx, a.sig[1], a.kap[1], a.siginv[1], p0y,
                                      a.sig[2], a.kap[2], a.siginv[2], p0z, inx);
@@ -390,6 +474,31 @@ __device__ __forceinline__ void de3_point(const FusedArgs<R> &a, const int k[3])
   // (four more arrays per pole and component) one component after the other
   // keeps the registers, and so the occupancy, in bounds.
   EShell<R> ox, oy, oz;
+  if constexpr (NP > 0) {
+    EPoleOut<R, NPR> rx, ry, rz;
+    if (vx) rx = epole_from<R, NP>(a, 0, cx.f, F.s1[0], p1x, qx);
+    if (vy) ry = epole_from<R, NP>(a, 1, cy.f, F.s1[1], p1y, qy);
+    if (vz) rz = epole_from<R, NP>(a, 2, cz.f, F.s1[2], p1z, qz);
+    if (vx) {
+      a.d[0][i] = cx.f;
+      if (cx.wfu) a.fu[2][0][i] = cx.fu;
+      if (cx.wfc) a.fcnd[2][0][i] = cx.fc;
+      epole_store<R, NP>(a, 0, i, qx, rx);
+    }
+    if (vy) {
+      a.d[1][i] = cy.f;
+      if (cy.wfu) a.fu[2][1][i] = cy.fu;
+      if (cy.wfc) a.fcnd[2][1][i] = cy.fc;
+      epole_store<R, NP>(a, 1, i, qy, ry);
+    }
+    if (vz) {
+      a.d[2][i] = cz.f;
+      if (cz.wfu) a.fu[2][2][i] = cz.fu;
+      if (cz.wfc) a.fcnd[2][2][i] = cz.fc;
+      epole_store<R, NP>(a, 2, i, qz, rz);
+    }
+    return;
+  }
   if constexpr (POLES) {
     if (vx) {
       ox = e_general<R, POLES>(a, 0, i, cx.f, F.s1[0], p1x, am);
@@ -570,11 +679,13 @@ __global__ void __launch_bounds__(256, (FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8
   if (band_coords(bd, k)) b3_point<R, CND, FX, FY, FZ>(a, k);
 }
 
-template <typename R, bool CND, bool POLES, bool FX, bool FY, bool FZ>
-__global__ void __launch_bounds__(256, (FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8)
+// with poles in registers every operand of a point is loaded before any
+// store: 64 registers (half occupancy, each thread keeps ~30 loads in flight)
+template <typename R, bool CND, int NP, bool FX, bool FY, bool FZ>
+__global__ void __launch_bounds__(256, NP > 0 ? 4 : ((FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8))
     de3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];
-  if (band_coords(bd, k)) de3_point<R, CND, POLES, FX, FY, FZ>(a, k);
+  if (band_coords(bd, k)) de3_point<R, CND, NP, FX, FY, FZ>(a, k);
 }
 
 } // namespace cuda_impl

@@ -3,12 +3,11 @@
 // in a file-scope device array instead of memory the engine allocates.
 //
 // Who needs it: callers that may not allocate device memory at the moment
-// they reduce a spectrum -- code recording a CUDA graph (an allocation there
-// is not part of the graph and cudaMalloc/cudaFree synchronise the device),
-// hosts whose device memory is owned by another allocator (a framework's
-// caching pool, a JVM/FFI host that hands out pre-allocated buffers), and
-// latency-bound loops that cannot afford the implicit device synchronisation
-// of cudaMalloc/cudaFree.  They pass device buffers in and out and a stream.
+// they reduce a spectrum -- hosts whose device memory is owned by another
+// allocator (a framework's caching pool, a JVM/FFI host that hands out
+// pre-allocated buffers), and latency-bound loops that cannot afford the
+// implicit device synchronisation of cudaMalloc/cudaFree.  They pass device
+// buffers in and out and a stream.
 //
 // Limits: nfreq <= MFD_NOALLOC_MAX_FREQ and the scratch holds at most
 // MFD_NOALLOC_MAX_PARTS partial rows (larger monitors are folded into fewer,
@@ -19,7 +18,9 @@
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress (host code cannot use the symbol as a pointer), with
-// that device current; make that first call before any stream capture.
+// that device current, and keeps it; make that first call before any stream
+// capture.  The address is the device context's: after cudaDeviceReset the
+// library has to be reloaded before it is called again.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -42,23 +42,31 @@ __device__ __forceinline__ float4 q4step(const FusedArgs<float> &a, int t, int d
 }
 
 // The core: x and y interior, z interior rounded inwards to whole quads
-// (no PML slab and no metal wall in any direction).  A warp takes 128
-// consecutive z points of one row.
+// (no PML slab and no metal wall in any direction).  The quads of all core
+// rows are numbered row after row and a warp takes 32 consecutive ones, so
+// no lane idles at the end of a row (a row holds 38 quads in the 384^2 x 192
+// workload, 54 in the 256^3 one).
 struct QCore {
   int lo[3]; // first point (lo[2] a multiple of 4, >= 4)
   int n[2];  // x and y extents
   int zend;  // one past the last z point (a multiple of 4)
+  int nq;    // quads per row
+  long long total; // quads in the core
 };
 
 template <bool CND>
 __global__ void __launch_bounds__(256) b3q_core_kernel(const FusedArgs<float> a, const QCore b) {
-  if ((int)(blockIdx.y * 8 + threadIdx.y) >= b.n[1]) return; // whole warps (one row each)
-  const int k2 = b.lo[2] + 4 * (blockIdx.x * 32 + threadIdx.x);
-  const int k1 = b.lo[1] + blockIdx.y * 8 + threadIdx.y;
-  const int k0 = b.lo[0] + blockIdx.z;
-  // lanes past the end of the row load the row's first quad and store nothing
-  const bool on = k2 < b.zend;
-  const int i = k0 * a.s[0] + k1 * a.s[1] + (on ? k2 : b.lo[2]);
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  // threads past the end take the first quad (they join the shuffle) and
+  // store nothing
+  const bool on = t < b.total;
+  const long long tq = on ? t : 0;
+  const int q = (int)(tq % b.nq);
+  const long long row = tq / b.nq;
+  const int k2 = b.lo[2] + 4 * q;
+  const int k1 = b.lo[1] + (int)(row % b.n[1]);
+  const int k0 = b.lo[0] + (int)(row / b.n[1]);
+  const int i = k0 * a.s[0] + k1 * a.s[1] + k2;
   const int sx = a.s[0], sy = a.s[1];
   const float *__restrict__ Ex = a.e[0];
   const float *__restrict__ Ey = a.e[1];
@@ -67,10 +75,11 @@ __global__ void __launch_bounds__(256) b3q_core_kernel(const FusedArgs<float> a,
   const float4 ey = q4ld(Ey, i), eyx = q4ld(Ey, i + sx);
   const float4 ez = q4ld(Ez, i), ezx = q4ld(Ez, i + sx), ezy = q4ld(Ez, i + sy);
   const float4 bx = q4ld(a.b[0], i), by = q4ld(a.b[1], i), bz = q4ld(a.b[2], i);
-  // E one point up along z: the next lane's first element; the last lane of
-  // the warp and the last lane of the row load it (zend <= N: inside the row)
+  // E one point up along z: the next lane's first element when that lane
+  // holds the next quad of the same row; the last lane of the warp and the
+  // last quad of a row load it (zend <= N: inside the row)
   float nx = __shfl_down_sync(0xffffffffu, ex.x, 1), ny = __shfl_down_sync(0xffffffffu, ey.x, 1);
-  if (on && (threadIdx.x == 31 || k2 + 4 >= b.zend)) {
+  if (on && ((threadIdx.x & 31) == 31 || q == b.nq - 1)) {
     nx = Ex[i + 4];
     ny = Ey[i + 4];
   }

@@ -289,6 +289,32 @@ static void case_vec3d_full_trunc(Writer &w, int steps) {
       w.rec(std::string(names[i]) + "_z" + std::to_string(kz), plane_field(*wl->f, wl->gv, cs[i], kz));
 }
 
+/* The dispersive workload on a 96^3 grid over its full 3000 steps: the
+   single-precision error of the DFT spectrum, per frequency, is a property
+   of the arithmetic; this case measures it for the reference's own FP32
+   build.  Records: the DFT summary (a hashed sample of every 97th point);
+   with GOLDEN_DFT_DUMP set, every point's spectrum is also written there as
+   raw complex doubles (chunk order, frequency fastest). */
+static void case_disp3d_cube(Writer &w, int steps) {
+  auto wl = make_disp3d(96, 96, 96, 20.0, 0.8, 200, 1);
+  run_steps(*wl, steps);
+  w.scalar("t", wl->f->time());
+  write_dft_summary(w, "dft_Ez", wl->dftf->chunks, Ez, wl->gv, 97);
+  if (const char *path = getenv("GOLDEN_DFT_DUMP")) {
+    FILE *fp = fopen(path, "wb");
+    if (!fp) {
+      fprintf(stderr, "cannot open %s\n", path);
+      exit(2);
+    }
+    for (dft_chunk *ch = wl->dftf->chunks; ch; ch = ch->next_in_dft)
+      for (size_t k = 0; k < ch->N * ch->omega.size(); k++) {
+        const complex<double> v(ch->dft[k]);
+        fwrite(&v, sizeof(v), 1, fp);
+      }
+    fclose(fp);
+  }
+}
+
 static void case_disp3d_full_trunc(Writer &w, int steps) {
   auto wl = make_disp3d(384, 384, 192, 20.0, 0.8, 200, 1);
   run_steps(*wl, steps);
@@ -1405,6 +1431,8 @@ int main(int argc, char **argv) {
     case_vec3d_full_trunc(w, steps > 0 ? steps : 600);
   else if (cs == "disp3d_full_trunc")
     case_disp3d_full_trunc(w, steps > 0 ? steps : 384);
+  else if (cs == "disp3d_cube")
+    case_disp3d_cube(w, steps > 0 ? steps : 3000);
   else if (cs == "disp3d_small")
     case_disp3d(w, 20, 18, 16, 20.0, 0.25, steps > 0 ? steps : 600, 7, true, 1);
   else if (cs == "known")
