@@ -81,7 +81,7 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
                    nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True,
-                   boxed=False):
+                   boxed=False, palette=False):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -93,7 +93,10 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     cases); ecur=False makes every E source integrated (no D current).
     boxed: conductivities and pole strengths are zero outside random boxes
     (separate ones per array), so long grids hold runs of points where a
-    pole or a conductivity is absent next to runs where it is present."""
+    pole or a conductivity is absent next to runs where it is present.
+    palette: permittivities, conductivities and pole strengths take a few
+    values only (eps 1, 4, 12; conductivity 0, 0.3; sigma 0, 0.7, 1.5), as
+    in structures built from a few media."""
     rng = np.random.default_rng(seed)
     nrand = n
     if dim == 2:
@@ -120,9 +123,15 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
         sim.set_bloch([int(d in bloch) for d in range(3)], [bloch.get(d, 0.0) for d in range(3)])
     ext = sim.ext
     shape = tuple(ext)
+    def pal(arr, values):
+        """the palette value nearest to each entry"""
+        v = np.asarray(values)
+        return v[np.abs(np.asarray(arr)[..., None] - v).argmin(axis=-1)]
+
     for c in comps:
         if c // 3 == _lib.E:
-            sim.set_chi1inv(c, c % 3, 1.0 / rng.uniform(1.0, 12.0, size=shape))
+            eps = rng.uniform(1.0, 12.0, size=shape)
+            sim.set_chi1inv(c, c % 3, 1.0 / (pal(eps, [1.0, 4.0, 12.0]) if palette else eps))
     if offdiag:
         for c, dirs in ((_lib.comp(_lib.E, 0), (1, 2)), (_lib.comp(_lib.E, 1), (2,)), (_lib.comp(_lib.E, 2), (1,))):
             if c not in comps:
@@ -143,6 +152,8 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
                 arr = np.where(rng.uniform(size=shape) < 0.3, rng.uniform(0, 0.5, size=shape), 0.0)
                 if boxed:
                     arr = np.where(box_mask(), rng.uniform(0, 0.5, size=shape), 0.0)
+                if palette:
+                    arr = pal(arr, [0.0, 0.3])
                 sim.set_conductivity(c, arr)
     if poles:
         for (w0, g, dr) in ((1e-5, 0.05, True), (0.8, 0.1, False)):
@@ -152,6 +163,8 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
                 arr = rng.uniform(0, 2.0, size=shape) if c in comps else None
                 if boxed and arr is not None:
                     arr = np.where(box_mask(), arr, 0.0)
+                if palette and arr is not None:
+                    arr = pal(arr, [0.0, 0.7, 1.5])
                 sig.append(arr)
             sim.add_lorentzian(w0, g, dr, sig)
     ecomps = [c for c in comps if c // 3 == _lib.E]

@@ -121,3 +121,27 @@ def test_boxed_materials_fp32(engine_lib, oracle_lib):
     o = _run(oracle_lib, 54, 3, 32, **kw)
     for k in o:
         assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
+
+
+@pytest.mark.parametrize("seed,n,boxed,offdiag", [(61, (18, 16, 100), False, False), (62, (17, 16, 97), True, False),
+                                                  (63, (16, 18, 130), True, True), (64, (18, 16, 20), False, False)])
+def test_palette_materials_fp64_bitwise(seed, n, boxed, offdiag, engine_lib, oracle_lib):
+    """Materials from a few values (boxed and layered media as a structure
+    built from objects has them), long z rows: every field bit of the 3-D
+    band kernels equals the oracle's."""
+    kw = dict(palette=True, boxed=boxed, ecur=False, n=n, steps=60, offdiag=offdiag)
+    g = _run(engine_lib, seed, 3, 64, **kw)
+    o = _run(oracle_lib, seed, 3, 64, **kw)
+    for k in o:
+        if k.startswith("c"):
+            assert np.array_equal(g[k], o[k]), k
+        else:
+            assert relerr(g[k], o[k]) <= 1e-13, (k, relerr(g[k], o[k]))
+
+
+def test_palette_materials_fp32(engine_lib, oracle_lib):
+    kw = dict(palette=True, boxed=True, ecur=False, n=(18, 16, 100), steps=60)
+    g = _run(engine_lib, 65, 3, 32, **kw)
+    o = _run(oracle_lib, 65, 3, 32, **kw)
+    for k in o:
+        assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
