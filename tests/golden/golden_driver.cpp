@@ -19,6 +19,7 @@
 
 #include "cases.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -34,6 +35,7 @@ using namespace meep;
 using std::complex;
 
 #ifndef MEEP_GB300
+#include "meep_internals.hpp" // src_vol, for the adjoint case's source points
 // The reference keeps DFT sums in host memory already.
 static void sync_dfts(fields &) {}
 #endif
@@ -1406,6 +1408,272 @@ static void case_py_ldos(Writer &w) {
   w.scalar("t", f.time());
 }
 
+#ifndef MEEP_GB300
+/* ------------------------------------------------------------ adjoint_tm2d
+   The reference's adjoint-solver gradient for a pixel-permittivity design
+   (2-D TM), for comparison with the engine's reverse-time gradient.
+   Reference core only: it calls dft_fields::fourier_sourcedata and
+   fields::add_srcdata (src/dft.cpp:1491-1590, src/sources.cpp:314-338),
+   which the drop-in does not carry.
+
+   Cell 10 x 6 at resolution 10 (100 x 60 pixels), PML 1 on every side, an
+   eps = 12 guide on the Ez rows |y| <= 0.4, a 20 x 20-pixel design block on
+   the Ez points x, y in [-1, 0.9] with eps = eps1 + u (eps2 - eps1), u drawn
+   from mt19937_64(2024); Gaussian Ez current line source (f 0.15, fwidth
+   0.1, not integrated) across the guide at x = -3; J = sum |F|^2 over the
+   Ez DFT (f 0.15, Yee grid) on the line x = 3, |y| <= 1.  Real fields, DFT
+   decimation 1.
+
+   The steps of the reference's Python adjoint layer, restated in C++:
+     forward   FourierFields.register_monitors (python/adjoint/objective.py:
+               358-368) and the design-region Dz DFT on the Yee grid
+               (python/adjoint/utils.py:160-178: Dx, Dy, Dz; TM has Dz only);
+               NFWD steps, so the forward time covers the adjoint profile
+               that _adj_src_scale transforms over [0, T)
+     dJ        autograd's convention for a real function of complex F,
+               dJ/dRe F - i dJ/dIm F = 2 conj(F)
+     adjoint   FourierFields.place_adjoint_source (objective.py:370-416):
+               fourier_sourcedata(dJ) amplitudes times _adj_src_scale
+               (objective.py:65-136; include_resolution False; one frequency:
+               dV * iomega / fwd_dtft / adj_src_phase, times 2 for real
+               fields), time profile GaussianSource(f, 0.1 f, cutoff 5)
+               (objective.py:139-153), on fresh fields (restart_fields), the
+               design-region Dz DFT, NADJ steps (sources end at t = 666.7)
+     gradient  material_grids_addgradient (src/meepgeom.cpp:2835-3011) for a
+               material grid whose nodes are the design block's Ez points,
+               no smoothing and beta = 0, so every Ez point meets one node
+               with weight 1 (add_interpolate_weights, :2710-2756): it adds
+               Re[adj * fwd (chi1inv(u - du) - chi1inv(u + du)) / 2du],
+               du = 1e-3 (utils.py FD_DEFAULT), chi1inv(u) = 1 / (eps1 +
+               u (eps2 - eps1)) (epsilon_material_grid, :569-581)
+   Central differences of J on the reference core at the four pixels with
+   the largest gradient, and along a random direction, pin the restatement. */
+namespace adj2d {
+const int NX = 100, NY = 60;
+const double RES = 10.0;
+const double EPS1 = 1.5, EPS2 = 6.0, EPS_GUIDE = 12.0;
+const int DI0 = 40, DJ0 = 20, DN = 20;
+const double F0 = 0.15;
+const int NFWD = 14000, NADJ = 16000;
+
+class PixelEps : public material_function {
+public:
+  std::vector<double> eps; // Ez points (NX + 1) x (NY + 1), x-major
+  double at(const vec &r) const {
+    long i = lround((r.x() + 0.5 * NX / RES) * RES), j = lround((r.y() + 0.5 * NY / RES) * RES);
+    i = std::min<long>(std::max<long>(i, 0), NX);
+    j = std::min<long>(std::max<long>(j, 0), NY);
+    return eps[i * (NY + 1) + j];
+  }
+  virtual double chi1p1(field_type ft, const vec &r) { return ft == H_stuff ? 1.0 : at(r); }
+  virtual void eff_chi1inv_row(component c, double row[3], const volume &v, double tol, int maxeval) {
+    (void)tol;
+    (void)maxeval;
+    row[0] = row[1] = row[2] = 0.0;
+    row[component_direction(c) % 3] = type(c) == H_stuff ? 1.0 : 1.0 / at(v.center());
+  }
+};
+
+static grid_volume gvol() {
+  grid_volume gv = vol2d(NX / RES, NY / RES, RES);
+  gv.center_origin();
+  return gv;
+}
+static volume source_line() { return volume(vec(-3.0, -0.45), vec(-3.0, 0.45)); }
+static volume obj_vol() { return volume(vec(3.0, -1.0), vec(3.0, 1.0)); }
+static volume design_vol() { return volume(vec(-1.0, -1.0), vec(0.9, 0.9)); }
+
+static void add_forward_source(fields &f) {
+  double width = std::max(0.0, 1 / 0.1);
+  gaussian_src_time src(F0, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, source_line(), complex<double>(1.0, 0.0));
+}
+
+/* (ivec coordinates, value) of every point of a one-frequency DFT */
+static std::map<std::vector<int>, complex<double> > dft_points(dft_chunk *chunks, component c,
+                                                                const grid_volume &gv) {
+  std::map<std::vector<int>, complex<double> > out;
+  std::vector<double> flat = dump_dft_chunks(chunks, c, gv);
+  const size_t rec = 2 + 2;
+  for (size_t k = 0; k + rec <= flat.size(); k += rec)
+    out[{int(flat[k]), int(flat[k + 1])}] = complex<double>(flat[k + 2], flat[k + 3]);
+  return out;
+}
+
+/* J = sum |F|^2 of a forward run with the given permittivity */
+static double forward_J(const std::vector<double> &eps) {
+  grid_volume gv = gvol();
+  PixelEps mat;
+  mat.eps = eps;
+  structure s(gv, mat, pml(1.0), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  add_forward_source(f);
+  component cz = Ez;
+  double fr = F0;
+  dft_fields obj = f.add_dft_fields(&cz, 1, obj_vol(), &fr, 1, false, 1, false);
+  for (int n = 0; n < NFWD; n++)
+    f.step();
+  double J = 0;
+  for (auto &kv : dft_points(obj.chunks, Ez, gv))
+    J += std::norm(kv.second);
+  return J;
+}
+} // namespace adj2d
+
+static void case_adjoint_tm2d(Writer &w) {
+  using namespace adj2d;
+  grid_volume gv = gvol();
+  std::vector<double> eps((NX + 1) * (NY + 1), 1.0);
+  for (int i = 0; i <= NX; i++)
+    for (int j = 26; j <= 34; j++)
+      eps[i * (NY + 1) + j] = EPS_GUIDE;
+  std::mt19937_64 rng(2024);
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  std::vector<double> u(DN * DN);
+  for (int a = 0; a < DN; a++)
+    for (int b = 0; b < DN; b++) {
+      u[a * DN + b] = uni(rng);
+      eps[(DI0 + a) * (NY + 1) + DJ0 + b] = EPS1 + u[a * DN + b] * (EPS2 - EPS1);
+    }
+  w.rec("eps", eps);
+  w.rec("u", u);
+  w.rec("eps12", {EPS1, EPS2});
+  w.rec("design_lo_n", {double(DI0), double(DJ0), double(DN)});
+  w.rec("steps", {double(NFWD), double(NADJ)});
+
+  PixelEps mat;
+  mat.eps = eps;
+  structure s(gv, mat, pml(1.0), identity(), 0, 0.5, false);
+
+  /* forward */
+  fields f(&s);
+  f.use_real_fields();
+  add_forward_source(f);
+  std::vector<double> srcpts; // ivec x, y, Re amp, Im amp
+  for (int ic = 0; ic < f.num_chunks; ic++) {
+    fields_chunk *fc = f.chunks[ic];
+    if (!fc->is_mine()) continue;
+    for (int ft = 0; ft < NUM_FIELD_TYPES; ft++)
+      for (const meep::src_vol &sv : fc->sources[ft])
+        for (size_t j = 0; j < sv.num_points(); j++) {
+          ivec iv = fc->gv.iloc(sv.c, sv.index_at(j));
+          srcpts.push_back(iv.x());
+          srcpts.push_back(iv.y());
+          srcpts.push_back(sv.amplitude_at(j).real());
+          srcpts.push_back(sv.amplitude_at(j).imag());
+        }
+  }
+  w.rec("src_points", srcpts);
+  component cz = Ez, cdz = Dz;
+  double fr = F0;
+  dft_fields obj = f.add_dft_fields(&cz, 1, obj_vol(), &fr, 1, false, 1, false);
+  dft_fields fwd_design = f.add_dft_fields(&cdz, 1, design_vol(), &fr, 1, false, 1, false);
+  for (int n = 0; n < NFWD; n++)
+    f.step();
+  std::map<std::vector<int>, complex<double> > F = dft_points(obj.chunks, Ez, gv);
+  std::vector<double> rec_F;
+  double J = 0;
+  int ymin = 1 << 30;
+  for (auto &kv : F) {
+    rec_F.insert(rec_F.end(), {double(kv.first[0]), double(kv.first[1]), kv.second.real(), kv.second.imag()});
+    J += std::norm(kv.second);
+    ymin = std::min(ymin, kv.first[1]);
+  }
+  w.rec("obj_F", rec_F);
+  w.scalar("J", J);
+
+  /* dJ in the monitor's array order (points along y) */
+  std::vector<complex<double> > dJ(F.size());
+  for (auto &kv : F)
+    dJ[(kv.first[1] - ymin) / 2] = 2.0 * std::conj(kv.second);
+
+  /* _adj_src_scale */
+  const double T = f.time(), dt = f.dt;
+  const double width_adj = std::max(0.0, 1 / (0.1 * F0));
+  gaussian_src_time prof(F0, width_adj, 0.0, 0.0 + 2 * width_adj * 5);
+  prof.is_integrated = false;
+  const complex<double> iomega = (1.0 - std::exp(complex<double>(-0.0, -(2 * pi * F0)) * dt)) * (1.0 / dt);
+  const size_t nt = size_t(std::ceil(T / dt));
+  complex<double> dtft = 0;
+  for (size_t k = 0; k < nt; k++) {
+    const double ph = (((2 * pi) * F0) * double(k)) * dt;
+    dtft += std::polar(1.0, ph) * prof.current(double(k) * dt, dt);
+  }
+  dtft = dtft * dt / std::sqrt(2 * pi);
+  const complex<double> fwidth_scale = std::exp(complex<double>(-0.0, -2 * pi) * 5.0 / 0.1);
+  const complex<double> phase = std::polar(1.0, std::arg(dtft)) * fwidth_scale;
+  const complex<double> scale = 1.0 * iomega / dtft / phase * 2.0;
+  w.rec("adj_scale", {T, dtft.real(), dtft.imag(), scale.real(), scale.imag()});
+
+  /* adjoint */
+  std::vector<sourcedata> sd = obj.fourier_sourcedata(obj_vol(), Ez, f, dJ.data());
+  fields f2(&s);
+  f2.use_real_fields();
+  for (sourcedata &d : sd) {
+    std::vector<complex<double> > amps(d.amp_arr.size());
+    for (size_t k = 0; k < amps.size(); k++)
+      amps[k] = d.amp_arr[k] * scale;
+    f2.add_srcdata(d, &prof, amps.size(), amps.data(), false);
+  }
+  f2.require_source_components();
+  dft_fields adj_design = f2.add_dft_fields(&cdz, 1, design_vol(), &fr, 1, false, 1, false);
+  for (int n = 0; n < NADJ; n++)
+    f2.step();
+
+  /* material_grids_addgradient for the pixel grid */
+  std::map<std::vector<int>, complex<double> > fw = dft_points(fwd_design.chunks, Dz, gv);
+  std::map<std::vector<int>, complex<double> > ad = dft_points(adj_design.chunks, Dz, gv);
+  const double du = 1e-3;
+  std::vector<double> grad(DN * DN, 0.0), rec_design;
+  for (auto &kv : ad) {
+    const int i = (kv.first[0] + NX) / 2, j = (kv.first[1] + NY) / 2;
+    const int a = i - DI0, b = j - DJ0;
+    const complex<double> fv = fw.at(kv.first);
+    rec_design.insert(rec_design.end(), {double(kv.first[0]), double(kv.first[1]), fv.real(), fv.imag(),
+                                         kv.second.real(), kv.second.imag()});
+    if (a < 0 || a >= DN || b < 0 || b >= DN) continue;
+    const double uu = u[a * DN + b];
+    const double row1 = 1.0 / (EPS1 + (uu - du) * (EPS2 - EPS1));
+    const double row2 = 1.0 / (EPS1 + (uu + du) * (EPS2 - EPS1));
+    const complex<double> prod = kv.second * (fv * (row1 - row2) / (2 * du));
+    grad[a * DN + b] += prod.real();
+  }
+  w.rec("design_dft", rec_design);
+  w.rec("grad_u", grad);
+
+  /* central differences of J on the reference core */
+  std::vector<int> order(DN * DN);
+  for (int k = 0; k < DN * DN; k++)
+    order[k] = k;
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return std::fabs(grad[x]) > std::fabs(grad[y]); });
+  const double h = 1e-3;
+  std::vector<double> fd;
+  for (int q = 0; q < 4; q++) {
+    const int k = order[q], a = k / DN, b = k % DN;
+    std::vector<double> ep = eps, em = eps;
+    ep[(DI0 + a) * (NY + 1) + DJ0 + b] = EPS1 + (u[k] + h) * (EPS2 - EPS1);
+    em[(DI0 + a) * (NY + 1) + DJ0 + b] = EPS1 + (u[k] - h) * (EPS2 - EPS1);
+    fd.push_back(k);
+    fd.push_back((forward_J(ep) - forward_J(em)) / (2 * h));
+  }
+  w.rec("fd_pixels", fd);
+  std::vector<double> dp(DN * DN);
+  for (double &x : dp)
+    x = uni(rng) - 0.5;
+  const double hs = 1e-3;
+  std::vector<double> ep = eps, em = eps;
+  for (int k = 0; k < DN * DN; k++) {
+    const int a = k / DN, b = k % DN;
+    ep[(DI0 + a) * (NY + 1) + DJ0 + b] = EPS1 + (u[k] + hs * dp[k]) * (EPS2 - EPS1);
+    em[(DI0 + a) * (NY + 1) + DJ0 + b] = EPS1 + (u[k] - hs * dp[k]) * (EPS2 - EPS1);
+  }
+  w.rec("dp", dp);
+  w.scalar("fd_directional", (forward_J(ep) - forward_J(em)) / (2 * hs));
+}
+#endif
+
 int main(int argc, char **argv) {
   initialize mpi(argc, argv);
   verbosity = 0;
@@ -1471,6 +1739,10 @@ int main(int argc, char **argv) {
     case_py_n2f(w);
   else if (cs == "n2f_periodic2d")
     case_n2f_periodic2d(w, steps > 0 ? steps : 1600);
+#ifndef MEEP_GB300
+  else if (cs == "adjoint_tm2d")
+    case_adjoint_tm2d(w);
+#endif
   else {
     fprintf(stderr, "unknown case %s\n", cs.c_str());
     return 2;

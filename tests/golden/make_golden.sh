@@ -14,6 +14,9 @@ for c in $CASES; do
     OMP_NUM_THREADS=${OMP_NUM_THREADS:-8} "$ROOT/oracle/_ref/fp${p#f}/golden_driver" "$c" "$HERE/$c.$p.bin"
   done
 done
+# The reference's adjoint-solver gradient (FP64 only: forward, adjoint and
+# finite-difference runs of a 2-D design problem; about a minute on 8 threads).
+OMP_NUM_THREADS=${OMP_NUM_THREADS:-8} "$ROOT/oracle/_ref/fp64/golden_driver" adjoint_tm2d "$HERE/adjoint_tm2d.f64.bin"
 # The sphere quadrature table of the reference's subpixel averaging, as the
 # reference's generator prints it (oracle/_ref/gen/sphere-quad.h): rows of
 # "dim index x y z weight".
