@@ -497,6 +497,14 @@ public:
   void set_conductivity(component c, double Cfunc(const vec &));
   void add_susceptibility(material_function &sigma, field_type ft, const susceptibility &sus);
   void add_susceptibility(double sigma(const vec &), field_type ft, const susceptibility &sus);
+  // Extension (the reference reaches material grids through its libctl
+  // geometry, src/meepgeom.cpp:489-581): a material grid over the axis-
+  // aligned block (center, size), weights u (n[0] x n[1] x n[2], row-major),
+  // projection (beta, eta), eps = eps1 + p (eps2 - eps1) per direction.  The
+  // engine evaluates it on the device over the E components' diagonal
+  // chi1inv when the fields are created, after the other materials.
+  void add_material_grid(const double center[3], const double size[3], const int n[3], const double *weights,
+                         double beta, double eta, const double eps1[3], const double eps2[3]);
 
   // host copies handed to the engine when fields are created
   struct impl;

@@ -139,6 +139,12 @@ int mgb_yee_array(mgb_sim *s, int component, int part, double *out, long long *n
  * k (fields::use_bloch(vec)); before the first step.  A nonzero k makes the
  * fields complex. */
 int mgb_use_bloch(mgb_sim *s, const double k[3]);
+/* A material grid over the block (center, size): weights n[0] x n[1] x n[2]
+ * (row-major), projection (beta, eta), eps = eps1 + p (eps2 - eps1) per
+ * direction (structure::add_material_grid); right after mgb_create. */
+int mgb_add_material_grid(mgb_sim *s, const double center[3], const double size[3], const int n[3],
+                          const double *weights, double beta, double eta, const double eps1[3],
+                          const double eps2[3]);
 /* epsilon of the material at n points (no averaging) */
 int mgb_get_epsilon_points(mgb_sim *s, int n, const double *xyz, double *eps);
 

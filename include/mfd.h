@@ -194,6 +194,34 @@ int mfd_forward(mfd_sim *sim, int nsteps, int checkpoint_every);
 int mfd_backward(mfd_sim *sim, int nmon, const int *mon_ids, const double *const *dft_grad,
                  double *grad_chi1inv);
 
+/* Material grid (replaces the MaterialGrid material of a Block: the weights
+ * interpolated by material_grid_val / matgrid_val, src/meepgeom.cpp:489-540,
+ * projected by tanh_projection, :497-502, and mapped to eps by
+ * epsilon_material_grid, :569-581; python/geom.py MaterialGrid).  Every
+ * E-component Yee point x inside the axis-aligned block |x - center| <=
+ * size / 2 (per direction) takes the diagonal chi1inv
+ *   1 / (eps1[d] + p (eps2[d] - eps1[d])),  p = tanh_projection(u(r), beta, eta),
+ * u(r) the linear interpolation of the weights (n[0] x n[1] x n[2], row-major,
+ * nodes at cell centres, mirror faces: linear_interpolate, src/fields.cpp:
+ * 792-806) at r = 0.5 + (x - center) / size (0 along a zero-size direction).
+ * Grids apply in the order added, over the chi1inv arrays, at the first step;
+ * the CUDA engine evaluates them on the device.  Default grid type only (no
+ * overlap rule), no subpixel smoothing of the grid (do_averaging false, the
+ * reference's default), weights in [0, 1], beta >= 0 (may be infinite), eta
+ * in [0, 1].  *id receives the grid's index.
+ *
+ * mfd_material_grid_vjp: dJ/du of grid `id` (n[0]*n[1]*n[2] doubles) from
+ * dJ/dchi1inv of the E components `comps` over the point box lo..hi
+ * (mfd_backward's layout: per component, the box points x slowest), through
+ * the projection and the interpolation (the chain material_grids_addgradient
+ * forms by finite differences, src/meepgeom.cpp:2626-2756); points another,
+ * later grid covers do not count. */
+int mfd_add_material_grid(mfd_sim *sim, const double center[3], const double size[3], const int n[3],
+                          const double *weights, double beta, double eta, const double eps1[3],
+                          const double eps2[3], int *id);
+int mfd_material_grid_vjp(mfd_sim *sim, int id, int ncomp, const int *comps, const int lo[3], const int hi[3],
+                          const double *grad_chi1inv, double *grad_weights);
+
 /* Bloch-periodic boundaries (replaces fields::use_bloch, src/boundaries.cpp:
  * 90-109): directions with periodic[d] != 0 get the Bloch wavevector k[d]
  * (units of 2 pi / a); the other directions keep metallic walls.  A nonzero

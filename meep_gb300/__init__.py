@@ -11,7 +11,7 @@ loading raises if the CUDA library has not been built.
 from ._lib import PRODUCT_LIB, Engine, MeepError, Sim, comp  # noqa: F401
 from .simulation import (  # noqa: F401
     ALL, AUTOMATIC, Block, Bx, By, Bz, ContinuousSource, Cylinder, DrudeSusceptibility, Dx, Dy, Dz, Ex, Ey, Ez,
-    EnergyRegion, Ldos, FluxData, FluxRegion, ForceData, NearToFarData, ForceRegion, GaussianSource, High, Hx, Hy, Hz, LorentzianSusceptibility, Low, Medium, Near2FarRegion, PML,
+    EnergyRegion, Ldos, FluxData, FluxRegion, ForceData, NearToFarData, ForceRegion, GaussianSource, High, Hx, Hy, Hz, LorentzianSusceptibility, Low, MaterialGrid, Medium, Near2FarRegion, PML,
     Simulation, Source, Sphere, Vector3, Volume, X, Y, Z, after_time, air, at_beginning, at_end, at_every,
     dft_ldos, get_electric_energy, get_ldos_freqs, get_energy_freqs, get_flux_freqs, get_fluxes, get_magnetic_energy, get_total_energy, get_force_freqs, get_forces, get_near2far_freqs, inf, scale_flux_fields, scale_near2far_fields,
     stop_when_fields_decayed, vacuum)

@@ -80,6 +80,8 @@ SIGNATURES = [
     ("mfd_design", C.c_int, [_P, C.c_int, _IP, _IP, _IP]),
     ("mfd_forward", C.c_int, [_P, C.c_int, C.c_int]),
     ("mfd_backward", C.c_int, [_P, C.c_int, _IP, C.POINTER(_DP), _DP]),
+    ("mfd_add_material_grid", C.c_int, [_P, _DP, _DP, _IP, _DP, C.c_double, C.c_double, _DP, _DP, _IP]),
+    ("mfd_material_grid_vjp", C.c_int, [_P, C.c_int, C.c_int, _IP, _IP, _IP, _DP, _DP]),
     ("mfd_set_bloch", C.c_int, [_P, C.POINTER(C.c_int), _DP]),
     ("mfd_get_field_im", C.c_int, [_P, C.c_int, _DP]),
     ("mfd_subpixel_rows", C.c_int, [C.c_int, C.c_int, C.c_int64, _DP, _DP, C.c_double, C.c_int, C.c_int,
@@ -338,9 +340,46 @@ class Sim:
         """Declare the design: chi1inv of E components `comps` over the point
         box lo..hi (inclusive)."""
         self.design_comps = list(comps)
+        self.design_lo, self.design_hi = tuple(int(x) for x in lo), tuple(int(x) for x in hi)
         self.design_shape = tuple(int(hi[d]) - int(lo[d]) + 1 for d in range(3))
         ca = (C.c_int * len(comps))(*comps)
         self.eng.check(self.eng.lib.mfd_design(self.h, len(comps), ca, (C.c_int * 3)(*lo), (C.c_int * 3)(*hi)))
+
+    def add_material_grid(self, center, size, weights, eps1, eps2, beta=0.0, eta=0.5):
+        """Material grid over the axis-aligned block (center, size): weights
+        u of shape (n0, n1, n2) (fewer axes are padded with 1), projected with
+        (beta, eta), eps = eps1 + p (eps2 - eps1) per direction (scalars or
+        3-vectors).  Returns the grid's id."""
+        u = np.asarray(weights, dtype=np.float64)
+        u = u.reshape(u.shape + (1,) * (3 - u.ndim))
+        n = (C.c_int * 3)(*u.shape)
+        e1 = np.broadcast_to(np.asarray(eps1, dtype=np.float64), (3,)).copy()
+        e2 = np.broadcast_to(np.asarray(eps2, dtype=np.float64), (3,)).copy()
+        c = np.asarray(center, dtype=np.float64).reshape(3).copy()
+        z = np.asarray(size, dtype=np.float64).reshape(3).copy()
+        uu = np.ascontiguousarray(u.reshape(-1))
+        i = C.c_int()
+        self.eng.check(self.eng.lib.mfd_add_material_grid(self.h, _dptr(c), _dptr(z), n, _dptr(uu), float(beta),
+                                                          float(eta), _dptr(e1), _dptr(e2), C.byref(i)))
+        self.matgrid_shapes = getattr(self, "matgrid_shapes", {})
+        self.matgrid_shapes[i.value] = u.shape
+        return i.value
+
+    def material_grid_vjp(self, grid, grad_chi1inv, comps=None, lo=None, hi=None):
+        """dJ/du of a material grid from dJ/dchi1inv over a point box (by
+        default the design's components and box: backward()'s output)."""
+        comps = list(self.design_comps if comps is None else comps)
+        lo = self.design_lo if lo is None else lo
+        hi = self.design_hi if hi is None else hi
+        g = np.ascontiguousarray(np.asarray(grad_chi1inv, dtype=np.float64).reshape(-1))
+        shapes = getattr(self, "matgrid_shapes", {})
+        if grid not in shapes:
+            raise MeepError("meep: material grid id out of range")
+        out = np.zeros(int(np.prod(shapes[grid])))
+        self.eng.check(self.eng.lib.mfd_material_grid_vjp(self.h, int(grid), len(comps), (C.c_int * len(comps))(*comps),
+                                                          (C.c_int * 3)(*lo), (C.c_int * 3)(*hi), _dptr(g),
+                                                          _dptr(out)))
+        return out.reshape(self.matgrid_shapes[grid])
 
     def forward(self, n, checkpoint_every=0):
         self.eng.check(self.eng.lib.mfd_forward(self.h, int(n), int(checkpoint_every)))

@@ -283,10 +283,18 @@ struct PoleSpec {
   std::vector<double> sigma[3]; // dense per E component direction (empty = absent)
 };
 
+struct MatGridRec {
+  double center[3], size[3], beta, eta, eps1[3], eps2[3];
+  int n[3];
+  std::vector<double> u;
+};
+
 struct structure::impl {
   std::vector<double> chi1inv[3][3]; // [E component direction][row entry direction]
   std::vector<double> cond[2][3];    // [0 = D, 1 = B][direction]
   std::vector<PoleSpec> poles;       // in add order
+  std::vector<MatGridRec> matgrids;  // in add order
+  bool engine_created = false;       // materials were handed to an engine
 };
 
 static volume dV(const grid_volume &gv, const ivec &here, double diameter = 1.0) {
@@ -506,6 +514,26 @@ void structure::add_susceptibility(double sigma(const vec &), field_type ft,
   add_susceptibility(m, ft, sus);
 }
 
+void structure::add_material_grid(const double center[3], const double size[3], const int n[3],
+                                  const double *weights, double beta, double eta, const double eps1[3],
+                                  const double eps2[3]) {
+  if (!center || !size || !n || !weights || !eps1 || !eps2) meep::abort("null material grid argument");
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) meep::abort("material grid sizes must be at least 1");
+  if (d->engine_created) meep::abort("material grids must be added before the fields are stepped or monitored");
+  MatGridRec m;
+  for (int q = 0; q < 3; q++) {
+    m.center[q] = center[q];
+    m.size[q] = size[q];
+    m.n[q] = n[q];
+    m.eps1[q] = eps1[q];
+    m.eps2[q] = eps2[q];
+  }
+  m.beta = beta;
+  m.eta = eta;
+  m.u.assign(weights, weights + (size_t)n[0] * n[1] * n[2]);
+  d->matgrids.push_back(std::move(m));
+}
+
 /* ------------------------------------------------------------- sources */
 gaussian_src_time::gaussian_src_time(double f, double fw, double s) : explicit_window(false) {
   freq = f;
@@ -683,6 +711,9 @@ static void ensure_engine(fields &f) {
       if (!ps.sigma[q].empty() && ((I.components >> (3 * MFD_E + q)) & 1)) sg[q] = ps.sigma[q].data();
     chk(mfd_add_lorentzian(I.sim, MFD_E, ps.omega0, ps.gamma, ps.drude ? 1 : 0, sg));
   }
+  for (const MatGridRec &m : S.matgrids)
+    chk(mfd_add_material_grid(I.sim, m.center, m.size, m.n, m.u.data(), m.beta, m.eta, m.eps1, m.eps2, nullptr));
+  S.engine_created = true;
   std::vector<int> ids;
   for (const auto &st : I.srcs) {
     int id = -1;

@@ -690,6 +690,18 @@ int mgb_get_field_points(mgb_sim *s, int component_, int n, const double *xyz, d
   }
 }
 
+int mgb_add_material_grid(mgb_sim *s, const double center[3], const double size[3], const int n[3],
+                          const double *weights, double beta, double eta, const double eps1[3],
+                          const double eps2[3]) {
+  try {
+    if (!s || !center || !size || !n || !weights || !eps1 || !eps2) throw std::runtime_error("null argument");
+    s->s->add_material_grid(center, size, n, weights, beta, eta, eps1, eps2);
+    return 0;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
 int mgb_use_bloch(mgb_sim *s, const double k[3]) {
   try {
     if (!s || !k) throw std::runtime_error("null argument");

@@ -93,6 +93,12 @@ public:
   }
   virtual void adjoint_step(Plan &p, int64_t s, int64_t slot) { (void)p, (void)s, (void)slot; }
   virtual void adjoint_end(Plan &p, double *grad) { (void)p, (void)grad; }
+  // dJ/du of material grid `id` from dJ/dchi1inv over the design box
+  // (mfd_material_grid_vjp); the oracle evaluates it on the host
+  virtual void matgrid_vjp(Plan &p, int id, const std::vector<int> &comps, const int lo[3], const int hi[3],
+                           const double *gchi, double *gu) {
+    p.matgrid_vjp_host(id, comps, lo, hi, gchi, gu);
+  }
 };
 
 // Defined by whichever backend is linked in.

@@ -22,6 +22,7 @@ struct mfd_sim {
   // differentiation state
   bool design = false;
   int64_t design_points = 0;
+
   int64_t fwd_t0 = -1, fwd_n = 0;
   int fwd_K = 0;
   std::vector<int> snaps;
@@ -255,6 +256,51 @@ int mfd_design(mfd_sim *s, int ncomp, const int *comps, const int lo[3], const i
   s->be->set_design(*s->plan, std::vector<int>(comps, comps + ncomp), lo, hi);
   s->design = true;
   s->design_points = (int64_t)ncomp * (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+  MFD_CATCH
+}
+
+int mfd_add_material_grid(mfd_sim *s, const double center[3], const double size[3], const int n[3],
+                          const double *weights, double beta, double eta, const double eps1[3],
+                          const double eps2[3], int *id) {
+  MFD_TRY
+  need(s && s->plan && center && size && n && weights && eps1 && eps2, "null argument");
+  need(!s->setup_done, "materials must be set before the first step");
+  need(n[0] >= 1 && n[1] >= 1 && n[2] >= 1, "material grid sizes must be at least 1");
+  need(beta >= 0 && eta >= 0 && eta <= 1, "material grid projection needs beta >= 0 and eta in [0, 1]");
+  Plan::MatGrid mg;
+  for (int d = 0; d < 3; d++) {
+    need(size[d] >= 0 && std::isfinite(size[d]) && std::isfinite(center[d]) &&
+             std::fabs(center[d]) + 0.5 * size[d] < 1e6, "invalid material grid block");
+    need(eps1[d] > 0 && eps2[d] > 0, "material grid permittivities must be positive");
+    mg.spec.center[d] = center[d];
+    mg.spec.size[d] = size[d];
+    mg.spec.n[d] = n[d];
+    mg.spec.eps1[d] = eps1[d];
+    mg.spec.eps2[d] = eps2[d];
+  }
+  mg.spec.beta = beta;
+  mg.spec.eta = eta;
+  mg.u.assign(weights, weights + (size_t)n[0] * n[1] * n[2]);
+  for (double w : mg.u)
+    need(w >= 0.0 && w <= 1.0, "The weights parameter of MaterialGrid must be in the range [0,1].");
+  s->plan->matgrids.push_back(std::move(mg));
+  if (id) *id = int(s->plan->matgrids.size()) - 1;
+  MFD_CATCH
+}
+
+int mfd_material_grid_vjp(mfd_sim *s, int id, int ncomp, const int *comps, const int lo[3], const int hi[3],
+                          const double *grad_chi1inv, double *grad_weights) {
+  MFD_TRY
+  need(s && s->plan && comps && lo && hi && grad_chi1inv && grad_weights, "null argument");
+  need(id >= 0 && id < int(s->plan->matgrids.size()), "material grid id out of range");
+  need(ncomp >= 1 && ncomp <= 3, "1 to 3 components");
+  const Plan &p = *s->plan;
+  for (int q = 0; q < ncomp; q++)
+    need(comps[q] >= 0 && comps[q] < 3 && p.have[comps[q]], "components must be allocated E components");
+  for (int d = 0; d < 3; d++)
+    need(lo[d] >= 0 && lo[d] <= hi[d] && hi[d] <= (p.present[d] ? p.N[d] : 0), "box out of range");
+  ensure_setup(s);
+  s->be->matgrid_vjp(*s->plan, id, std::vector<int>(comps, comps + ncomp), lo, hi, grad_chi1inv, grad_weights);
   MFD_CATCH
 }
 

@@ -372,6 +372,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 #include "mfd_dft_tc.cuh"
 #include "mfd_adjoint.cuh"
 #include "mfd_adjoint3.cuh"
+#include "mfd_matgrid.cuh"
 namespace mfd {
 namespace cuda_impl {
 
@@ -982,6 +983,7 @@ public:
           }
     }
     setup_sources(p);
+    apply_matgrids(p);
     build_active_mask(p);
     if (p.any_offdiag)
       for (int d = 0; d < 3; d++) {
@@ -1006,6 +1008,88 @@ public:
     if (p.any_offdiag && p.g.dim != 3) fused_mask = -1;
     if (fused_mask >= 0) plan_boxes(p);
     cuda_check(cudaStreamSynchronize(stream), "setup sync");
+  }
+
+  // ---------------------------------------------------- material grids
+  MGPoints mg_points(const Plan &p, int c, const int lo[3], const int hi[3]) const {
+    MGPoints a;
+    for (int d = 0; d < 3; d++) {
+      a.lo[d] = lo[d];
+      a.n[d] = hi[d] - lo[d] + 1;
+      a.io[d] = p.g.io[d];
+      a.sh[d] = p.shift[c][d];
+      a.present[d] = p.present[d];
+      a.stride[d] = p.stride[d];
+    }
+    a.inva = p.inva;
+    return a;
+  }
+  // the projected weights of every material grid into the diagonal chi1inv
+  // of the E components, grids in order
+  void apply_matgrids(const Plan &p) {
+    for (int id = 0; id < int(p.matgrids.size()); id++) {
+      const Plan::MatGrid &mg = p.matgrids[id];
+      double *du = dupload(mg.u);
+      for (int d = 0; d < 3; d++) {
+        const int c = comp(MFD_E, d);
+        if (!p.have[c]) continue;
+        int lo[3], hi[3];
+        p.matgrid_box(id, c, lo, hi);
+        if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) continue; // block outside the cell
+        const MGPoints a = mg_points(p, c, lo, hi);
+        const long long n = (long long)a.n[0] * a.n[1] * a.n[2];
+        matgrid_chi_kernel<R><<<unsigned((n + 255) / 256), 256, 0, stream>>>(a, mg.spec, du, d, chi[c]);
+        cuda_check(cudaGetLastError(), "matgrid_chi_kernel");
+        nlaunch++;
+      }
+    }
+    cuda_check(cudaStreamSynchronize(stream), "material grids");
+  }
+  void matgrid_vjp(Plan &p, int id, const std::vector<int> &comps, const int lo[3], const int hi[3],
+                   const double *gchi, double *gu) override {
+    const Plan::MatGrid &mg = p.matgrids[id];
+    std::vector<MatGridSpec> specs;
+    for (const Plan::MatGrid &m : p.matgrids)
+      specs.push_back(m.spec);
+    const long long nbox = (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    const long long nu = (long long)mg.spec.n[0] * mg.spec.n[1] * mg.spec.n[2];
+    std::vector<void *> tmp;
+    auto alloc = [&](size_t bytes) {
+      void *ptr = nullptr;
+      cuda_check(cudaMalloc(&ptr, bytes ? bytes : 1), "cudaMalloc");
+      tmp.push_back(ptr);
+      return ptr;
+    };
+    try {
+      MatGridSpec *dspec = (MatGridSpec *)alloc(specs.size() * sizeof(MatGridSpec));
+      double *du = (double *)alloc(nu * sizeof(double));
+      double *dg = (double *)alloc(comps.size() * nbox * sizeof(double));
+      double *drho = (double *)alloc(nbox * sizeof(double));
+      double *dgu = (double *)alloc(nu * sizeof(double));
+      cuda_check(cudaMemcpyAsync(dspec, specs.data(), specs.size() * sizeof(MatGridSpec), cudaMemcpyHostToDevice,
+                                 stream), "upload");
+      cuda_check(cudaMemcpyAsync(du, mg.u.data(), nu * sizeof(double), cudaMemcpyHostToDevice, stream), "upload");
+      cuda_check(cudaMemcpyAsync(dg, gchi, comps.size() * nbox * sizeof(double), cudaMemcpyHostToDevice, stream),
+                 "upload");
+      for (size_t q = 0; q < comps.size(); q++) {
+        const int c = comps[q];
+        const MGPoints a = mg_points(p, c, lo, hi);
+        matgrid_grho_kernel<<<unsigned((nbox + 255) / 256), 256, 0, stream>>>(
+            a, dspec, int(specs.size()), id, du, c % 3, dg + q * nbox, drho);
+        cuda_check(cudaGetLastError(), "matgrid_grho_kernel");
+        matgrid_gather_kernel<<<unsigned((nu + 127) / 128), 128, 0, stream>>>(a, mg.spec, drho, dgu, q > 0);
+        cuda_check(cudaGetLastError(), "matgrid_gather_kernel");
+        nlaunch += 2;
+      }
+      cuda_check(cudaMemcpyAsync(gu, dgu, nu * sizeof(double), cudaMemcpyDeviceToHost, stream), "download");
+      cuda_check(cudaStreamSynchronize(stream), "material grid gradient");
+    } catch (...) {
+      for (void *ptr : tmp)
+        cudaFree(ptr);
+      throw;
+    }
+    for (void *ptr : tmp)
+      cudaFree(ptr);
   }
 
   // activity bits per row segment of 32 z points (FusedArgs::amask) for

@@ -6,6 +6,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 
 namespace mfd {
 
@@ -368,3 +369,91 @@ void Plan::set_bloch(const int per[3], const double k[3]) {
 
 } // namespace mfd
 
+
+namespace mfd {
+
+/* ------------------------------------------------------- material grids */
+void Plan::matgrid_box(int id, int c, int lo[3], int hi[3]) const {
+  const MatGridSpec &s = matgrids[id].spec;
+  for (int d = 0; d < 3; d++) {
+    if (!present[d]) {
+      lo[d] = hi[d] = 0;
+      continue;
+    }
+    const double a2 = 2.0 * g.a;
+    const double k0 = ((s.center[d] - 0.5 * s.size[d]) * a2 - g.io[d] - shift[c][d]) / 2;
+    const double k1 = ((s.center[d] + 0.5 * s.size[d]) * a2 - g.io[d] - shift[c][d]) / 2;
+    lo[d] = std::max(0, int(std::floor(k0)) - 1);
+    hi[d] = std::min(N[d], int(std::ceil(k1)) + 1);
+  }
+}
+
+int Plan::matgrid_at(int c, const int k[3]) const {
+  double x[3];
+  point_coords(c, k, x);
+  for (int id = int(matgrids.size()) - 1; id >= 0; id--)
+    if (mg_inside(matgrids[id].spec, x)) return id;
+  return -1;
+}
+
+void Plan::apply_matgrids_host() {
+  for (int id = 0; id < int(matgrids.size()); id++) {
+    const MatGrid &mg = matgrids[id];
+    for (int d = 0; d < 3; d++) {
+      const int c = comp(MFD_E, d);
+      if (!have[c]) continue;
+      std::vector<double> &chi = chi1inv[c][d];
+      if (chi.empty()) chi.assign(ndense, 1.0);
+      int lo[3], hi[3], k[3];
+      matgrid_box(id, c, lo, hi);
+      for (k[0] = lo[0]; k[0] <= hi[0]; k[0]++)
+        for (k[1] = lo[1]; k[1] <= hi[1]; k[1]++)
+          for (k[2] = lo[2]; k[2] <= hi[2]; k[2]++) {
+            double x[3], r[3];
+            point_coords(c, k, x);
+            if (!mg_inside(mg.spec, x)) continue;
+            mg_coords(mg.spec, x, r);
+            const double up = mg_project(mg_interp(mg.u.data(), mg.spec.n, r), mg.spec.beta, mg.spec.eta);
+            chi[(int64_t(k[0]) * ext[1] + k[1]) * ext[2] + k[2]] = 1.0 / mg_eps(mg.spec, d, up);
+          }
+    }
+  }
+}
+
+void Plan::matgrid_vjp_host(int id, const std::vector<int> &comps, const int lo[3], const int hi[3],
+                            const double *gchi, double *gu) const {
+  const MatGrid &mg = matgrids[id];
+  const MatGridSpec &s = mg.spec;
+  const int64_t nu = int64_t(s.n[0]) * s.n[1] * s.n[2];
+  std::fill(gu, gu + nu, 0.0);
+  int64_t q = 0;
+  for (int c : comps) {
+    const int d = c % 3;
+    int k[3];
+    for (k[0] = lo[0]; k[0] <= hi[0]; k[0]++)
+      for (k[1] = lo[1]; k[1] <= hi[1]; k[1]++)
+        for (k[2] = lo[2]; k[2] <= hi[2]; k[2]++, q++) {
+          if (gchi[q] == 0.0 || matgrid_at(c, k) != id) continue;
+          double x[3], r[3];
+          point_coords(c, k, x);
+          mg_coords(s, x, r);
+          const double rho = mg_interp(mg.u.data(), s.n, r);
+          const double eps = mg_eps(s, d, mg_project(rho, s.beta, s.eta));
+          const double grho = gchi[q] * (-(s.eps2[d] - s.eps1[d]) / (eps * eps)) *
+                              mg_project_deriv(rho, s.beta, s.eta);
+          int i1[3], i2[3];
+          double w[3];
+          for (int e = 0; e < 3; e++)
+            mg_map(r[e], s.n[e], i1[e], i2[e], w[e]);
+          for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+              for (int cc = 0; cc < 2; cc++) {
+                const int x0 = a ? i2[0] : i1[0], y0 = b ? i2[1] : i1[1], z0 = cc ? i2[2] : i1[2];
+                const double wt = (a ? w[0] : 1.0 - w[0]) * (b ? w[1] : 1.0 - w[1]) * (cc ? w[2] : 1.0 - w[2]);
+                gu[(int64_t(x0) * s.n[1] + y0) * s.n[2] + z0] += grho * wt;
+              }
+        }
+  }
+}
+
+} // namespace mfd

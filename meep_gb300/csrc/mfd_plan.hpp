@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "mfd.h"
+#include "matgrid.hpp"
 
 namespace mfd {
 
@@ -181,6 +182,33 @@ public:
     double w[8] = {};
   };
   ProbePoints center_probe(int d) const;
+
+  // Material grids (mfd_add_material_grid): at setup every E-component Yee
+  // point inside a grid's block takes the diagonal chi1inv 1 / eps of the
+  // projected, interpolated weights (matgrid.hpp), grids applied in the
+  // order added (a later one wins where blocks overlap, as the last object
+  // of a geometry does).  The CUDA engine evaluates them on the device; the
+  // CPU oracle through apply_matgrids_host.
+  struct MatGrid {
+    MatGridSpec spec;
+    std::vector<double> u; // n0 * n1 * n2, row-major
+  };
+  std::vector<MatGrid> matgrids;
+  // physical coordinates of point k of component c: (io + shift + 2k) / (2a)
+  void point_coords(int c, const int k[3], double x[3]) const {
+    for (int d = 0; d < 3; d++)
+      x[d] = present[d] ? double(g.io[d] + shift[c][d] + 2 * k[d]) * (0.5 * inva) : 0.0;
+  }
+  // index box of component c that holds every point of grid id's block
+  // (the kernels test each point exactly)
+  void matgrid_box(int id, int c, int lo[3], int hi[3]) const;
+  // the grid id that sets point k of E component c (-1: none)
+  int matgrid_at(int c, const int k[3]) const;
+  void apply_matgrids_host();
+  // dJ/du of grid id from dJ/dchi1inv over a design box (mfd_backward's
+  // layout: per design component, the box points x-major)
+  void matgrid_vjp_host(int id, const std::vector<int> &comps, const int lo[3], const int hi[3],
+                        const double *gchi, double *gu) const;
   int64_t dense_count() const { return ndense; }
   int64_t store_index_of_dense(int64_t di) const;
   void dense_coords(int64_t di, int k[3]) const;

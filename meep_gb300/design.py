@@ -96,6 +96,50 @@ class DesignProblem2D:
         sim.close()
         return -gchi / (eps_design * eps_design)  # chi1inv = 1/eps
 
+    def grid_block(self):
+        """(center, size) of the block that a material grid over the design
+        takes: the design's Ez points with half a pixel around them, so a
+        grid of design-sized nodes puts one node on every point."""
+        h = 0.5 / self.res
+        x0 = [(-n + 2 * l) * h for n, l in ((self.nx, self.lo[0]), (self.ny, self.lo[1]))]
+        x1 = [(-n + 2 * l) * h for n, l in ((self.nx, self.hi[0]), (self.ny, self.hi[1]))]
+        return ((0.5 * (x0[0] + x1[0]), 0.5 * (x0[1] + x1[1]), 0.0),
+                (x1[0] - x0[0] + 2 * h, x1[1] - x0[1] + 2 * h, 0.0))
+
+    def run_grid(self, weights, grid, grad=False, checkpoint_every=55, precision=None):
+        """Forward run with the design block's permittivity from a material
+        grid: weights u of shape grid['n'], eps = eps1 + p (eps2 - eps1) with
+        p the (beta, eta) projection of u interpolated to each Ez point,
+        evaluated by the engine (mfd_add_material_grid).  Returns (F, handle)
+        as run() does."""
+        prec = precision or self.precision
+        sim, mid = self._sim(np.full(self.design, float(grid["eps1"])), prec)
+        center, size = self.grid_block()
+        gid = sim.add_material_grid(center, size, np.asarray(weights, dtype=np.float64).reshape(grid["n"]),
+                                    grid["eps1"], grid["eps2"], beta=grid.get("beta", 0.0),
+                                    eta=grid.get("eta", 0.5))
+        if grad:
+            sim.design([self.ez], self.lo, self.hi)
+            sim.forward(self.steps, checkpoint_every)
+        else:
+            sim.step(self.steps)
+        F = sim.get_dft(mid)
+        if not grad:
+            sim.close()
+            return F, None
+        return F, (sim, mid, gid, tuple(grid["n"]))
+
+    @staticmethod
+    def backward_grid(handle, dJdF):
+        """dJ/du of the material grid's weights for dJdF (run_grid handle):
+        the reverse-time dJ/dchi1inv through the projection and the
+        interpolation (mfd_material_grid_vjp)."""
+        sim, mid, gid, n = handle
+        gchi = sim.backward({mid: dJdF})
+        gu = sim.material_grid_vjp(gid, gchi)
+        sim.close()
+        return gu.reshape(n)
+
     @staticmethod
     def objective(F):
         """sum over frequencies of the mean over the line of |F|^2, and dJ/dF."""

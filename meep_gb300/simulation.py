@@ -38,6 +38,7 @@ import ctypes as C
 import math
 import numbers
 import os
+import warnings
 
 import numpy as np
 
@@ -187,10 +188,66 @@ class Medium:
 vacuum = air = Medium(epsilon=1.0)
 
 
+class MaterialGrid:
+    """Material on a rectilinear grid of design weights u in [0, 1] over a
+    Block (python/geom.py MaterialGrid): u is interpolated linearly to each
+    point (nodes at cell centres, mirror faces), optionally projected by
+    (tanh(beta eta) + tanh(beta (u - eta))) / (tanh(beta eta) + tanh(beta (1 -
+    eta))), and eps = eps1 + u (eps2 - eps1) with eps1, eps2 the diagonal
+    permittivities of medium1 and medium2 (src/meepgeom.cpp:489-581).  The
+    engine evaluates it on the device.  Covered: the default grid type, no
+    subpixel smoothing of the grid (do_averaging=False, the reference's
+    default), no damping, media without susceptibilities or conductivity; a
+    grid is the material of a Block.  With eps_averaging=True the pixels
+    straddling the block's faces are averaged against medium1 (the reference
+    evaluates the grid there)."""
+
+    def __init__(self, grid_size, medium1, medium2, weights=None, grid_type="U_DEFAULT", do_averaging=False,
+                 beta=0, eta=0.5, damping=0):
+        gs = _v3(grid_size)
+        self.grid_size = Vector3(*(1 if math.isclose(v, 0, abs_tol=1e-9) else int(round(v)) for v in gs))
+        self.medium1, self.medium2 = medium1, medium2
+        self.num_params = int(self.grid_size.x * self.grid_size.y * self.grid_size.z)
+        self.do_averaging, self.beta, self.eta, self.damping = do_averaging, float(beta), float(eta), damping
+        unsupported = []
+        if grid_type != "U_DEFAULT":
+            unsupported.append("material grid type %s" % grid_type)
+        if do_averaging:
+            unsupported.append("subpixel smoothing of material grids")
+        if damping:
+            unsupported.append("material grid damping")
+        for m in (medium1, medium2):
+            if m.E_susceptibilities or any(m.D_conductivity_diag):
+                unsupported.append("dispersive or conductive material grid media")
+                break
+        if unsupported:
+            raise NotImplementedError("meep: %s not supported by the GB300 engine" % ", ".join(unsupported))
+        if weights is None:
+            self.weights = np.zeros(self.num_params)
+        elif np.asarray(weights).size != self.num_params:
+            raise ValueError("weights of shape {} do not match user specified grid dimension: {}".format(
+                np.asarray(weights).shape, self.grid_size))
+        else:
+            self.weights = self.check_weights(np.asarray(weights, dtype=np.float64).flatten())
+
+    def check_weights(self, w):
+        if np.amin(w) >= 0.0 and np.amax(w) <= 1.0:
+            return w
+        warnings.warn("The weights parameter of MaterialGrid must be in the range [0,1].")
+        return np.clip(w, 0.0, 1.0)
+
+    def update_weights(self, x):
+        x = np.asarray(x, dtype=np.float64)
+        if x.size != self.num_params:
+            raise ValueError("weights of size {} do not match user specified grid dimension: {}".format(
+                x.size, self.grid_size))
+        self.weights[:] = self.check_weights(x).flatten()
+
+
 # -------------------------------------------------------------- geometry
 class GeometricObject:
     def __init__(self, material=Medium(), center=Vector3(), epsilon_func=None, label=None):
-        if callable(material) and not isinstance(material, Medium):
+        if callable(material) and not isinstance(material, (Medium, MaterialGrid)):
             raise NotImplementedError("meep: material functions are not supported by the GB300 engine")
         self.material = material
         self.center = _v3(center)
@@ -437,6 +494,7 @@ _SIGS = [
     ("mgb_get_epsilon_points", C.c_int, [_P, C.c_int, _DP, _DP]),
     ("mgb_yee_array", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_longlong)]),
     ("mgb_use_bloch", C.c_int, [_P, _DP]),
+    ("mgb_add_material_grid", C.c_int, [_P, _DP, _DP, C.POINTER(C.c_int), _DP, C.c_double, C.c_double, _DP, _DP]),
     ("mgb_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.POINTER(C.c_size_t)]),
     ("mgb_load_flux_data", C.c_int, [_P, C.c_int, C.c_int, _DP, C.c_size_t]),
     ("mgb_flux_scale", C.c_int, [_P, C.c_int, C.c_double, C.c_double]),
@@ -612,12 +670,22 @@ class Simulation:
     def init_sim(self):
         if self._h is not None:
             return
+        if isinstance(self.default_material, MaterialGrid):
+            raise NotImplementedError("meep: a material grid as the default material is not supported by the "
+                                      "GB300 engine; put it in a Block")
         media = [self.default_material]
         index = {id(self.default_material): 0}
+        grids = []
         for g in self.geometry:
-            if id(g.material) not in index:
-                index[id(g.material)] = len(media)
-                media.append(g.material)
+            mat = g.material
+            if isinstance(mat, MaterialGrid):
+                if not isinstance(g, Block):
+                    raise NotImplementedError("meep: a material grid must be the material of a Block")
+                grids.append(g)
+                mat = mat.medium1  # the block's faces average against medium1
+            if id(mat) not in index:
+                index[id(mat)] = len(media)
+                media.append(mat)
         sus_keys = []
         for m in media:
             for s in m.E_susceptibilities:
@@ -637,7 +705,7 @@ class Simulation:
         for q, g in enumerate(self.geometry):
             o = objs[q]
             o.center[:] = list(g.center)
-            o.material = index[id(g.material)]
+            o.material = index[id(g.material.medium1 if isinstance(g.material, MaterialGrid) else g.material)]
             if isinstance(g, Block):
                 o.kind = 0
                 o.size[:] = list(g.size)
@@ -664,6 +732,15 @@ class Simulation:
                                          int(self.eps_averaging), self.subpixel_tol, self.subpixel_maxeval,
                                          C.byref(h)))
         self._h = h
+        for g in grids:
+            m = g.material
+            n = (C.c_int * 3)(*(int(v) for v in m.grid_size))
+            c_a, c_p = _arr(list(g.center))
+            z_a, z_p = _arr(list(g.size))
+            w_a, w_p = _arr(m.weights)
+            e1_a, e1_p = _arr(list(m.medium1.epsilon_diag))
+            e2_a, e2_p = _arr(list(m.medium2.epsilon_diag))
+            self._check(self._lib.mgb_add_material_grid(self._h, c_p, z_p, n, w_p, m.beta, m.eta, e1_p, e2_p))
         if self.k_point is not False:
             # Bloch-periodic walls in every direction (Simulation._init_fields);
             # complex fields when k != 0

@@ -142,6 +142,7 @@ public:
   }
 
   void setup(Plan &p) override {
+    p.apply_matgrids_host();
     p.plan_offdiag();
     for (int c = 0; c < NC; c++) {
       if (!p.have[c]) continue;

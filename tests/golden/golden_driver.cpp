@@ -1364,6 +1364,103 @@ static void case_py_energy(Writer &w) {
                                             center=mp.Vector3(0.1, 0.05))])
      sim.run(mp.dft_ldos(1.0, 0.2, 5), until_after_sources=20)
      sim.ldos_data, sim.ldos_Fdata, sim.ldos_Jdata */
+/* Script (the weights u: mt19937_64(77) uniform [0, 1), 15 x 11, written to
+   the fixture as "weights"):
+     mg = mp.MaterialGrid(mp.Vector3(15, 11), mp.Medium(epsilon=1.5), mp.Medium(epsilon=9),
+                          weights=u, beta=6, eta=0.45)
+     geometry = [mp.Cylinder(0.6, center=mp.Vector3(-2, 1.5), material=mp.Medium(epsilon=4)),
+                 mp.Block(center=mp.Vector3(0.3, -0.2), size=mp.Vector3(3.1, 2.3), material=mg)]
+     sim = mp.Simulation(cell_size=mp.Vector3(10, 8), resolution=10, geometry=geometry,
+                         boundary_layers=[mp.PML(1.0)], eps_averaging=False,
+                         sources=[mp.Source(mp.GaussianSource(0.2, fwidth=0.2), component=mp.Ez,
+                                            center=mp.Vector3(-3, 0))])
+     flux = sim.add_flux(0.2, 0.2, 5, mp.FluxRegion(center=mp.Vector3(3), size=mp.Vector3(0, 4)))
+     sim.run(until=60)
+   The grid material as the reference's geometry evaluates it without
+   smoothing: the weights linearly interpolated at the point's block
+   coordinates (linear_interpolate with mirror faces, src/fields.cpp:759-806),
+   projected (tanh_projection, src/meepgeom.cpp:497-502), eps1 + u (eps2 -
+   eps1) (epsilon_material_grid, :569-581). */
+class PyMatGridGeom : public material_function {
+public:
+  double bc[3] = {0.3, -0.2, 0.0}, bs[3] = {3.1, 2.3, 0.0};
+  int n[3] = {15, 11, 1};
+  std::vector<double> u;
+  double beta = 6, eta = 0.45, e1 = 1.5, e2 = 9.0;
+  static int mirror(int i, int m) { return i >= m ? 2 * m - 1 - i : (i < 0 ? -1 - i : i); }
+  double interp(const double r0[3]) const {
+    int i1[3], i2[3];
+    double w[3];
+    for (int d = 0; d < 3; d++) {
+      double r = r0[d] < 0.0 ? -r0[d] : (r0[d] > 1.0 ? 1.0 - r0[d] : r0[d]);
+      i1[d] = mirror(int(r * n[d]), n[d]);
+      double dd = r * n[d] - i1[d] - 0.5;
+      i2[d] = mirror(dd >= 0.0 ? i1[d] + 1 : i1[d] - 1, n[d]);
+      w[d] = std::fabs(dd);
+    }
+    auto U = [&](int x, int y, int z) { return u[(x * n[1] + y) * n[2] + z]; };
+    return (((U(i1[0], i1[1], i1[2]) * (1.0 - w[0]) + U(i2[0], i1[1], i1[2]) * w[0]) * (1.0 - w[1]) +
+             (U(i1[0], i2[1], i1[2]) * (1.0 - w[0]) + U(i2[0], i2[1], i1[2]) * w[0]) * w[1]) *
+                (1.0 - w[2]) +
+            ((U(i1[0], i1[1], i2[2]) * (1.0 - w[0]) + U(i2[0], i1[1], i2[2]) * w[0]) * (1.0 - w[1]) +
+             (U(i1[0], i2[1], i2[2]) * (1.0 - w[0]) + U(i2[0], i2[1], i2[2]) * w[0]) * w[1]) *
+                w[2]);
+  }
+  double eps_at(const vec &v) const {
+    const double p[3] = {v.x(), v.y(), 0.0};
+    bool in = true;
+    for (int d = 0; d < 3; d++)
+      in = in && std::fabs(p[d] - bc[d]) <= 0.5 * bs[d];
+    if (in) {
+      double r[3];
+      for (int d = 0; d < 3; d++)
+        r[d] = bs[d] == 0 ? 0.0 : 0.5 + (p[d] - bc[d]) / bs[d];
+      double x = interp(r);
+      if (beta != 0) {
+        const double t = std::tanh(beta * eta);
+        x = x == eta ? 0.5 : (t + std::tanh(beta * (x - eta))) / (t + std::tanh(beta * (1 - eta)));
+      }
+      return e1 + x * (e2 - e1);
+    }
+    const double dx = p[0] + 2, dy = p[1] - 1.5;
+    return dx * dx + dy * dy <= 0.6 * 0.6 ? 4.0 : 1.0;
+  }
+  virtual double chi1p1(field_type ft, const vec &r) { return ft == H_stuff ? 1.0 : eps_at(r); }
+  virtual void eff_chi1inv_row(component c, double row[3], const volume &v, double, int) {
+    row[0] = row[1] = row[2] = 0.0;
+    row[component_direction(c) % 3] = type(c) == H_stuff ? 1.0 : 1.0 / eps_at(v.center());
+  }
+};
+
+static void case_py_matgrid(Writer &w) {
+  grid_volume gv = vol2d(10, 8, 10);
+  gv.center_origin();
+  PyMatGridGeom g;
+  std::mt19937_64 rng(77);
+  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  g.u.resize(15 * 11);
+  for (double &x : g.u)
+    x = uni(rng);
+  w.rec("weights", g.u);
+  structure s(gv, g, pml(1.0), identity(), 0, 0.5, false);
+  fields f(&s);
+  f.use_real_fields();
+  double width = std::max(0.0, 1 / 0.2);
+  gaussian_src_time src(0.2, width, 0.0, 0.0 + 2 * width * 5.0);
+  src.is_integrated = false;
+  f.add_volume_source(Ez, src, volume(vec(-3, 0), vec(-3, 0)), complex<double>(1.0, 0.0));
+  std::vector<double> fr = np_linspace(0.2 - 0.5 * 0.2, 0.2 + 0.5 * 0.2, 5);
+  volume_list r1(volume(vec(3, -2), vec(3, 2)), Sx, 1.0);
+  dft_flux fl = f.add_dft_flux(&r1, fr.data(), fr.size(), true, true, 0);
+  py_run_until(f, 60);
+  sync_dfts(f);
+  double *F = fl.flux();
+  w.rec("flux", std::vector<double>(F, F + fr.size()));
+  delete[] F;
+  w.scalar("t", f.time());
+  w.rec("Ez", global_field(f, gv, Ez));
+}
+
 static void case_py_ldos(Writer &w) {
   const double inf = 1.0e20;
   grid_volume gv = vol2d(6, 6, 20);
@@ -1731,6 +1828,8 @@ int main(int argc, char **argv) {
     case_n2f(w, D3, Ez, Hx, steps > 0 ? steps : 900);
   else if (cs == "py_ldos")
     case_py_ldos(w);
+  else if (cs == "py_matgrid")
+    case_py_matgrid(w);
   else if (cs == "py_energy")
     case_py_energy(w);
   else if (cs == "py_force")

@@ -207,3 +207,69 @@ def test_precision_from_environment(monkeypatch):
     monkeypatch.setenv("MEEP_GB300_PRECISION", "16")
     with pytest.raises(ValueError):
         sm._product_lib()
+
+
+# --- material grids ----------------------------------------------------------
+
+def script_matgrid(lib, beta=6):
+    """golden_driver case py_matgrid: a projected MaterialGrid block beside a
+    cylinder (the weights come from the fixture)."""
+    u = np.asarray(golden("py_matgrid")["weights"]).reshape(15, 11)
+    mg = mp.MaterialGrid(mp.Vector3(15, 11), mp.Medium(epsilon=1.5), mp.Medium(epsilon=9), weights=u, beta=beta,
+                         eta=0.45)
+    geometry = [mp.Cylinder(0.6, center=mp.Vector3(-2, 1.5), material=mp.Medium(epsilon=4)),
+                mp.Block(center=mp.Vector3(0.3, -0.2), size=mp.Vector3(3.1, 2.3), material=mg)]
+    sim = mp.Simulation(cell_size=mp.Vector3(10, 8), resolution=10, geometry=geometry,
+                        boundary_layers=[mp.PML(1.0)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(0.2, fwidth=0.2), component=mp.Ez,
+                                           center=mp.Vector3(-3, 0))], _library=lib)
+    flux = sim.add_flux(0.2, 0.2, 5, mp.FluxRegion(center=mp.Vector3(3), size=mp.Vector3(0, 4)))
+    sim.run(until=60)
+    return {"flux": mp.get_fluxes(flux), "t": sim.meep_time(), "Ez": sim.get_yee_array(mp.Ez).reshape(-1),
+            "weights": u.reshape(-1)}
+
+
+def test_script_matgrid_on_oracle(oracle_meep_lib):
+    """MaterialGrid through the front end, evaluated by the CPU oracle: within
+    1e-12 of the reference core running the restated grid material (the
+    projection's tanh and the points' coordinates may round differently)."""
+    _compare(script_matgrid(oracle_meep_lib), golden("py_matgrid"), 1e-12)
+
+
+def test_matgrid_unsupported_options_raise(oracle_meep_lib):
+    m1, m2 = mp.Medium(epsilon=1), mp.Medium(epsilon=4)
+    with pytest.raises(NotImplementedError, match="smoothing"):
+        mp.MaterialGrid(mp.Vector3(3, 3), m1, m2, do_averaging=True)
+    with pytest.raises(NotImplementedError, match="U_MEAN"):
+        mp.MaterialGrid(mp.Vector3(3, 3), m1, m2, grid_type="U_MEAN")
+    with pytest.raises(NotImplementedError, match="dispersive"):
+        mp.MaterialGrid(mp.Vector3(3, 3), m1, mp.Medium(epsilon=2, D_conductivity=0.1))
+    with pytest.raises(ValueError):
+        mp.MaterialGrid(mp.Vector3(3, 3), m1, m2, weights=np.zeros(4))
+    with pytest.warns(UserWarning, match="range"):
+        g = mp.MaterialGrid(mp.Vector3(2, 2), m1, m2, weights=np.array([-0.5, 0.2, 0.7, 1.5]))
+    assert list(g.weights) == [0.0, 0.2, 0.7, 1.0]
+    sim = mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, default_material=g, _library=oracle_meep_lib,
+                        sources=[mp.Source(mp.GaussianSource(0.2, fwidth=0.2), component=mp.Ez,
+                                           center=mp.Vector3())])
+    with pytest.raises(NotImplementedError, match="default material"):
+        sim.init_sim()
+    sim = mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, _library=oracle_meep_lib,
+                        geometry=[mp.Sphere(0.5, material=g)],
+                        sources=[mp.Source(mp.GaussianSource(0.2, fwidth=0.2), component=mp.Ez,
+                                           center=mp.Vector3())])
+    with pytest.raises(NotImplementedError, match="Block"):
+        sim.init_sim()
+
+
+@pytest.mark.gpu
+def test_script_matgrid_on_gpu(engine_lib):
+    """The same on the CUDA engine (grid evaluated on the device): FP64
+    within 1e-12 of the reference core, FP32 within 3x the reference's own
+    FP32 error (or 1e-5)."""
+    _compare(script_matgrid(PRODUCT_LIB), golden("py_matgrid"), 1e-12)
+    out = script_matgrid(SINGLE_LIB)
+    ref64, ref32 = golden("py_matgrid"), golden("py_matgrid", "f32")
+    for k in ("Ez", "flux"):
+        bound = max(3 * relerr(ref32[k], ref64[k]), 1e-5)
+        assert relerr(np.reshape(out[k], -1), ref64[k]) <= bound, k
