@@ -159,9 +159,8 @@ __global__ void __launch_bounds__(256) adj_de_kernel(Geo g, Tables<R> tb, AdjCur
 
 // Reverse of the B half step for one B component (H part, then the B curl).
 template <typename R>
-__global__ void __launch_bounds__(256) adj_bh_kernel(Geo g, Tables<R> tb, AdjCurlArgs<R> a) {
-  int k[3];
-  if (!box_point(g, a.box, k)) return;
+__device__ __forceinline__ void adj_bh_point(const Geo &g, const Tables<R> &tb, const AdjCurlArgs<R> &a,
+                                             const int k[3]) {
   const long long i = lin(g, k);
   // curl adjoints of the D half step that read H (inside the H slab) or B
   const R gsum = gather_at(g, a.gat, k, i);
@@ -178,6 +177,29 @@ __global__ void __launch_bounds__(256) adj_bh_kernel(Geo g, Tables<R> tb, AdjCur
   else
     lam += gsum;
   adj_curl_core(g, tb, a, k, i, lam);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) adj_bh_kernel(Geo g, Tables<R> tb, AdjCurlArgs<R> a) {
+  int k[3];
+  if (!box_point(g, a.box, k)) return;
+  adj_bh_point(g, tb, a, k);
+}
+
+// Two B components of a grid whose slow direction is one point thick (2-D):
+// blockIdx.z picks the component.  The reversed B updates of different
+// components touch disjoint arrays, so one launch does both.
+template <typename R>
+__global__ void __launch_bounds__(256) adj_bh2_kernel(Geo g, Tables<R> tb, AdjCurlArgs<R> a0, AdjCurlArgs<R> a1) {
+  const AdjCurlArgs<R> &a = blockIdx.z ? a1 : a0;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= a.box.n[g.fast] || m >= a.box.n[g.mid] || a.box.n[g.slow] < 1) return;
+  int k[3];
+  k[g.fast] = a.box.lo[g.fast] + x;
+  k[g.mid] = a.box.lo[g.mid] + m;
+  k[g.slow] = a.box.lo[g.slow];
+  adj_bh_point(g, tb, a, k);
 }
 
 template <typename R> __global__ void __launch_bounds__(256) adj_gather_kernel(Geo g, GatherArgs<R> a) {
@@ -212,7 +234,9 @@ template <typename R> struct InjectArgs {
   int lo[3], n[3];
   int ad0, ad1;
   const double2 *G;  // [npts][nf]
-  const double2 *ph; // [nf] phases of this sample
+  const double2 *ph; // [nf] phases of this sample, or null: formed per block
+  const double *freq; // with ph null: scale * exp(2 pi i f time) per block
+  double time, sre, sim;
   int nf;
   long long npts;
 };
@@ -225,11 +249,23 @@ template <typename R> __device__ __forceinline__ void inj_add(const Geo &g, cons
 }
 
 template <typename R> __global__ void adj_inject_kernel(Geo g, InjectArgs<R> a) {
+  extern __shared__ double2 sph[];
+  const double2 *phase = a.ph;
+  if (!phase) {
+    // the sample's phases, as dft_phase_kernel forms them
+    for (int w = threadIdx.x; w < a.nf; w += blockDim.x) {
+      double s, c;
+      sincos(2 * kPi * a.freq[w] * a.time, &s, &c);
+      sph[w] = make_double2(c * a.sre - s * a.sim, c * a.sim + s * a.sre);
+    }
+    __syncthreads();
+    phase = sph;
+  }
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= a.npts) return;
   double s = 0;
   for (int w = 0; w < a.nf; w++) {
-    const double2 G = a.G[p * a.nf + w], ph = a.ph[w];
+    const double2 G = a.G[p * a.nf + w], ph = phase[w];
     s += G.x * ph.x + G.y * ph.y;
   }
   if (s == 0) return;

@@ -2302,8 +2302,13 @@ public:
       const int nf = (int)m.freq.size();
       double timeE = tn * p.dt;
       double time = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? timeE - 0.5 * p.dt : timeE;
-      dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(), m.scale.imag(),
-                                                              dm.ph);
+      // phases formed in the inject kernel's shared memory when they fit
+      const bool inline_ph = size_t(nf) * sizeof(double2) <= 32768;
+      if (!inline_ph) {
+        dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(),
+                                                                m.scale.imag(), dm.ph);
+        nlaunch++;
+      }
       InjectArgs<R> ia{};
       ia.lam = lam_f[m.c];
       ia.lamb = nullptr;
@@ -2330,11 +2335,16 @@ public:
             else ia.ad0 = d;
           }
       ia.G = adj_G[id];
-      ia.ph = dm.ph;
+      ia.ph = inline_ph ? nullptr : dm.ph;
+      ia.freq = dm.freq;
+      ia.time = time;
+      ia.sre = m.scale.real();
+      ia.sim = m.scale.imag();
       ia.nf = nf;
       ia.npts = (long long)m.npts;
-      adj_inject_kernel<R><<<(unsigned)((ia.npts + 255) / 256), 256, 0, stream>>>(geo, ia);
-      nlaunch += 2;
+      adj_inject_kernel<R><<<(unsigned)((ia.npts + 255) / 256), 256, inline_ph ? size_t(nf) * sizeof(double2) : 0,
+                             stream>>>(geo, ia);
+      nlaunch++;
     }
     // 2-3. the 3-D band kernels when the forward runs them
     if (p.g.dim == 3 && fused_mask == MASK3) {
@@ -2368,6 +2378,7 @@ public:
       nlaunch++;
     }
     // 3. reverse B half step (H through f_w inside the slab, then the curl)
+    std::vector<AdjCurlArgs<R>> bargs;
     for (int d = 0; d < 3; d++) {
       int c = comp(MFD_B, d);
       if (!p.have[c] || p.curl[c].g1 < 0) continue;
@@ -2377,11 +2388,29 @@ public:
       a.lfw = lam_fw[hc];
       a.isB = 1;
       a.gat = gather_args(p, hc, MFD_D);
+      bargs.push_back(a);
+    }
+    if (bargs.size() == 2 && bargs[0].box.n[geo.slow] == 1 && bargs[1].box.n[geo.slow] == 1) {
+      // both B components in one launch (2-D)
+      // one block shape for both, from the wider box; the grid covers both
+      const int wide = bargs[0].box.n[geo.fast] >= bargs[1].box.n[geo.fast] ? 0 : 1;
       dim3 grid, block;
-      launch_dims(a.box, grid, block);
-      adj_bh_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+      launch_dims(bargs[wide].box, grid, block);
+      for (const AdjCurlArgs<R> &a : bargs) {
+        grid.x = std::max(grid.x, unsigned((a.box.n[geo.fast] + block.x - 1) / block.x));
+        grid.y = std::max(grid.y, unsigned((a.box.n[geo.mid] + block.y - 1) / block.y));
+      }
+      grid.z = 2;
+      adj_bh2_kernel<R><<<grid, block, 0, stream>>>(geo, tb, bargs[0], bargs[1]);
       nlaunch++;
     }
+    else
+      for (const AdjCurlArgs<R> &a : bargs) {
+        dim3 grid, block;
+        launch_dims(a.box, grid, block);
+        adj_bh_kernel<R><<<grid, block, 0, stream>>>(geo, tb, a);
+        nlaunch++;
+      }
   }
 
   // reversed step on the 3-D bands: D/E (E part and D curl of all three

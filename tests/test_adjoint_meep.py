@@ -123,9 +123,10 @@ def test_gradient_matches_reference_adjoint_fp64(engine_lib):
     within 1e-10 of the reference's; dJ/du within 1e-5 (relative, infinity
     norm over the 400 pixels) of the reference's adjoint-solver gradient and of
     its finite differences at four pixels; the directional derivative along dp
-    within 1e-5 of both.  1e-5 is 200x tighter than the reference test's
-    0.002 and 4x above the level at which the reference's own gradient meets
-    its finite differences."""
+    within 1e-5 of both.  The reference's gradient is a frequency-domain
+    estimate: it meets its own finite differences within 2.5e-6 at the
+    largest pixels, and the engine's exact gradient within 7.3e-6 over all
+    pixels (measured); 1e-5 is 200x tighter than the reference test's 0.002."""
     rec = _fixture()
     eng = _lib.Engine(engine_lib)
     F, g = _engine_gradient(eng, rec, 64)
@@ -143,9 +144,9 @@ def test_gradient_matches_reference_adjoint_fp64(engine_lib):
 @pytest.mark.gpu
 def test_gradient_matches_reference_adjoint_fp32(engine_lib):
     """FP32 engine (fields, adjoint fields and their products in single
-    precision, DFT sums in double): dJ/du within 1e-3 of the reference's FP64
-    adjoint-solver gradient, the directional derivative within 1e-3 (the
-    reference test allows 0.075 for its FP32 build,
+    precision, DFT sums in double): dJ/du within 5e-5 of the reference's FP64
+    adjoint-solver gradient (measured 7.8e-6), the directional derivative
+    within 5e-5 (the reference test allows 0.075 for its FP32 build,
     python/tests/test_adjoint_solver.py:550)."""
     rec = _fixture()
     eng = _lib.Engine(engine_lib)
@@ -153,6 +154,6 @@ def test_gradient_matches_reference_adjoint_fp32(engine_lib):
     assert relerr(F, _reference_F(rec)) <= 1e-4
     gm = np.asarray(rec["grad_u"])
     print("FP32 engine vs reference adjoint gradient: %.3g" % relerr(g, gm))
-    assert relerr(g, gm) <= 1e-3, relerr(g, gm)
+    assert relerr(g, gm) <= 5e-5, relerr(g, gm)
     dp = np.asarray(rec["dp"])
-    assert abs(dp @ g / (dp @ gm) - 1) <= 1e-3
+    assert abs(dp @ g / (dp @ gm) - 1) <= 5e-5
