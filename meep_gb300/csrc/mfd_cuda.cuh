@@ -1280,6 +1280,51 @@ public:
     nlaunch++;
   }
 
+  // the shell bands of a half-step as one launch (ShellSet)
+  ShellSet shell_set() const {
+    ShellSet s{};
+    const Band *bands[5] = {&band_xface_zi, &band_yface_zi, &band_xzedge, &band_yzedge, &band_xyedge};
+    int total = 0;
+    for (int q = 0; q < 5; q++) {
+      const Band &b = *bands[q];
+      s.b[q] = b;
+      const bool empty = b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0;
+      s.gz[q] = empty ? 1 : (b.s[2].n + 31) / 32;
+      s.gy[q] = empty ? 1 : (b.s[1].n + 7) / 8;
+      s.first[q] = total;
+      if (!empty) total += s.gz[q] * s.gy[q] * b.s[0].n;
+    }
+    s.first[5] = total;
+    return s;
+  }
+  void launch_b_shell(const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
+    const ShellSet s = shell_set();
+    if (s.first[5] == 0) return;
+    const dim3 g(s.first[5]), blk(32, 8);
+    if (cnd && zp) b3_shell_kernel<R, true, true><<<g, blk, 0, st>>>(a, s);
+    else if (cnd) b3_shell_kernel<R, true, false><<<g, blk, 0, st>>>(a, s);
+    else if (zp) b3_shell_kernel<R, false, true><<<g, blk, 0, st>>>(a, s);
+    else b3_shell_kernel<R, false, false><<<g, blk, 0, st>>>(a, s);
+    nlaunch++;
+  }
+  template <int NP> void launch_de_shell_p(const ShellSet &s, const FusedArgs<R> &a, bool cnd, bool zp,
+                                           cudaStream_t st) {
+    const dim3 g(s.first[5]), blk(32, 8);
+    if (cnd && zp) de3_shell_kernel<R, true, NP, true><<<g, blk, 0, st>>>(a, s);
+    else if (cnd) de3_shell_kernel<R, true, NP, false><<<g, blk, 0, st>>>(a, s);
+    else if (zp) de3_shell_kernel<R, false, NP, true><<<g, blk, 0, st>>>(a, s);
+    else de3_shell_kernel<R, false, NP, false><<<g, blk, 0, st>>>(a, s);
+  }
+  void launch_de_shell(const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
+    const ShellSet s = shell_set();
+    if (s.first[5] == 0) return;
+    if (a.npoles == 1) launch_de_shell_p<1>(s, a, cnd, zp, st);
+    else if (a.npoles == 2) launch_de_shell_p<2>(s, a, cnd, zp, st);
+    else if (a.npoles > 2) launch_de_shell_p<-1>(s, a, cnd, zp, st);
+    else launch_de_shell_p<0>(s, a, cnd, zp, st);
+    nlaunch++;
+  }
+
   // the two passes of the off-diagonal D/E half-step (3-D)
   template <bool FX, bool FY, bool ZCAN = true>
   void launch_d_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp_, cudaStream_t st) {
@@ -1588,13 +1633,9 @@ public:
       }
       else
         launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
-      // x and y slab faces: their z interior (no z flags; whole warps in
-      // FP32) and their z ends as separate launches
-      launch_b_band<true, false, false>(band_xface_zi, a, cndB, zp, side[0]);
-      launch_b_band<false, true, false>(band_yface_zi, a, cndB, zp, side[1]);
-      launch_b_band<true, false>(band_xzedge, a, cndB, zp, side[4]);
-      launch_b_band<false, true>(band_yzedge, a, cndB, zp, side[5]);
-      launch_b_band<true, true>(band_xyedge, a, cndB, zp, side[3]);
+      // the shell: x and y slab faces over their z interior (no z flags;
+      // whole warps in FP32) and their z ends, and the x-y edges, one launch
+      launch_b_shell(a, cndB, zp, side[0]);
       join();
     }
     else {
@@ -1647,11 +1688,7 @@ public:
       }
       else
         launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
-      launch_de_band<true, false, false>(band_xface_zi, a, cndD, zp, side[0]);
-      launch_de_band<false, true, false>(band_yface_zi, a, cndD, zp, side[1]);
-      launch_de_band<true, false>(band_xzedge, a, cndD, zp, side[4]);
-      launch_de_band<false, true>(band_yzedge, a, cndD, zp, side[5]);
-      launch_de_band<true, true>(band_xyedge, a, cndD, zp, side[3]);
+      launch_de_shell(a, cndD, zp, side[0]);
       join();
     }
     else {

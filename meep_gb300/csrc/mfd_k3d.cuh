@@ -688,5 +688,69 @@ __global__ void __launch_bounds__(256, NP > 0 ? 4 : ((FX || FY) ? (sizeof(R) == 
   if (band_coords(bd, k)) de3_point<R, CND, NP, FX, FY, FZ>(a, k);
 }
 
+// The shell of a 3-D half-step in one launch: the z-interior x and y faces,
+// their z edges and the x-y edges.  Each band keeps its own compile-time PML
+// directions; a block of 32 x 8 threads works on one band (blocks numbered
+// band after band, in each band z blocks fastest, then y, then x), so the
+// shell has one launch and one tail instead of five.
+struct ShellSet {
+  Band b[5];    // x face z interior, y face z interior, x face z edges, y face z edges, x-y edges
+  int gz[5];    // blocks along z (32 points each) of each band
+  int gy[5];    // blocks along y (8 rows each)
+  int first[6]; // first block of each band; first[5] is the total
+};
+
+// point of this thread in band q of the shell; false past the band's end
+__device__ __forceinline__ bool shell_coords(const ShellSet &s, int &q, int k[3]) {
+  const int blk = blockIdx.x;
+  q = 0;
+#pragma unroll
+  for (int r = 1; r < 5; r++)
+    q += blk >= s.first[r] ? 1 : 0;
+  Band bd;
+  int gz, gy, f0;
+  switch (q) { // constant indices: the parameters stay in the constant bank
+    case 0: bd = s.b[0], gz = s.gz[0], gy = s.gy[0], f0 = s.first[0]; break;
+    case 1: bd = s.b[1], gz = s.gz[1], gy = s.gy[1], f0 = s.first[1]; break;
+    case 2: bd = s.b[2], gz = s.gz[2], gy = s.gy[2], f0 = s.first[2]; break;
+    case 3: bd = s.b[3], gz = s.gz[3], gy = s.gy[3], f0 = s.first[3]; break;
+    default: bd = s.b[4], gz = s.gz[4], gy = s.gy[4], f0 = s.first[4]; break;
+  }
+  const int lb = blk - f0;
+  const int t[3] = {lb / (gz * gy), (lb / gz) % gy * 8 + (int)threadIdx.y, lb % gz * 32 + (int)threadIdx.x};
+  if (t[1] >= bd.s[1].n || t[2] >= bd.s[2].n) return false;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    k[d] = t[d] + (t[d] < bd.s[d].split ? bd.s[d].a0 : bd.s[d].a1);
+  return true;
+}
+
+template <typename R, bool CND, bool ZP>
+__global__ void __launch_bounds__(256, sizeof(R) == 8 ? 4 : 6) b3_shell_kernel(const FusedArgs<R> a, const ShellSet s) {
+  int q, k[3];
+  if (!shell_coords(s, q, k)) return;
+  switch (q) {
+    case 0: b3_point<R, CND, true, false, false>(a, k); break;
+    case 1: b3_point<R, CND, false, true, false>(a, k); break;
+    case 2: b3_point<R, CND, true, false, ZP>(a, k); break;
+    case 3: b3_point<R, CND, false, true, ZP>(a, k); break;
+    default: b3_point<R, CND, true, true, ZP>(a, k); break;
+  }
+}
+
+template <typename R, bool CND, int NP, bool ZP>
+__global__ void __launch_bounds__(256, NP > 0 ? 4 : (sizeof(R) == 8 ? 4 : 6))
+    de3_shell_kernel(const FusedArgs<R> a, const ShellSet s) {
+  int q, k[3];
+  if (!shell_coords(s, q, k)) return;
+  switch (q) {
+    case 0: de3_point<R, CND, NP, true, false, false>(a, k); break;
+    case 1: de3_point<R, CND, NP, false, true, false>(a, k); break;
+    case 2: de3_point<R, CND, NP, true, false, ZP>(a, k); break;
+    case 3: de3_point<R, CND, NP, false, true, ZP>(a, k); break;
+    default: de3_point<R, CND, NP, true, true, ZP>(a, k); break;
+  }
+}
+
 } // namespace cuda_impl
 } // namespace mfd
