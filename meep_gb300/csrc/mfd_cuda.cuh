@@ -369,6 +369,7 @@ __global__ void src_post_kernel(Geo g, EArgs<R> a, const SrcPoint *pts, int n, c
 #include "mfd_fused.cuh"
 #include "mfd_k3d.cuh"
 #include "mfd_q3d.cuh"
+#include "mfd_q3f.cuh"
 #include "mfd_dft_tc.cuh"
 #include "mfd_adjoint.cuh"
 #include "mfd_adjoint3.cuh"
@@ -1124,7 +1125,20 @@ public:
     }
     d_amask = dupload(m);
     amask_nseg = nseg;
+    // z extent of the segments where some pole is active anywhere: rows
+    // outside it take the pole-free D/E kernel
+    const unsigned pole_bits = (1u << (3 * MAX_POLES)) - 1u;
+    int s0 = nseg, s1 = -1;
+    for (size_t c = 0; c < m.size(); c++)
+      if (m[c] & pole_bits) {
+        const int sg = (int)(c % nseg);
+        s0 = std::min(s0, sg);
+        s1 = std::max(s1, sg);
+      }
+    pole_z0 = s1 >= s0 ? 32 * s0 : 0;
+    pole_z1 = s1 >= s0 ? std::min(32 * (s1 + 1), p.ext[2]) : 0;
   }
+  int pole_z0 = 0, pole_z1 = -1; // z points [pole_z0, pole_z1) hold every active pole (-1: unknown)
 
   static constexpr int MASK3 = 0xFFF;
   static constexpr int MASK_TM = (1 << 2) | (1 << 3) | (1 << 4) | (1 << 8) | (1 << 9) | (1 << 10);
@@ -1207,6 +1221,10 @@ public:
   // FP64 (issue-bound) shell: faces over the z interior only (no z flags) and
   // the z edges of the faces
   Band band_xface_zi{}, band_yface_zi{}, band_xzedge{}, band_yzedge{};
+  // FP32: the z-interior faces of the B half-step as quads (QFaces) when
+  // their z run is whole quads; the B shell launch then leaves them out
+  QFaces qfaces{};
+  bool use_qfaces = false;
   // the rows without their z slabs and walls (z range of the quad core): no
   // PML flag in any direction; band_zend holds the rest of the rows
   Band band_core{};
@@ -1281,14 +1299,15 @@ public:
   }
 
   // the shell bands of a half-step as one launch (ShellSet)
-  ShellSet shell_set() const {
+  // skip_zi: the z-interior faces run elsewhere (FP32 B half-step: quads)
+  ShellSet shell_set(bool skip_zi) const {
     ShellSet s{};
     const Band *bands[5] = {&band_xface_zi, &band_yface_zi, &band_xzedge, &band_yzedge, &band_xyedge};
     int total = 0;
     for (int q = 0; q < 5; q++) {
       const Band &b = *bands[q];
       s.b[q] = b;
-      const bool empty = b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0;
+      const bool empty = b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0 || (skip_zi && q < 2);
       s.gz[q] = empty ? 1 : (b.s[2].n + 31) / 32;
       s.gy[q] = empty ? 1 : (b.s[1].n + 7) / 8;
       s.first[q] = total;
@@ -1298,7 +1317,7 @@ public:
     return s;
   }
   void launch_b_shell(const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
-    const ShellSet s = shell_set();
+    const ShellSet s = shell_set(use_qfaces);
     if (s.first[5] == 0) return;
     const dim3 g(s.first[5]), blk(32, 8);
     if (cnd && zp) b3_shell_kernel<R, true, true><<<g, blk, 0, st>>>(a, s);
@@ -1315,8 +1334,8 @@ public:
     else if (zp) de3_shell_kernel<R, false, NP, true><<<g, blk, 0, st>>>(a, s);
     else de3_shell_kernel<R, false, NP, false><<<g, blk, 0, st>>>(a, s);
   }
-  void launch_de_shell(const FusedArgs<R> &a, bool cnd, bool zp, cudaStream_t st) {
-    const ShellSet s = shell_set();
+  void launch_de_shell(const FusedArgs<R> &a, bool cnd, bool zp, bool skip_zi, cudaStream_t st) {
+    const ShellSet s = shell_set(skip_zi);
     if (s.first[5] == 0) return;
     if (a.npoles == 1) launch_de_shell_p<1>(s, a, cnd, zp, st);
     else if (a.npoles == 2) launch_de_shell_p<2>(s, a, cnd, zp, st);
@@ -1325,6 +1344,28 @@ public:
     nlaunch++;
   }
 
+  // FP32 D/E faces as quads when there are no poles (the shell then leaves
+  // them out); true if launched
+  bool launch_de_qfaces(const FusedArgs<R> &a, bool cnd, cudaStream_t st) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (!use_qfaces || a.npoles != 0) return false;
+      const dim3 g(qfaces.nblk[0] + qfaces.nblk[1]);
+      if (cnd) de3q_faces_kernel<true><<<g, 256, 0, st>>>(a, qfaces);
+      else de3q_faces_kernel<false><<<g, 256, 0, st>>>(a, qfaces);
+      nlaunch++;
+      return true;
+    }
+    return false;
+  }
+  void launch_b_qfaces(const FusedArgs<R> &a, bool cnd, cudaStream_t st) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (!use_qfaces) return;
+      const dim3 g(qfaces.nblk[0] + qfaces.nblk[1]);
+      if (cnd) b3q_faces_kernel<true><<<g, 256, 0, st>>>(a, qfaces);
+      else b3q_faces_kernel<false><<<g, 256, 0, st>>>(a, qfaces);
+      nlaunch++;
+    }
+  }
   // the two passes of the off-diagonal D/E half-step (3-D)
   template <bool FX, bool FY, bool ZCAN = true>
   void launch_d_band(const Band &bd, const FusedArgs<R> &a, bool cnd, bool zp_, cudaStream_t st) {
@@ -1482,6 +1523,21 @@ public:
       band_yface_zi = Band{{sxr, syo, szr}};
       band_xzedge = Band{{sxo, syr, szo}};
       band_yzedge = Band{{sxr, syo, szo}};
+      use_qfaces = false;
+      if (std::is_same<R, float>::value && szr.n > 0 && szr.a0 % 4 == 0 && szr.n % 4 == 0 && p.stride[2] == 1 &&
+          p.stride[1] % 4 == 0 && p.stride[0] % 4 == 0) {
+        qfaces = QFaces{};
+        const Band *fb[2] = {&band_xface_zi, &band_yface_zi};
+        for (int f = 0; f < 2; f++) {
+          qfaces.b[f] = *fb[f];
+          qfaces.nq[f] = szr.n / 4;
+          qfaces.nquads[f] = fb[f]->s[0].n > 0 && fb[f]->s[1].n > 0
+                                 ? (long long)fb[f]->s[0].n * fb[f]->s[1].n * qfaces.nq[f]
+                                 : 0;
+          qfaces.nblk[f] = (int)((qfaces.nquads[f] + 255) / 256);
+        }
+        use_qfaces = qfaces.nblk[0] + qfaces.nblk[1] > 0;
+      }
       // the B core: z interior (no slab, off the low wall) rounded inwards to quads
       qcore = QCore{};
       qcore.lo[0] = xlo;
@@ -1634,7 +1690,9 @@ public:
       else
         launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
       // the shell: x and y slab faces over their z interior (no z flags;
-      // whole warps in FP32) and their z ends, and the x-y edges, one launch
+      // FP32: quads, a launch of their own) and their z ends, and the x-y
+      // edges, one launch; the z ends of the rows beside them
+      launch_b_qfaces(a, cndB, side[1]);
       launch_b_shell(a, cndB, zp, side[0]);
       join();
     }
@@ -1686,9 +1744,29 @@ public:
         launch_de_band<false, false, false>(band_core, a, cndD, zp, stream);
         launch_de_band<false, false>(band_zend, a, cndD, zp, side[2]);
       }
+      else if (a.npoles > 0 && pole_z1 >= 0 && (pole_z0 > 0 || std::min(pole_z1, p.N[2]) < p.N[2])) {
+        // rows (z points 0..N-1) split along z at the pole region: the kernel
+        // with poles in registers where some pole is active, the pole-free one
+        // elsewhere (P stays 0 there; its registers would only cost occupancy)
+        const int z1 = std::min(pole_z1, p.N[2]);
+        if (z1 > pole_z0) {
+          Band bp = band_rows;
+          bp.s[2] = span_run(pole_z0, z1 - 1);
+          launch_de_band<false, false>(bp, a, cndD, zp, stream);
+        }
+        Band bn = band_rows;
+        bn.s[2] = z1 > pole_z0 ? span_outside(p.N[2], pole_z0, z1 - 1) : span_run(0, p.N[2] - 1);
+        dim3 g, blk;
+        band_shape(bn, g, blk);
+        if (g.x) {
+          launch_de_band_p<false, false, 0>(bn, g, blk, a, cndD, zp, side[2]);
+          nlaunch++;
+        }
+      }
       else
         launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
-      launch_de_shell(a, cndD, zp, side[0]);
+      const bool qde = launch_de_qfaces(a, cndD, side[1]);
+      launch_de_shell(a, cndD, zp, qde, side[0]);
       join();
     }
     else {
