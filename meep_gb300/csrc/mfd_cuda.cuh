@@ -1299,13 +1299,15 @@ public:
   }
 
   // the shell bands of a half-step as one launch (ShellSet)
-  // skip_zi: the z-interior faces run elsewhere (FP32 B half-step: quads)
-  ShellSet shell_set(bool skip_zi) const {
+  // skip_zi: the z-interior faces run elsewhere (FP32: quads); zi: their z
+  // span when only part of it stays in the shell (null: all of it)
+  ShellSet shell_set(bool skip_zi, const Span *zi = nullptr) const {
     ShellSet s{};
     const Band *bands[5] = {&band_xface_zi, &band_yface_zi, &band_xzedge, &band_yzedge, &band_xyedge};
     int total = 0;
     for (int q = 0; q < 5; q++) {
-      const Band &b = *bands[q];
+      Band b = *bands[q];
+      if (zi && q < 2) b.s[2] = *zi;
       s.b[q] = b;
       const bool empty = b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0 || (skip_zi && q < 2);
       s.gz[q] = empty ? 1 : (b.s[2].n + 31) / 32;
@@ -1334,8 +1336,9 @@ public:
     else if (zp) de3_shell_kernel<R, false, NP, true><<<g, blk, 0, st>>>(a, s);
     else de3_shell_kernel<R, false, NP, false><<<g, blk, 0, st>>>(a, s);
   }
-  void launch_de_shell(const FusedArgs<R> &a, bool cnd, bool zp, bool skip_zi, cudaStream_t st) {
-    const ShellSet s = shell_set(skip_zi);
+  void launch_de_shell(const FusedArgs<R> &a, bool cnd, bool zp, bool skip_zi, cudaStream_t st,
+                       const Span *zi = nullptr) {
+    const ShellSet s = shell_set(skip_zi, zi);
     if (s.first[5] == 0) return;
     if (a.npoles == 1) launch_de_shell_p<1>(s, a, cnd, zp, st);
     else if (a.npoles == 2) launch_de_shell_p<2>(s, a, cnd, zp, st);
@@ -1344,14 +1347,25 @@ public:
     nlaunch++;
   }
 
-  // FP32 D/E faces as quads when there are no poles (the shell then leaves
-  // them out); true if launched
-  bool launch_de_qfaces(const FusedArgs<R> &a, bool cnd, cudaStream_t st) {
+  // FP32 D/E faces as quads where no pole is active (over the z run zq of
+  // the z interior, or all of it; the shell takes the rest); true if launched
+  bool launch_de_qfaces(const FusedArgs<R> &a, bool cnd, cudaStream_t st, const Span *zq = nullptr) {
     if constexpr (std::is_same<R, float>::value) {
-      if (!use_qfaces || a.npoles != 0) return false;
-      const dim3 g(qfaces.nblk[0] + qfaces.nblk[1]);
-      if (cnd) de3q_faces_kernel<true><<<g, 256, 0, st>>>(a, qfaces);
-      else de3q_faces_kernel<false><<<g, 256, 0, st>>>(a, qfaces);
+      if (!use_qfaces || (a.npoles != 0 && !zq)) return false;
+      QFaces f = qfaces;
+      if (zq) {
+        for (int q = 0; q < 2; q++) {
+          f.b[q].s[2] = *zq;
+          f.nq[q] = zq->n / 4;
+          f.nquads[q] = f.b[q].s[0].n > 0 && f.b[q].s[1].n > 0 ? (long long)f.b[q].s[0].n * f.b[q].s[1].n * f.nq[q]
+                                                              : 0;
+          f.nblk[q] = (int)((f.nquads[q] + 255) / 256);
+        }
+        if (f.nblk[0] + f.nblk[1] == 0) return false;
+      }
+      const dim3 g(f.nblk[0] + f.nblk[1]);
+      if (cnd) de3q_faces_kernel<true><<<g, 256, 0, st>>>(a, f);
+      else de3q_faces_kernel<false><<<g, 256, 0, st>>>(a, f);
       nlaunch++;
       return true;
     }
@@ -1765,8 +1779,40 @@ public:
       }
       else
         launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
-      const bool qde = launch_de_qfaces(a, cndD, side[1]);
-      launch_de_shell(a, cndD, zp, qde, side[0]);
+      // D/E faces: with poles confined to one end of the z interior, its
+      // pole-free part as quads and the rest in the shell
+      bool split = false;
+      if (F32 && use_qfaces && a.npoles > 0 && a.npoles <= 2 && pole_z1 >= 0) {
+        const Span zi = band_xface_zi.s[2];
+        const int zlo = zi.a0, zhi = zi.a0 + zi.n; // [zlo, zhi)
+        const int p0 = std::max(zlo, pole_z0), p1 = std::min(zhi, pole_z1);
+        Span zq{}, zs{};
+        if (p1 <= p0) { // no pole in the z interior
+          zq = zi;
+          zs = span_run(0, -1);
+          split = true;
+        }
+        else if (p0 == zlo && p1 < zhi) {
+          zs = span_run(zlo, p1 - 1);
+          zq = span_run(p1, zhi - 1);
+          split = true;
+        }
+        else if (p1 == zhi && p0 > zlo) {
+          zs = span_run(p0, zhi - 1);
+          zq = span_run(zlo, p0 - 1);
+          split = true;
+        }
+        if (split && zq.n % 4 == 0 && zq.a0 % 4 == 0) {
+          launch_de_qfaces(a, cndD, side[1], &zq);
+          launch_de_shell(a, cndD, zp, false, side[0], &zs);
+        }
+        else
+          split = false;
+      }
+      if (!split) {
+        const bool qde = launch_de_qfaces(a, cndD, side[1]);
+        launch_de_shell(a, cndD, zp, qde, side[0]);
+      }
       join();
     }
     else {
