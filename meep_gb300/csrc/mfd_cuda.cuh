@@ -1225,6 +1225,7 @@ public:
   // their z run is whole quads; the B shell launch then leaves them out
   QFaces qfaces{};
   bool use_qfaces = false;
+
   // the rows without their z slabs and walls (z range of the quad core): no
   // PML flag in any direction; band_zend holds the rest of the rows
   Band band_core{};
@@ -1370,6 +1371,22 @@ public:
       return true;
     }
     return false;
+  }
+  // FP64 (issue-bound): the shell bands as separate launches on the side
+  // streams (one launch per half-step ran 2.5% slower there)
+  void launch_b_shell_bands(const FusedArgs<R> &a, bool cnd, bool zp) {
+    launch_b_band<true, false, false>(band_xface_zi, a, cnd, zp, side[0]);
+    launch_b_band<false, true, false>(band_yface_zi, a, cnd, zp, side[1]);
+    launch_b_band<true, false>(band_xzedge, a, cnd, zp, side[4]);
+    launch_b_band<false, true>(band_yzedge, a, cnd, zp, side[5]);
+    launch_b_band<true, true>(band_xyedge, a, cnd, zp, side[3]);
+  }
+  void launch_de_shell_bands(const FusedArgs<R> &a, bool cnd, bool zp) {
+    launch_de_band<true, false, false>(band_xface_zi, a, cnd, zp, side[0]);
+    launch_de_band<false, true, false>(band_yface_zi, a, cnd, zp, side[1]);
+    launch_de_band<true, false>(band_xzedge, a, cnd, zp, side[4]);
+    launch_de_band<false, true>(band_yzedge, a, cnd, zp, side[5]);
+    launch_de_band<true, true>(band_xyedge, a, cnd, zp, side[3]);
   }
   void launch_b_qfaces(const FusedArgs<R> &a, bool cnd, cudaStream_t st) {
     if constexpr (std::is_same<R, float>::value) {
@@ -1706,8 +1723,12 @@ public:
       // the shell: x and y slab faces over their z interior (no z flags;
       // FP32: quads, a launch of their own) and their z ends, and the x-y
       // edges, one launch; the z ends of the rows beside them
-      launch_b_qfaces(a, cndB, side[1]);
-      launch_b_shell(a, cndB, zp, side[0]);
+      if (F32) {
+        launch_b_qfaces(a, cndB, side[1]);
+        launch_b_shell(a, cndB, zp, side[0]);
+      }
+      else
+        launch_b_shell_bands(a, cndB, zp);
       join();
     }
     else {
@@ -1809,10 +1830,12 @@ public:
         else
           split = false;
       }
-      if (!split) {
+      if (!split && F32) {
         const bool qde = launch_de_qfaces(a, cndD, side[1]);
         launch_de_shell(a, cndD, zp, qde, side[0]);
       }
+      else if (!split)
+        launch_de_shell_bands(a, cndD, zp);
       join();
     }
     else {

@@ -10,7 +10,8 @@
 // poles: with two poles the quad kernel needs 190 registers and ran slower
 // than the one-point bands, which then stay in the shell launch.  (A D/E
 // quad core beside one-point z ends ran slower than whole one-point rows:
-// 0.398 against 0.384 ms.)
+// 0.398 against 0.384 ms; so did the B z ends of the rows as quads with the
+// quads that straddle a slab edge done point by point: 0.391 against 0.380.)
 //
 // The z neighbour of a quad (E one point up for B, H one point down for D)
 // comes from the next (previous) lane by a warp shuffle when that lane holds
