@@ -663,7 +663,12 @@ private:
   std::vector<Mon> mons;
   std::vector<std::complex<double>> Jdft;
   double Jsum = 1.0, saved_overall_scale = 1.0;
+  // the engine's monitors sample every step, so update() must run on every
+  // step for F and J to hold the same samples (checked in F, J and ldos)
+  long long last_t = -1;
+  bool skipped = false;
   void attach(fields &f);
+  void check_every_step() const;
 };
 
 // electric and magnetic energy density spectra in volumes (src/dft.cpp

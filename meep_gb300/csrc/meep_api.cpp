@@ -1920,6 +1920,7 @@ void dft_ldos::attach(fields &f) {
   for (const PendingSource &ps : I.pending) {
     if (ps.idx.empty()) continue;
     const int t = ps.c / 3, d = ps.c % 3;
+    // (sources on D or B components are refused when they are added)
     if (t != MFD_E && t != MFD_H) continue;
     // the field the reference reads for this source: E (or H) along its direction
     const int mc = 3 * t + d;
@@ -1957,9 +1958,16 @@ void dft_ldos::attach(fields &f) {
   Jsum *= std::sqrt(vol);
 }
 
+void dft_ldos::check_every_step() const {
+  if (skipped)
+    meep::abort("dft_ldos::update must run on every step: the engine's DFT of the fields samples every step");
+}
+
 void dft_ldos::update(fields &f) {
   if (!fld) attach(f);
   if (fld != &f) meep::abort("dft_ldos updated with another fields object");
+  if (last_t >= 0 && f.t > last_t + 1) skipped = true;
+  last_t = f.t;
   // the first source's current as the last step left it: its value at the
   // current time (none before the first step)
   if (f.t == 0 || f.d->srcs.empty()) return;
@@ -1974,6 +1982,7 @@ void dft_ldos::update(fields &f) {
 }
 
 std::complex<double> *dft_ldos::F() const {
+  check_every_step();
   const size_t nf = freq.size();
   std::complex<double> *out = new std::complex<double>[nf];
   for (size_t i = 0; i < nf; i++)
@@ -1991,6 +2000,7 @@ std::complex<double> *dft_ldos::F() const {
 }
 
 std::complex<double> *dft_ldos::J() const {
+  check_every_step();
   std::complex<double> *out = new std::complex<double>[freq.size()];
   for (size_t i = 0; i < freq.size(); i++)
     out[i] = Jdft[i];
@@ -1999,6 +2009,7 @@ std::complex<double> *dft_ldos::J() const {
 
 // dft_ldos::ldos (src/dft_ldos.cpp:63-86)
 double *dft_ldos::ldos() {
+  check_every_step();
   saved_overall_scale = 4.0 / pi * -0.5 / (Jsum * Jsum);
   std::complex<double> *Fd = F();
   double *out = new double[freq.size()];

@@ -66,3 +66,16 @@ def test_gpu_matches_reference(gpu_drivers, tmp_path):
     _check(run_driver(GPU_DRIVER[32], "py_ldos", tmp_path), ref, 1e-4)
     from meep_gb300.simulation import PRODUCT_LIB
     _check(script_ldos(PRODUCT_LIB), ref, 1e-10)
+
+
+def test_ldos_update_must_run_every_step(oracle_lib):
+    """The engine's DFT of the fields samples every step, so an LDOS whose
+    update runs less often (at_every) would mix samples: the results raise."""
+    import meep_gb300 as mp
+    lib = os.path.join(os.path.dirname(oracle_lib), "liboracle_meep.so")
+    sim = mp.Simulation(cell_size=mp.Vector3(4, 4), resolution=10, boundary_layers=[mp.PML(1)], eps_averaging=False,
+                        sources=[mp.Source(mp.GaussianSource(1.0, fwidth=0.2), component=mp.Ez,
+                                           center=mp.Vector3())], _library=lib)
+    ldos = mp.Ldos(1.0, 0.2, 3)
+    with pytest.raises(RuntimeError, match="every step"):
+        sim.run(mp.at_every(0.5, mp.dft_ldos(ldos=ldos)), until=5)
