@@ -1971,7 +1971,7 @@ public:
     size_t smem = (size_t)dm.cnt * chunk * sizeof(float2);
     long long np = (long long)m.npts;
     if (dm.tc)
-      dft_contract_tc_kernel<<<(unsigned)((np + TC_M - 1) / TC_M), 128, TC_SMEM, stream>>>(dm.A, dm.cnt, np, dm.B, nf,
+      dft_contract_tc_kernel<<<(unsigned)((np + TC_M - 1) / TC_M), TC_THREADS, TC_SMEM, stream>>>(dm.A, dm.cnt, np, dm.B, nf,
                                                                                           dm.acc, d_tc_err);
     else
       dft_contract_kernel<<<(unsigned)((np + 127) / 128), 128, smem, stream>>>(dm.A, dm.cnt, np, dm.B, nf, dm.acc);

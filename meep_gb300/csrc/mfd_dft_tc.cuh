@@ -10,9 +10,12 @@
 // Split precision (3xTF32): a = a_hi + a_lo and b = b_hi + b_lo, each part
 // rounded to TF32, and C = a_hi b_hi + a_hi b_lo + a_lo b_hi, accumulated in
 // FP32 over the 64 samples; the products dropped (a_lo b_lo) are below FP32
-// rounding.  The four warps read the accumulator back (warp w owns TMEM lanes
-// 32w..32w+31 = points) into a shared tile, and add it to the FP64 running
-// sums row by row (a warp per point row, lanes along frequency: coalesced).
+// rounding.  Eight warps read the accumulator back (warp w owns TMEM lanes
+// 32 (w % 4) .. + 31 = points and columns 32 (w / 4) .. + 31) into a shared
+// tile, and add it to the FP64 running sums row by row (a warp per point row,
+// lanes along frequency: coalesced; eight rows per warp in flight).  The FP64
+// update bounds the kernel, so the eight warps (two CTAs per SM) double the
+// loads in flight of a four-warp CTA.
 //
 // Operands are K-major in shared memory without swizzle: the canonical layout
 // of 8-row x 16-byte core matrices, element (r, k) of a tile at byte
@@ -99,8 +102,9 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
 
 // A: [64][npts] samples (rows t >= cnt are stale and read as zero); B:
 // [64][nf] phases; acc: [npts][nf] FP64 sums; err: set to 1 when a wait ran
-// out.  Block: 128 threads.  Dynamic shared memory: TC_SMEM.
-static __global__ void __launch_bounds__(128, 1)
+// out.  Block: TC_THREADS threads.  Dynamic shared memory: TC_SMEM.
+constexpr int TC_THREADS = 256;
+static __global__ void __launch_bounds__(TC_THREADS, 1)
     dft_contract_tc_kernel(const float *__restrict__ A, int cnt, long long npts, const float2 *__restrict__ B,
                            int nf, double2 *__restrict__ acc, int *err) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -121,13 +125,17 @@ static __global__ void __launch_bounds__(128, 1)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem_addr(&mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  // the sample tile, split into TF32 hi / lo parts: thread = point row
-  for (int t = 0; t < TC_K; t++) {
-    const long long p = p0 + tid;
-    const float a = (t < cnt && p < npts) ? A[(long long)t * npts + p] : 0.0f;
-    const float hi = tc_tf32(a), lo = tc_tf32(a - hi);
-    *reinterpret_cast<float *>(sAhi + tc_off(tid, t)) = hi;
-    *reinterpret_cast<float *>(sAlo + tc_off(tid, t)) = lo;
+  // the sample tile, split into TF32 hi / lo parts: thread = point row and
+  // half of the samples
+  {
+    const int row = tid & (TC_M - 1), t0 = (tid / TC_M) * (TC_K / 2);
+    for (int t = t0; t < t0 + TC_K / 2; t++) {
+      const long long p = p0 + row;
+      const float a = (t < cnt && p < npts) ? A[(long long)t * npts + p] : 0.0f;
+      const float hi = tc_tf32(a), lo = tc_tf32(a - hi);
+      *reinterpret_cast<float *>(sAhi + tc_off(row, t)) = hi;
+      *reinterpret_cast<float *>(sAlo + tc_off(row, t)) = lo;
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -182,33 +190,35 @@ static __global__ void __launch_bounds__(128, 1)
     // accumulator row (point 32 warp + lane of the CTA) into a shared tile over
     // the phase buffers (the MMAs that read them have completed)
     float *tile = reinterpret_cast<float *>(sBhi);
+    const int quad = warp & 3, half = warp >> 2, trow = quad * 32 + lane;
 #pragma unroll
-    for (int c0 = 0; c0 < TC_N; c0 += 8) {
+    for (int c0 = half * (TC_N / 2); c0 < (half + 1) * (TC_N / 2); c0 += 8) {
       uint32_t r[8];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0;
       asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                    : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
       for (int j = 0; j < 8; j++)
-        tile[tid * TC_T_STRIDE + c0 + j] = __uint_as_float(r[j]);
+        tile[trow * TC_T_STRIDE + c0 + j] = __uint_as_float(r[j]);
     }
     __syncthreads();
     // FP64 running sums, one point row per warp at a time: lane = frequency,
     // so each warp reads and writes 32 consecutive complex doubles of a row
     // (eight rows per batch: their loads are all in flight before any store)
     const int w = w0 + lane;
-    for (int row0 = warp; row0 < TC_M; row0 += 4 * 8) {
+    constexpr int NW = TC_THREADS / 32;
+    for (int row0 = warp; row0 < TC_M; row0 += NW * 8) {
       double2 v[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        const long long p = p0 + row0 + 4 * j;
+        const long long p = p0 + row0 + NW * j;
         v[j] = (p < npts && w < nf) ? acc[p * nf + w] : make_double2(0.0, 0.0);
       }
 #pragma unroll
       for (int j = 0; j < 8; j++) {
-        const int row = row0 + 4 * j;
+        const int row = row0 + NW * j;
         const long long p = p0 + row;
         if (p < npts && w < nf) {
           v[j].x += (double)tile[row * TC_T_STRIDE + 2 * lane];

@@ -81,7 +81,7 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
                    nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True,
-                   boxed=False, palette=False):
+                   boxed=False, palette=False, bcond=False, poles_below=None):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -96,7 +96,10 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     pole or a conductivity is absent next to runs where it is present.
     palette: permittivities, conductivities and pole strengths take a few
     values only (eps 1, 4, 12; conductivity 0, 0.3; sigma 0, 0.7, 1.5), as
-    in structures built from a few media."""
+    in structures built from a few media.
+    bcond: conductivities on the B components too.
+    poles_below: pole strengths zero at z points >= poles_below (a layer of
+    dispersive medium at the low z end, as the dispersive benchmark has)."""
     rng = np.random.default_rng(seed)
     nrand = n
     if dim == 2:
@@ -148,7 +151,7 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
 
     if cond:
         for c in comps:
-            if c // 3 == _lib.D:
+            if c // 3 == _lib.D or (bcond and c // 3 == _lib.B):
                 arr = np.where(rng.uniform(size=shape) < 0.3, rng.uniform(0, 0.5, size=shape), 0.0)
                 if boxed:
                     arr = np.where(box_mask(), rng.uniform(0, 0.5, size=shape), 0.0)
@@ -163,6 +166,10 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
                 arr = rng.uniform(0, 2.0, size=shape) if c in comps else None
                 if boxed and arr is not None:
                     arr = np.where(box_mask(), arr, 0.0)
+                if poles_below is not None and arr is not None:
+                    # poles only in the low z layer (points k_z < poles_below)
+                    arr = arr.copy()
+                    arr[..., poles_below:] = 0.0
                 if palette and arr is not None:
                     arr = pal(arr, [0.0, 0.7, 1.5])
                 sig.append(arr)

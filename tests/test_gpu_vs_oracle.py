@@ -145,3 +145,31 @@ def test_palette_materials_fp32(engine_lib, oracle_lib):
     o = _run(oracle_lib, 65, 3, 32, **kw)
     for k in o:
         assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
+
+
+@pytest.mark.parametrize("seed,n,kw", [(71, (16, 14, 100), dict(bcond=True)),
+                                       (72, (17, 15, 130), dict(poles_below=64)),
+                                       (73, (16, 16, 100), dict(poles_below=48, bcond=True, palette=True))])
+def test_bcond_and_layered_poles_fp64_bitwise(seed, n, kw, engine_lib, oracle_lib):
+    """B conductivity (the B kernels' conductivity branch, FP32 quads on the
+    faces) and poles confined to a low z layer (rows and faces split along z
+    at the poles' extent): every field bit equals the oracle's in FP64."""
+    kw = dict(kw, ecur=False, n=n, steps=60)
+    g = _run(engine_lib, seed, 3, 64, **kw)
+    o = _run(oracle_lib, seed, 3, 64, **kw)
+    for k in o:
+        if k.startswith("c"):
+            assert np.array_equal(g[k], o[k]), k
+        else:
+            assert relerr(g[k], o[k]) <= 1e-13, (k, relerr(g[k], o[k]))
+
+
+@pytest.mark.parametrize("seed,n,kw", [(71, (16, 14, 100), dict(bcond=True)),
+                                       (72, (17, 15, 130), dict(poles_below=64)),
+                                       (73, (16, 16, 100), dict(poles_below=48, bcond=True, palette=True))])
+def test_bcond_and_layered_poles_fp32(seed, n, kw, engine_lib, oracle_lib):
+    kw = dict(kw, ecur=False, n=n, steps=60)
+    g = _run(engine_lib, seed, 3, 32, **kw)
+    o = _run(oracle_lib, seed, 3, 32, **kw)
+    for k in o:
+        assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
