@@ -1775,12 +1775,8 @@ public:
       fork();
       // FP64 (issue-bound): the flagless core and the z ends; FP32
       // (bandwidth-bound): whole rows, whose z slabs ride along in full warps
-      // the D/E rows walk x downwards: the B half-step ended at high x, so its
-      // last planes are still in L2
-      Band rows = band_rows, core = band_core;
-      rows.rev = core.rev = 1;
       if (!F32 && band_core.s[2].n > 0) {
-        launch_de_band<false, false, false>(core, a, cndD, zp, stream);
+        launch_de_band<false, false, false>(band_core, a, cndD, zp, stream);
         launch_de_band<false, false>(band_zend, a, cndD, zp, side[2]);
       }
       else if (a.npoles > 0 && pole_z1 >= 0 && (pole_z0 > 0 || std::min(pole_z1, p.N[2]) < p.N[2])) {
@@ -1789,11 +1785,11 @@ public:
         // elsewhere (P stays 0 there; its registers would only cost occupancy)
         const int z1 = std::min(pole_z1, p.N[2]);
         if (z1 > pole_z0) {
-          Band bp = rows;
+          Band bp = band_rows;
           bp.s[2] = span_run(pole_z0, z1 - 1);
           launch_de_band<false, false>(bp, a, cndD, zp, stream);
         }
-        Band bn = rows;
+        Band bn = band_rows;
         bn.s[2] = z1 > pole_z0 ? span_outside(p.N[2], pole_z0, z1 - 1) : span_run(0, p.N[2] - 1);
         dim3 g, blk;
         band_shape(bn, g, blk);
@@ -1803,7 +1799,7 @@ public:
         }
       }
       else
-        launch_de_band<false, false>(rows, a, cndD, zp, stream);
+        launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
       // D/E faces: with poles confined to one end of the z interior, its
       // pole-free part as quads and the rest in the shell
       bool split = false;

@@ -23,7 +23,6 @@ struct Span {
 };
 struct Band {
   Span s[3];
-  int rev; // 1: blocks walk x downwards (the D/E rows start where the B half-step ended, in L2)
 };
 
 template <typename R> struct CurlRes {
@@ -128,8 +127,8 @@ __device__ __forceinline__ void band_flags(const FusedArgs<R> &a, const int k[3]
 
 // point of this thread; false past the end of the band
 __device__ __forceinline__ bool band_coords(const Band &bd, int k[3]) {
-  const int t[3] = {bd.rev ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z,
-                    (int)(blockIdx.y * blockDim.y + threadIdx.y), (int)(blockIdx.x * blockDim.x + threadIdx.x)};
+  const int t[3] = {(int)blockIdx.z, (int)(blockIdx.y * blockDim.y + threadIdx.y),
+                    (int)(blockIdx.x * blockDim.x + threadIdx.x)};
   if (t[1] >= bd.s[1].n || t[2] >= bd.s[2].n) return false;
 #pragma unroll
   for (int d = 0; d < 3; d++)
