@@ -1706,13 +1706,16 @@ public:
     if constexpr (DIM == 3) {
       fork();
       if constexpr (F32) {
+        // the side streams' launches first (their blocks go first anyway)
+        launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
+        launch_b_qfaces(a, cndB, side[1]);
+        launch_b_shell(a, cndB, zp, side[0]);
         const dim3 g = core_grid();
         if (g.x) {
           if (cndB) b3q_core_kernel<true><<<g, 256, 0, stream>>>(a, qcore);
           else b3q_core_kernel<false><<<g, 256, 0, stream>>>(a, qcore);
           nlaunch++;
         }
-        launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
       }
       else if (band_core.s[2].n > 0) {
         launch_b_band<false, false, false>(band_core, a, cndB, zp, stream);
@@ -1723,12 +1726,7 @@ public:
       // the shell: x and y slab faces over their z interior (no z flags;
       // FP32: quads, a launch of their own) and their z ends, and the x-y
       // edges, one launch; the z ends of the rows beside them
-      if (F32) {
-        launch_b_qfaces(a, cndB, side[1]);
-        launch_b_shell(a, cndB, zp, side[0]);
-      }
-      else
-        launch_b_shell_bands(a, cndB, zp);
+      if (!F32) launch_b_shell_bands(a, cndB, zp);
       join();
     }
     else {
