@@ -1771,33 +1771,7 @@ public:
       }
     if constexpr (DIM == 3) {
       fork();
-      // FP64 (issue-bound): the flagless core and the z ends; FP32
-      // (bandwidth-bound): whole rows, whose z slabs ride along in full warps
-      if (!F32 && band_core.s[2].n > 0) {
-        launch_de_band<false, false, false>(band_core, a, cndD, zp, stream);
-        launch_de_band<false, false>(band_zend, a, cndD, zp, side[2]);
-      }
-      else if (a.npoles > 0 && pole_z1 >= 0 && (pole_z0 > 0 || std::min(pole_z1, p.N[2]) < p.N[2])) {
-        // rows (z points 0..N-1) split along z at the pole region: the kernel
-        // with poles in registers where some pole is active, the pole-free one
-        // elsewhere (P stays 0 there; its registers would only cost occupancy)
-        const int z1 = std::min(pole_z1, p.N[2]);
-        if (z1 > pole_z0) {
-          Band bp = band_rows;
-          bp.s[2] = span_run(pole_z0, z1 - 1);
-          launch_de_band<false, false>(bp, a, cndD, zp, stream);
-        }
-        Band bn = band_rows;
-        bn.s[2] = z1 > pole_z0 ? span_outside(p.N[2], pole_z0, z1 - 1) : span_run(0, p.N[2] - 1);
-        dim3 g, blk;
-        band_shape(bn, g, blk);
-        if (g.x) {
-          launch_de_band_p<false, false, 0>(bn, g, blk, a, cndD, zp, side[2]);
-          nlaunch++;
-        }
-      }
-      else
-        launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
+      // the side streams' launches first (their blocks start at once).
       // D/E faces: with poles confined to one end of the z interior, its
       // pole-free part as quads and the rest in the shell
       bool split = false;
@@ -1834,6 +1808,33 @@ public:
       }
       else if (!split)
         launch_de_shell_bands(a, cndD, zp);
+      // FP64 (issue-bound): the flagless core and the z ends; FP32
+      // (bandwidth-bound): whole rows, whose z slabs ride along in full warps
+      if (!F32 && band_core.s[2].n > 0) {
+        launch_de_band<false, false>(band_zend, a, cndD, zp, side[2]);
+        launch_de_band<false, false, false>(band_core, a, cndD, zp, stream);
+      }
+      else if (a.npoles > 0 && pole_z1 >= 0 && (pole_z0 > 0 || std::min(pole_z1, p.N[2]) < p.N[2])) {
+        // rows (z points 0..N-1) split along z at the pole region: the kernel
+        // with poles in registers where some pole is active, the pole-free one
+        // elsewhere (P stays 0 there; its registers would only cost occupancy)
+        const int z1 = std::min(pole_z1, p.N[2]);
+        Band bn = band_rows;
+        bn.s[2] = z1 > pole_z0 ? span_outside(p.N[2], pole_z0, z1 - 1) : span_run(0, p.N[2] - 1);
+        dim3 g, blk;
+        band_shape(bn, g, blk);
+        if (g.x) {
+          launch_de_band_p<false, false, 0>(bn, g, blk, a, cndD, zp, side[2]);
+          nlaunch++;
+        }
+        if (z1 > pole_z0) {
+          Band bp = band_rows;
+          bp.s[2] = span_run(pole_z0, z1 - 1);
+          launch_de_band<false, false>(bp, a, cndD, zp, stream);
+        }
+      }
+      else
+        launch_de_band<false, false>(band_rows, a, cndD, zp, stream);
       join();
     }
     else {
