@@ -295,6 +295,12 @@ struct SrcPoint {
   double amp[MAXS][2];
 };
 
+// Empty kernel put on the main stream between a join and the next fork when
+// no other kernel sits there: with the fork's event recorded right behind the
+// join's waits, the next half-step's launches started about 6 us later on
+// GB300 (measured over the 256^3 and 384^2 x 192 steps)
+static __global__ void stream_order_kernel() {}
+
 template <typename R> struct SrcBuf {
   EPoint<R> *v;
 };
@@ -303,6 +309,28 @@ struct DipoleVals {
   double re[16], im[16];
 };
 
+// term t of a source point: the real part of amp * dipole (the std::complex
+// product), rounded product by product as on the host
+__device__ __forceinline__ double src_term(const SrcPoint &sp, int t, const DipoleVals &dv) {
+  return __dsub_rn(__dmul_rn(sp.amp[t][0], dv.re[sp.src[t]]), __dmul_rn(sp.amp[t][1], dv.im[sp.src[t]]));
+}
+
+// Integrated E sources at points without an active pole and outside the E
+// slab of their own direction, after the D/E launches left D final there
+// and E = D chi1inv: E = (D - the terms in list order) chi1inv, the f_minus_p
+// of update_eh less the sources (src/update_eh.cpp:108-137; a pole with zero
+// sigma keeps P = 0, and D - 0 = D)
+template <typename R>
+__global__ void src_e_kernel(R *e, const R *dfield, const R *chi, const SrcPoint *pts, int n, DipoleVals dv) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const SrcPoint &sp = pts[j];
+  R gs = dfield[sp.i];
+  for (int t = 0; t < sp.nterm; t++)
+    gs -= R(src_term(sp, t, dv));
+  e[sp.i] = gs * chi[sp.i];
+}
+
 template <typename R>
 __global__ void src_pre_kernel(Geo g, Tables<R> tb, EArgs<R> a, const SrcPoint *pts, int n,
                                DipoleVals dv, EPoint<R> *out) {
@@ -310,11 +338,8 @@ __global__ void src_pre_kernel(Geo g, Tables<R> tb, EArgs<R> a, const SrcPoint *
   if (j >= n) return;
   const SrcPoint &sp = pts[j];
   R A[MAXS];
-  for (int t = 0; t < sp.nterm; t++) {
-    // real part of amp * dipole (std::complex product)
-    double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
-    A[t] = R(re);
-  }
+  for (int t = 0; t < sp.nterm; t++)
+    A[t] = R(src_term(sp, t, dv));
   e_point(g, tb, a, sp.k, sp.i, sp.nterm, A, out[j]);
 }
 
@@ -351,7 +376,7 @@ template <typename R> __global__ void src_fmp_kernel(FmpArgs<R> fa, const SrcPoi
   for (int q = 0; q < fa.np; q++)
     if (fa.p[q]) v -= fa.p[q][sp.i];
   for (int t = 0; t < sp.nterm; t++) {
-    const double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
+    const double re = src_term(sp, t, dv);
     v -= R(re);
   }
   fmp[sp.i] = v;
@@ -677,6 +702,13 @@ public:
       cuda_check(cudaEventCreateWithFlags(&side_ev[q], cudaEventDisableTiming), "event");
     }
     cuda_check(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming), "event");
+    // E/D monitors of the 3-D step: samples and block contractions on
+    // low-priority streams, their blocks filling in beside the next B
+    // half-step (high priority measured 2 us per step slower)
+    cuda_check(cudaStreamCreateWithPriority(&dstream, cudaStreamNonBlocking, prio_lo), "stream");
+    cuda_check(cudaStreamCreateWithPriority(&fstream, cudaStreamNonBlocking, prio_lo), "stream");
+    for (cudaEvent_t *e : {&dft_in_ev, &dft_out_ev, &fl_in_ev, &fl_out_ev})
+      cuda_check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
     (void)p;
   }
   ~CudaBackend() override {
@@ -690,6 +722,13 @@ public:
       cudaStreamDestroy(side[q]);
     }
     cudaEventDestroy(fork_ev);
+    for (DMon &dm : mons)
+      for (cudaEvent_t e : dm.fdone)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {dft_in_ev, dft_out_ev, fl_in_ev, fl_out_ev})
+      cudaEventDestroy(e);
+    cudaStreamDestroy(dstream);
+    cudaStreamDestroy(fstream);
     cudaStreamDestroy(stream);
   }
 
@@ -702,15 +741,40 @@ public:
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t side_ev[NSIDE] = {}, fork_ev = nullptr;
   void fork() {
-    cuda_check(cudaEventRecord(fork_ev, stream), "event record");
+    cudaEvent_t ev = fork_from ? fork_from : fork_ev;
+    if (!fork_from) cuda_check(cudaEventRecord(fork_ev, stream), "event record");
+    fork_from = nullptr;
     for (int q = 0; q < NSIDE; q++)
-      cuda_check(cudaStreamWaitEvent(side[q], fork_ev, 0), "stream wait");
+      cuda_check(cudaStreamWaitEvent(side[q], ev, 0), "stream wait");
   }
   void join() {
     for (int q = 0; q < NSIDE; q++) {
       cuda_check(cudaEventRecord(side_ev[q], side[q]), "event record");
       cuda_check(cudaStreamWaitEvent(stream, side_ev[q], 0), "stream wait");
     }
+  }
+  // DFT work off the main stream: the samples of E/D monitors (read E or D
+  // after a step; the next B half-step runs beside them, the next D/E
+  // half-step waits for them) and the block contractions (read the staged
+  // samples, write the running sums; everything else that reads the sums or
+  // the fields waits for both first)
+  cudaStream_t dstream = nullptr, fstream = nullptr;
+  cudaEvent_t dft_in_ev = nullptr, dft_out_ev = nullptr, fl_in_ev = nullptr, fl_out_ev = nullptr;
+  cudaEvent_t fork_from = nullptr; // event at the main stream's tail for the next fork, if any
+  bool dft_pending = false, fl_pending = false;
+  void join_samples() {
+    fork_from = nullptr;
+    if (!dft_pending) return;
+    cuda_check(cudaEventRecord(dft_out_ev, dstream), "event record");
+    cuda_check(cudaStreamWaitEvent(stream, dft_out_ev, 0), "stream wait");
+    dft_pending = false;
+  }
+  void join_dft() {
+    join_samples();
+    if (!fl_pending) return;
+    cuda_check(cudaEventRecord(fl_out_ev, fstream), "event record");
+    cuda_check(cudaStreamWaitEvent(stream, fl_out_ev, 0), "stream wait");
+    fl_pending = false;
   }
   std::vector<void *> allocs;
   Geo geo{};
@@ -792,6 +856,10 @@ public:
   // sources
   SrcPoint *d_srcpts[3] = {};
   int nsrcpts[3] = {};
+  // every integrated E source point of the 3-D step has no active pole and
+  // lies outside the E slab of its own direction: its E is set from the
+  // final D after the D/E launches (no kernel before them)
+  bool src_e_only = false;
   EPoint<R> *d_srcbuf[3] = {};
   DEOut<R> *d_fsrcbuf[3] = {};
   CurPoint *d_cur[NC] = {};
@@ -803,10 +871,17 @@ public:
     double *w[3] = {};
     bool block = false;      // blocked FP32 contraction
     bool tc = false;         // ... on the tensor cores (3xTF32 tcgen05)
-    float *A = nullptr;      // [DFT_BLOCK_T][npts] samples
+    float *A = nullptr;      // [DFT_BLOCK_T][npts] samples of the current block
     float2 *B = nullptr;     // [DFT_BLOCK_T][nf] phases
     int cnt = 0;             // samples in the current block
     long long tn0 = 0;       // step count of the block's first sample
+    // sampled off the main stream: two staging blocks, one filling while
+    // the other is contracted; fdone[b] marks the end of block b's contraction
+    bool async = false;
+    float *Ab[2] = {};
+    int cur = 0;
+    bool issued[2] = {};
+    cudaEvent_t fdone[2] = {};
   };
   std::vector<DMon> mons;
   int *d_tc_err = nullptr; // set by the tensor-core contraction when a wait ran out
@@ -1048,6 +1123,7 @@ public:
   }
   void matgrid_vjp(Plan &p, int id, const std::vector<int> &comps, const int lo[3], const int hi[3],
                    const double *gchi, double *gu) override {
+    join_dft();
     const Plan::MatGrid &mg = p.matgrids[id];
     std::vector<MatGridSpec> specs;
     for (const Plan::MatGrid &m : p.matgrids)
@@ -1744,6 +1820,7 @@ public:
       for (int d = 0; d < 3; d++)
         if (p.have[comp(MFD_H, d)]) update_h(p, comp(MFD_H, d));
     }
+    join_samples(); // the previous step's E/D samples read what D/E writes
     bool dcur = false;
     for (int d = 0; d < 3; d++)
       dcur = dcur || ncur[comp(MFD_D, d)] > 0;
@@ -1763,13 +1840,18 @@ public:
         return;
       }
     }
+    const bool e_only = DIM == 3 && src_e_only;
     for (int d = 0; d < 3; d++)
-      if (nsrcpts[d]) {
+      if (nsrcpts[d] && !e_only) {
         fused_src_pre_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(
             a, d_srcpts[d], nsrcpts[d], d, dip, d_fsrcbuf[d]);
         nlaunch++;
       }
     if constexpr (DIM == 3) {
+      if (e_only || !(nsrcpts[0] || nsrcpts[1] || nsrcpts[2])) {
+        stream_order_kernel<<<1, 32, 0, stream>>>();
+        nlaunch++;
+      }
       fork();
       // the side streams' launches first (their blocks start at once).
       // D/E faces: with poles confined to one end of the z interior, its
@@ -1849,8 +1931,12 @@ public:
     }
     for (int d = 0; d < 3; d++)
       if (nsrcpts[d]) {
-        fused_src_post_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(
-            a, d_srcpts[d], nsrcpts[d], d, d_fsrcbuf[d]);
+        if (e_only)
+          src_e_kernel<R><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(a.e[d], a.d[d], a.chi[d], d_srcpts[d],
+                                                                         nsrcpts[d], dip);
+        else
+          fused_src_post_kernel<R, DIM, MASK><<<(nsrcpts[d] + 127) / 128, 128, 0, stream>>>(
+              a, d_srcpts[d], nsrcpts[d], d, d_fsrcbuf[d]);
         nlaunch++;
       }
   }
@@ -1868,6 +1954,7 @@ public:
   void setup_sources(Plan &p) {
     if (p.srcs.size() > 16) throw Error("at most 16 source time functions are supported");
     // integrated E sources grouped per (component, point), in list order
+    bool e_only = p.g.dim == 3 && !p.any_offdiag;
     for (int d = 0; d < 3; d++) {
       std::vector<SrcPoint> pts;
       std::vector<int64_t> keys;
@@ -1896,11 +1983,19 @@ public:
       // neighbouring E points, so they stay (only f_minus_p uses the list then)
       std::vector<SrcPoint> keep;
       int ec = comp(MFD_E, d);
-      for (const SrcPoint &sp : pts) {
+      for (size_t q0 = 0; q0 < pts.size(); q0++) {
+        const SrcPoint &sp = pts[q0];
         bool in = true;
         for (int q = 0; q < 3; q++)
           in = in && sp.k[q] >= p.klo[ec][q] && sp.k[q] <= p.khi[ec][q];
-        if (in || p.any_offdiag) keep.push_back(sp);
+        if (!(in || p.any_offdiag)) continue;
+        keep.push_back(sp);
+        // E_d sits at half-pixel 2k + 1 along d; its f_w slab there
+        const int pw = 2 * sp.k[d] + 1;
+        if (p.pml_dir[d] && ((p.T[d][0] > 0 && pw <= 2 * p.T[d][0]) || (p.T[d][1] > 0 && pw > 2 * (p.N[d] - p.T[d][1]))))
+          e_only = false;
+        for (const Pole &pl : p.poles)
+          if (!pl.sigma[d].empty() && pl.sigma[d][keys[q0]] != 0.0) e_only = false;
       }
       nsrcpts[d] = (int)keep.size();
       if (!keep.empty()) {
@@ -1909,6 +2004,7 @@ public:
         d_fsrcbuf[d] = dalloc<DEOut<R>>(keep.size());
       }
     }
+    src_e_only = e_only;
     // current sources (non-integrated) on D or B
     for (int c = 0; c < NC; c++) {
       int t = ctype(c);
@@ -1932,6 +2028,7 @@ public:
   }
 
   void add_monitor(Plan &p, int id) override {
+    join_dft();
     if ((int)mons.size() <= id) mons.resize(id + 1);
     const Monitor &m = p.monitors[id];
     DMon &dm = mons[id];
@@ -1950,32 +2047,51 @@ public:
       cuda_check(cudaFuncSetAttribute(dft_contract_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM),
                  "tensor-core DFT shared memory");
     }
+    const int t = ctype(m.c);
+    dm.async = fused_mask == MASK3 && (t == MFD_E || t == MFD_D);
     if (dm.block) {
-      dm.A = dalloc<float>((size_t)DFT_BLOCK_T * m.npts);
+      dm.Ab[0] = dm.A = dalloc<float>((size_t)DFT_BLOCK_T * m.npts);
       dm.B = dalloc<float2>((size_t)DFT_BLOCK_T * m.freq.size());
+      if (dm.async) {
+        dm.Ab[1] = dalloc<float>((size_t)DFT_BLOCK_T * m.npts);
+        for (cudaEvent_t &e : dm.fdone)
+          cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+      }
     }
     cuda_check(cudaStreamSynchronize(stream), "monitor sync");
   }
 
   // contract the samples of the current block into the running sums
   void dft_flush(Plan &p, int id) {
+    join_dft();
+    flush_on(p, id, stream);
+  }
+  void flush_on(Plan &p, int id, cudaStream_t st) {
     const Monitor &m = p.monitors[id];
     DMon &dm = mons[id];
     if (!dm.block || dm.cnt == 0) return;
     const int nf = (int)m.freq.size();
     const int half = (ctype(m.c) == MFD_H || ctype(m.c) == MFD_B) ? 1 : 0;
-    dft_block_phase_kernel<<<dim3((nf + 127) / 128, dm.cnt), 128, 0, stream>>>(
+    dft_block_phase_kernel<<<dim3((nf + 127) / 128, dm.cnt), 128, 0, st>>>(
         dm.freq, nf, dm.cnt, dm.tn0, m.decimation, p.dt, half, m.scale.real(), m.scale.imag(), dm.B);
     const int chunk = 64; // frequencies per shared-memory pass (<= 32 KB)
     size_t smem = (size_t)dm.cnt * chunk * sizeof(float2);
     long long np = (long long)m.npts;
     if (dm.tc)
-      dft_contract_tc_kernel<<<(unsigned)((np + TC_M - 1) / TC_M), TC_THREADS, TC_SMEM, stream>>>(dm.A, dm.cnt, np, dm.B, nf,
-                                                                                          dm.acc, d_tc_err);
+      dft_contract_tc_kernel<<<(unsigned)((np + TC_M - 1) / TC_M), TC_THREADS, TC_SMEM, st>>>(dm.A, dm.cnt, np, dm.B,
+                                                                                              nf, dm.acc, d_tc_err);
     else
-      dft_contract_kernel<<<(unsigned)((np + 127) / 128), 128, smem, stream>>>(dm.A, dm.cnt, np, dm.B, nf, dm.acc);
+      dft_contract_kernel<<<(unsigned)((np + 127) / 128), 128, smem, st>>>(dm.A, dm.cnt, np, dm.B, nf, dm.acc);
     nlaunch += 2;
     dm.cnt = 0;
+    if (dm.async) {
+      // the next samples go to the other staging block once its own
+      // contraction is done
+      cuda_check(cudaEventRecord(dm.fdone[dm.cur], st), "event record");
+      dm.issued[dm.cur] = true;
+      dm.cur ^= 1;
+      dm.A = dm.Ab[dm.cur];
+    }
   }
 
   Box full_box(const Plan &p, int c) const {
@@ -2172,10 +2288,34 @@ public:
     }
   }
 
+  // E/D monitors of the 3-D step: sampled on dstream once the step's main
+  // stream work is queued (launch_samples)
+  struct QueuedSample {
+    int id;
+    double time;
+    int64_t tn;
+  };
+  std::vector<QueuedSample> queued;
   void dft(Plan &p, int id, double time, int64_t tn) {
+    bump(id);
+    if (mons[id].async) queued.push_back({id, time, tn});
+    else dft_launch(p, id, time, tn, stream);
+  }
+  void launch_samples(Plan &p) {
+    if (queued.empty()) return;
+    cuda_check(cudaEventRecord(dft_in_ev, stream), "event record");
+    cuda_check(cudaStreamWaitEvent(dstream, dft_in_ev, 0), "stream wait");
+    // the next fork waits on the same event (nothing is queued on the main
+    // stream behind it before then; every other call joins first)
+    fork_from = dft_in_ev;
+    dft_pending = true;
+    for (const QueuedSample &q : queued)
+      dft_launch(p, q.id, q.time, q.tn, dstream);
+    queued.clear();
+  }
+  void dft_launch(Plan &p, int id, double time, int64_t tn, cudaStream_t st) {
     const Monitor &m = p.monitors[id];
     DMon &dm = mons[id];
-    bump(id);
     int nf = (int)m.freq.size();
     DftArgs<R> a{};
     a.f = f[m.c];
@@ -2214,20 +2354,33 @@ public:
     a.nf = nf;
     a.npts = (long long)m.npts;
     if (dm.block) {
-      if (dm.cnt == 0) dm.tn0 = tn;
-      dft_sample_kernel<R><<<(unsigned)((a.npts + 255) / 256), 256, 0, stream>>>(geo, a,
-                                                                               dm.A + (size_t)dm.cnt * m.npts);
+      if (dm.cnt == 0) {
+        dm.tn0 = tn;
+        if (dm.async && dm.issued[dm.cur]) {
+          cuda_check(cudaStreamWaitEvent(dstream, dm.fdone[dm.cur], 0), "stream wait");
+          dm.issued[dm.cur] = false;
+        }
+      }
+      dft_sample_kernel<R><<<(unsigned)((a.npts + 255) / 256), 256, 0, st>>>(geo, a, dm.A + (size_t)dm.cnt * m.npts);
       nlaunch++;
-      if (++dm.cnt == DFT_BLOCK_T) dft_flush(p, id);
+      if (++dm.cnt == DFT_BLOCK_T) {
+        if (dm.async) {
+          cuda_check(cudaEventRecord(fl_in_ev, dstream), "event record");
+          cuda_check(cudaStreamWaitEvent(fstream, fl_in_ev, 0), "stream wait");
+          flush_on(p, id, fstream);
+          fl_pending = true;
+        }
+        else
+          dft_flush(p, id);
+      }
       return;
     }
-    dft_phase_kernel<<<(nf + 127) / 128, 128, 0, stream>>>(dm.freq, nf, time, m.scale.real(), m.scale.imag(),
-                                                            dm.ph);
+    dft_phase_kernel<<<(nf + 127) / 128, 128, 0, st>>>(dm.freq, nf, time, m.scale.real(), m.scale.imag(), dm.ph);
     nlaunch++;
     long long total = a.npts * nf;
     int bs = 256;
     long long nb = (total + bs - 1) / bs;
-    dft_kernel<R><<<(unsigned)nb, bs, 0, stream>>>(geo, a);
+    dft_kernel<R><<<(unsigned)nb, bs, 0, st>>>(geo, a);
     nlaunch++;
   }
 
@@ -2287,12 +2440,14 @@ public:
       dft(p, (int)id, time, tn);
     }
     if (finite_every > 0 && tn % finite_every == 0) launch_finite_probe(p);
+    launch_samples(p);
   }
 
   void begin_steps() override {
     cuda_check(cudaEventRecord(ev0, stream), "event record");
   }
   void end_steps() override {
+    join_dft();
     cuda_check(cudaEventRecord(ev1, stream), "event record");
     cuda_check(cudaEventSynchronize(ev1), "event sync");
     float fms = 0;
@@ -2305,6 +2460,7 @@ public:
   double last_step_ms() const override { return ms; }
   long long launches() const override { return nlaunch; }
   void synchronize() override {
+    join_dft();
     cuda_check(cudaStreamSynchronize(stream), "sync");
     check_finite();
   }
@@ -2325,6 +2481,7 @@ public:
   void set_skip_dft(bool s) override { skip_dft = s; }
 
   void set_design(Plan &p, const std::vector<int> &comps, const int lo[3], const int hi[3]) override {
+    join_dft();
     for (int c : comps)
       if (ctype(c) != MFD_E || !p.have[c]) throw Error("design components must be allocated E components");
     if (!p.poles.empty()) throw Error("the adjoint does not support dispersive materials yet");
@@ -2353,6 +2510,7 @@ public:
   }
 
   void alloc_record(Plan &p, int64_t nslots) override {
+    join_dft();
     (void)p;
     if (nslots <= rec_slots) return;
     rec = dalloc<R>((size_t)nslots * dcomps.size() * dnpts);
@@ -2360,6 +2518,7 @@ public:
   }
 
   void record_design(Plan &p, int64_t slot) override {
+    join_dft();
     for (size_t q = 0; q < dcomps.size(); q++) {
       int dc = comp(MFD_D, cdir(dcomps[q]));
       dim3 grid, block;
@@ -2385,6 +2544,7 @@ public:
   }
 
   int snapshot(Plan &p) override {
+    join_dft();
     collect_state(p);
     size_t tot = 0;
     for (auto &s_ : state_list)
@@ -2400,6 +2560,7 @@ public:
   }
 
   void restore(Plan &p, int slot) override {
+    join_dft();
     collect_state(p);
     size_t off = 0;
     for (auto &s_ : state_list) {
@@ -2410,6 +2571,7 @@ public:
   }
 
   void adjoint_begin(Plan &p, int nmon, const int *ids, const double *const *grads) override {
+    join_dft();
     for (int c = 0; c < NC; c++) {
       if (!p.have[c]) continue;
       if (!lam_f[c]) lam_f[c] = dalloc<R>(p.nstore);
@@ -2475,6 +2637,7 @@ public:
   }
 
   void adjoint_step(Plan &p, int64_t s, int64_t slot) override {
+    join_dft();
     // 1. objective terms of the DFT samples taken after this step
     const int64_t tn = s + 1;
     for (size_t id = 0; id < p.monitors.size(); id++) {
@@ -2669,6 +2832,7 @@ public:
   }
 
   void adjoint_end(Plan &p, double *out) override {
+    join_dft();
     (void)p;
     size_t n = dcomps.size() * dnpts;
     cuda_check(cudaMemcpyAsync(out, grad, n * sizeof(double), cudaMemcpyDeviceToHost, stream), "grad");
@@ -2677,6 +2841,7 @@ public:
   }
 
   void get_field_im(Plan &p, int c, double *out) override {
+    join_dft();
     if (!cplx) {
       std::fill(out, out + p.ndense, 0.0);
       return;
@@ -2692,6 +2857,7 @@ public:
   }
 
   void get_field(Plan &p, int c, double *out) override {
+    join_dft();
     std::vector<R> h(p.nstore), hb;
     cuda_check(cudaMemcpyAsync(h.data(), f[c], p.nstore * sizeof(R), cudaMemcpyDeviceToHost, stream),
                "download");
@@ -2714,6 +2880,7 @@ public:
   }
 
   void get_dft(Plan &p, int id, double *out) override {
+    join_dft();
     dft_flush(p, id);
     const Monitor &m = p.monitors[id];
     size_t n = m.npts * m.freq.size();
@@ -2743,6 +2910,7 @@ public:
   void bump(int id) { ver(id)++; }
 
   void flux(Plan &p, int npairs, const int *idE, const int *idH, double *out) override {
+    join_dft();
     FluxMemo key;
     key.e.assign(idE, idE + npairs);
     key.h.assign(idH, idH + npairs);
@@ -2786,6 +2954,7 @@ public:
   }
 
   void set_dft(Plan &p, int id, const double *in) override {
+    join_dft();
     dft_flush(p, id);
     bump(id);
     const Monitor &m = p.monitors[id];
@@ -2797,6 +2966,7 @@ public:
   }
 
   void scale_dft(Plan &p, int id, std::complex<double> sc) override {
+    join_dft();
     dft_flush(p, id);
     bump(id);
     const Monitor &m = p.monitors[id];
@@ -2807,6 +2977,7 @@ public:
 
   void farfield(Plan &p, const N2FSpec &s, const std::vector<N2FSheet> &sheets, int64_t nx, const double *x,
                 double *out) override {
+    join_dft();
     std::vector<N2FDevSheet> dev;
     for (const N2FSheet &sh : sheets) {
       dft_flush(p, sh.id);

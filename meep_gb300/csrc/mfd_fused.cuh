@@ -367,10 +367,8 @@ __global__ void fused_src_pre_kernel(FusedArgs<R> a, const SrcPoint *pts, int n,
   if (j >= n) return;
   const SrcPoint &sp = pts[j];
   R A[MAXS];
-  for (int t = 0; t < sp.nterm; t++) {
-    double re = sp.amp[t][0] * dv.re[sp.src[t]] - sp.amp[t][1] * dv.im[sp.src[t]];
-    A[t] = R(re);
-  }
+  for (int t = 0; t < sp.nterm; t++)
+    A[t] = R(src_term(sp, t, dv));
   int k[3] = {sp.k[0], sp.k[1], sp.k[2]};
   // the general (non-interior) path gives identical values in the interior
   if (dc == 0) {
