@@ -740,18 +740,36 @@ public:
   static constexpr int NSIDE = 6;
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t side_ev[NSIDE] = {}, fork_ev = nullptr;
+  // fork: the point of the main stream that side streams start from; S(q):
+  // side stream q, made to wait for that point on its first use; join: the
+  // main stream waits for the side streams used since the fork (every
+  // wait costs: the FP32 step measured 2-3 us faster with three side
+  // streams joined instead of six)
+  cudaEvent_t fork_cur = nullptr;
+  unsigned side_used = 0;
   void fork() {
-    cudaEvent_t ev = fork_from ? fork_from : fork_ev;
-    if (!fork_from) cuda_check(cudaEventRecord(fork_ev, stream), "event record");
+    if (fork_from) fork_cur = fork_from;
+    else {
+      cuda_check(cudaEventRecord(fork_ev, stream), "event record");
+      fork_cur = fork_ev;
+    }
     fork_from = nullptr;
-    for (int q = 0; q < NSIDE; q++)
-      cuda_check(cudaStreamWaitEvent(side[q], ev, 0), "stream wait");
+    side_used = 0;
+  }
+  cudaStream_t S(int q) {
+    if (!((side_used >> q) & 1u)) {
+      cuda_check(cudaStreamWaitEvent(side[q], fork_cur, 0), "stream wait");
+      side_used |= 1u << q;
+    }
+    return side[q];
   }
   void join() {
-    for (int q = 0; q < NSIDE; q++) {
-      cuda_check(cudaEventRecord(side_ev[q], side[q]), "event record");
-      cuda_check(cudaStreamWaitEvent(stream, side_ev[q], 0), "stream wait");
-    }
+    for (int q = 0; q < NSIDE; q++)
+      if ((side_used >> q) & 1u) {
+        cuda_check(cudaEventRecord(side_ev[q], side[q]), "event record");
+        cuda_check(cudaStreamWaitEvent(stream, side_ev[q], 0), "stream wait");
+      }
+    side_used = 0;
   }
   // DFT work off the main stream: the samples of E/D monitors (read E or D
   // after a step; the next B half-step runs beside them, the next D/E
@@ -1451,18 +1469,18 @@ public:
   // FP64 (issue-bound): the shell bands as separate launches on the side
   // streams (one launch per half-step ran 2.5% slower there)
   void launch_b_shell_bands(const FusedArgs<R> &a, bool cnd, bool zp) {
-    launch_b_band<true, false, false>(band_xface_zi, a, cnd, zp, side[0]);
-    launch_b_band<false, true, false>(band_yface_zi, a, cnd, zp, side[1]);
-    launch_b_band<true, false>(band_xzedge, a, cnd, zp, side[4]);
-    launch_b_band<false, true>(band_yzedge, a, cnd, zp, side[5]);
-    launch_b_band<true, true>(band_xyedge, a, cnd, zp, side[3]);
+    launch_b_band<true, false, false>(band_xface_zi, a, cnd, zp, S(0));
+    launch_b_band<false, true, false>(band_yface_zi, a, cnd, zp, S(1));
+    launch_b_band<true, false>(band_xzedge, a, cnd, zp, S(4));
+    launch_b_band<false, true>(band_yzedge, a, cnd, zp, S(5));
+    launch_b_band<true, true>(band_xyedge, a, cnd, zp, S(3));
   }
   void launch_de_shell_bands(const FusedArgs<R> &a, bool cnd, bool zp) {
-    launch_de_band<true, false, false>(band_xface_zi, a, cnd, zp, side[0]);
-    launch_de_band<false, true, false>(band_yface_zi, a, cnd, zp, side[1]);
-    launch_de_band<true, false>(band_xzedge, a, cnd, zp, side[4]);
-    launch_de_band<false, true>(band_yzedge, a, cnd, zp, side[5]);
-    launch_de_band<true, true>(band_xyedge, a, cnd, zp, side[3]);
+    launch_de_band<true, false, false>(band_xface_zi, a, cnd, zp, S(0));
+    launch_de_band<false, true, false>(band_yface_zi, a, cnd, zp, S(1));
+    launch_de_band<true, false>(band_xzedge, a, cnd, zp, S(4));
+    launch_de_band<false, true>(band_yzedge, a, cnd, zp, S(5));
+    launch_de_band<true, true>(band_xyedge, a, cnd, zp, S(3));
   }
   void launch_b_qfaces(const FusedArgs<R> &a, bool cnd, cudaStream_t st) {
     if constexpr (std::is_same<R, float>::value) {
@@ -1504,11 +1522,11 @@ public:
     (void)p;
     fork();
     launch(band_rows, 0, stream);
-    launch(band_xface_zi, 4, side[0]);
-    launch(band_yface_zi, 5, side[1]);
-    launch(band_xzedge, 6, side[4]);
-    launch(band_yzedge, 7, side[5]);
-    launch(band_xyedge, 3, side[3]);
+    launch(band_xface_zi, 4, S(0));
+    launch(band_yface_zi, 5, S(1));
+    launch(band_xzedge, 6, S(4));
+    launch(band_yzedge, 7, S(5));
+    launch(band_xyedge, 3, S(3));
     join();
   }
   void offdiag_de3(const Plan &p, const FusedArgs<R> &a, bool cnd, bool zp, const DipoleVals &dip) {
@@ -1783,9 +1801,9 @@ public:
       fork();
       if constexpr (F32) {
         // the side streams' launches first (their blocks go first anyway)
-        launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
-        launch_b_qfaces(a, cndB, side[1]);
-        launch_b_shell(a, cndB, zp, side[0]);
+        launch_b_band<false, false>(band_zend, a, cndB, zp, S(2));
+        launch_b_qfaces(a, cndB, S(1));
+        launch_b_shell(a, cndB, zp, S(0));
         const dim3 g = core_grid();
         if (g.x) {
           if (cndB) b3q_core_kernel<true><<<g, 256, 0, stream>>>(a, qcore);
@@ -1795,7 +1813,7 @@ public:
       }
       else if (band_core.s[2].n > 0) {
         launch_b_band<false, false, false>(band_core, a, cndB, zp, stream);
-        launch_b_band<false, false>(band_zend, a, cndB, zp, side[2]);
+        launch_b_band<false, false>(band_zend, a, cndB, zp, S(2));
       }
       else
         launch_b_band<false, false>(band_rows, a, cndB, zp, stream);
@@ -1878,22 +1896,22 @@ public:
           split = true;
         }
         if (split && zq.n % 4 == 0 && zq.a0 % 4 == 0) {
-          launch_de_qfaces(a, cndD, side[1], &zq);
-          launch_de_shell(a, cndD, zp, false, side[0], &zs);
+          launch_de_qfaces(a, cndD, S(1), &zq);
+          launch_de_shell(a, cndD, zp, false, S(0), &zs);
         }
         else
           split = false;
       }
       if (!split && F32) {
-        const bool qde = launch_de_qfaces(a, cndD, side[1]);
-        launch_de_shell(a, cndD, zp, qde, side[0]);
+        const bool qde = launch_de_qfaces(a, cndD, S(1));
+        launch_de_shell(a, cndD, zp, qde, S(0));
       }
       else if (!split)
         launch_de_shell_bands(a, cndD, zp);
       // FP64 (issue-bound): the flagless core and the z ends; FP32
       // (bandwidth-bound): whole rows, whose z slabs ride along in full warps
       if (!F32 && band_core.s[2].n > 0) {
-        launch_de_band<false, false>(band_zend, a, cndD, zp, side[2]);
+        launch_de_band<false, false>(band_zend, a, cndD, zp, S(2));
         launch_de_band<false, false, false>(band_core, a, cndD, zp, stream);
       }
       else if (a.npoles > 0 && pole_z1 >= 0 && (pole_z0 > 0 || std::min(pole_z1, p.N[2]) < p.N[2])) {
@@ -1906,7 +1924,7 @@ public:
         dim3 g, blk;
         band_shape(bn, g, blk);
         if (g.x) {
-          launch_de_band_p<false, false, 0>(bn, g, blk, a, cndD, zp, side[2]);
+          launch_de_band_p<false, false, 0>(bn, g, blk, a, cndD, zp, S(2));
           nlaunch++;
         }
         if (z1 > pole_z0) {
