@@ -727,6 +727,8 @@ public:
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : {dft_in_ev, dft_out_ev, fl_in_ev, fl_out_ev})
       cudaEventDestroy(e);
+    if (sgexec) cudaGraphExecDestroy(sgexec);
+    if (sgraph) cudaGraphDestroy(sgraph);
     cudaStreamDestroy(dstream);
     cudaStreamDestroy(fstream);
     cudaStreamDestroy(stream);
@@ -782,6 +784,11 @@ public:
   bool dft_pending = false, fl_pending = false;
   void join_samples() {
     fork_from = nullptr;
+    if (capturing) {
+      // in the step graph: wait for whatever the samples recorded last
+      cuda_check(cudaStreamWaitEvent(stream, dft_out_ev, cudaEventWaitExternal), "stream wait");
+      return;
+    }
     if (!dft_pending) return;
     cuda_check(cudaEventRecord(dft_out_ev, dstream), "event record");
     cuda_check(cudaStreamWaitEvent(stream, dft_out_ev, 0), "stream wait");
@@ -1959,7 +1966,100 @@ public:
       }
   }
 
+  // The 3-D step as one CUDA graph, captured at the first step: the side
+  // streams' forks and joins become graph edges, and the wait for the
+  // previous step's E/D samples an external event node.  Each step sets its
+  // source values on the source kernels' nodes.  Steps with current sources
+  // or off-diagonal chi1inv, or integrated sources that need the kernels
+  // around the D/E launches, keep the stream launches, and so do steps with
+  // Lorentz/Drude poles: on GB300 the graph took the 256^3 step without
+  // poles 5 us faster, the 384^2 x 192 step with poles (rows split at the
+  // pole region) 4 us slower, its side-stream kernels finishing after the
+  // main-stream ones instead of under them.
+  cudaGraph_t sgraph = nullptr;
+  cudaGraphExec_t sgexec = nullptr;
+  struct SrcNode {
+    cudaGraphNode_t node;
+    cudaKernelNodeParams kp;
+    R *e;
+    const R *d, *chi;
+    const SrcPoint *pts;
+    int n;
+  };
+  std::vector<SrcNode> src_nodes;
+  long long graph_nlaunch = 0;
+  bool graph_off = false, capturing = false;
+  bool graph_eligible(const Plan &p) const {
+    if (fused_mask != MASK3 || has_b_current || p.any_offdiag || !poles.empty()) return false;
+    for (int d = 0; d < 3; d++)
+      if (ncur[comp(MFD_D, d)] > 0 || (nsrcpts[d] > 0 && !src_e_only)) return false;
+    return true;
+  }
+  bool graph_step(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
+    if (graph_off || !graph_eligible(p)) return false;
+    if (!sgexec) {
+      // capture (the side streams join it through the fork events)
+      fork_from = nullptr;
+      const long long l0 = nlaunch;
+      cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      capturing = true;
+      bool ok = true;
+      try {
+        fused_step_t<3, MASK3>(p, curb, curd, dip);
+      } catch (const Error &) {
+        ok = false;
+      }
+      capturing = false;
+      ok = cudaStreamEndCapture(stream, &sgraph) == cudaSuccess && ok;
+      ok = ok && cudaGraphInstantiate(&sgexec, sgraph, 0) == cudaSuccess;
+      nlaunch = l0;
+      graph_nlaunch = 0;
+      if (!ok) {
+        // not capturable here: the stream launches from now on
+        (void)cudaGetLastError();
+        if (sgexec) cudaGraphExecDestroy(sgexec);
+        if (sgraph) cudaGraphDestroy(sgraph);
+        sgexec = nullptr;
+        sgraph = nullptr;
+        graph_off = true;
+        return false;
+      }
+      size_t nn = 0;
+      cuda_check(cudaGraphGetNodes(sgraph, nullptr, &nn), "graph nodes");
+      std::vector<cudaGraphNode_t> nodes(nn);
+      cuda_check(cudaGraphGetNodes(sgraph, nodes.data(), &nn), "graph nodes");
+      for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType ty;
+        cuda_check(cudaGraphNodeGetType(nd, &ty), "graph node type");
+        if (ty != cudaGraphNodeTypeKernel) continue;
+        SrcNode sn{};
+        cuda_check(cudaGraphKernelNodeGetParams(nd, &sn.kp), "graph node params");
+        graph_nlaunch++;
+        if (sn.kp.func != (void *)src_e_kernel<R>) continue;
+        sn.node = nd;
+        sn.e = *(R **)sn.kp.kernelParams[0];
+        sn.d = *(const R **)sn.kp.kernelParams[1];
+        sn.chi = *(const R **)sn.kp.kernelParams[2];
+        sn.pts = *(const SrcPoint **)sn.kp.kernelParams[3];
+        sn.n = *(int *)sn.kp.kernelParams[4];
+        src_nodes.push_back(sn);
+      }
+    }
+    for (SrcNode &sn : src_nodes) {
+      DipoleVals dv = dip;
+      void *args[] = {&sn.e, &sn.d, &sn.chi, &sn.pts, &sn.n, &dv};
+      cudaKernelNodeParams kp = sn.kp;
+      kp.kernelParams = args;
+      kp.extra = nullptr;
+      cuda_check(cudaGraphExecKernelNodeSetParams(sgexec, sn.node, &kp), "source node values");
+    }
+    cuda_check(cudaGraphLaunch(sgexec, stream), "graph launch");
+    nlaunch += graph_nlaunch;
+    return true;
+  }
+
   void fused_step(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
+    if (graph_step(p, curb, curd, dip)) return;
     switch (fused_mask) {
       case MASK3: fused_step_t<3, MASK3>(p, curb, curd, dip); break;
       case MASK_TM: fused_step_t<2, MASK_TM>(p, curb, curd, dip); break;
@@ -2323,13 +2423,20 @@ public:
     if (queued.empty()) return;
     cuda_check(cudaEventRecord(dft_in_ev, stream), "event record");
     cuda_check(cudaStreamWaitEvent(dstream, dft_in_ev, 0), "stream wait");
-    // the next fork waits on the same event (nothing is queued on the main
-    // stream behind it before then; every other call joins first)
-    fork_from = dft_in_ev;
     dft_pending = true;
     for (const QueuedSample &q : queued)
       dft_launch(p, q.id, q.time, q.tn, dstream);
     queued.clear();
+    if (sgexec) {
+      // the step graph waits on this event for the samples
+      cuda_check(cudaEventRecord(dft_out_ev, dstream), "event record");
+    }
+    else {
+      // the next fork waits on the same event as the samples (nothing is
+      // queued on the main stream behind it before then; every other call
+      // joins first)
+      fork_from = dft_in_ev;
+    }
   }
   void dft_launch(Plan &p, int id, double time, int64_t tn, cudaStream_t st) {
     const Monitor &m = p.monitors[id];
