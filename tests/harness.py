@@ -81,7 +81,8 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
                    nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True,
-                   boxed=False, palette=False, bcond=False, poles_below=None):
+                   boxed=False, palette=False, bcond=False, poles_below=None, hcur=True, hmon=True,
+                   src_box=None):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -99,7 +100,10 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     in structures built from a few media.
     bcond: conductivities on the B components too.
     poles_below: pole strengths zero at z points >= poles_below (a layer of
-    dispersive medium at the low z end, as the dispersive benchmark has)."""
+    dispersive medium at the low z end, as the dispersive benchmark has).
+    hcur=False: no H current source; hmon=False: the second monitor on a D
+    component instead of H (no flux); src_box=(lo, hi): E source points only
+    inside that index box (inclusive)."""
     rng = np.random.default_rng(seed)
     nrand = n
     if dim == 2:
@@ -178,16 +182,27 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     s_int = sim.add_gaussian_src(0.6, 2.0, integrated=True)
     s_cur = sim.add_gaussian_src(0.5, 1.5, integrated=False)
     ndense = int(np.prod(shape))
+    pool = np.arange(ndense)
+    if src_box is not None:
+        kk = np.indices(shape).reshape(len(shape), -1)
+        inside = np.ones(ndense, dtype=bool)
+        for d in range(len(shape)):
+            inside &= (kk[d] >= src_box[0][d]) & (kk[d] <= src_box[1][d])
+        pool = pool[inside]
     for j in range(nsrc):
         c = ecomps[j % len(ecomps)]
-        idx = rng.choice(ndense, size=4, replace=False)
+        idx = rng.choice(pool, size=4, replace=False)
         amp = rng.normal(size=4) + 1j * rng.normal(size=4)
         sim.add_source_points(c, s_int if (j or not ecur) else s_cur, idx, amp)
     # an H current source
     hc = [c for c in comps if c // 3 == _lib.H][0]
-    sim.add_source_points(hc, s_cur, rng.choice(ndense, size=3, replace=False), rng.normal(size=3))
+    hidx = rng.choice(ndense, size=3, replace=False)
+    hamp = rng.normal(size=3)
+    if hcur:
+        sim.add_source_points(hc, s_cur, hidx, hamp)
     mons = []
-    for c in (ecomps[0], [c for c in comps if c // 3 == _lib.H][-1]):
+    second = [c for c in comps if c // 3 == (_lib.H if hmon else _lib.D)][-1]
+    for c in (ecomps[0], second):
         lo = [1 if ext[d] > 1 else 0 for d in range(3)]
         hi = [ext[d] - 3 if ext[d] > 1 else 0 for d in range(3)]
         w = [rng.uniform(0.2, 1.0, size=hi[d] - lo[d] + 1) if ext[d] > 1 else None for d in range(3)]
@@ -199,7 +214,8 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
         out.update({"i%d" % c: sim.get_field_im(c) for c in comps})
     for m in mons:
         out["dft%d" % m] = sim.get_dft(m)
-    out["flux"] = sim.flux([mons[0]], [mons[1]], 5)
+    if hmon:
+        out["flux"] = sim.flux([mons[0]], [mons[1]], 5)
     sim.close()
     return out
 
