@@ -944,6 +944,7 @@ public:
     fp.flag = d_nonfinite;
     finite_probe_kernel<R><<<1, 1, 0, stream>>>(fp);
     nlaunch++;
+    probe_pending = true;
   }
   void check_finite() const {
     if (h_nonfinite && *(volatile int *)h_nonfinite) throw Error("simulation fields are NaN or Inf");
@@ -954,7 +955,7 @@ public:
   double *d_flux = nullptr;
   double *d_flux_part = nullptr;
   size_t flux_cap = 0;
-  double ms = 0;
+  mutable double ms = 0;
   bool timing = false;
 
   template <typename T> T *dalloc(size_t n) {
@@ -2568,21 +2569,38 @@ public:
     launch_samples(p);
   }
 
+  // a batch of steps without a divergence probe returns once it is queued
+  // (its device time is taken when asked for, the tensor-core error flag
+  // where results are read); a batch with a probe waits for it, so that a
+  // divergence raises in the call whose steps the probe saw
+  bool probe_pending = false;
   void begin_steps() override {
+    ms_pending = false; // the previous batch's time is not asked for any more
     cuda_check(cudaEventRecord(ev0, stream), "event record");
   }
   void end_steps() override {
     join_dft();
     cuda_check(cudaEventRecord(ev1, stream), "event record");
-    cuda_check(cudaEventSynchronize(ev1), "event sync");
-    float fms = 0;
-    cuda_check(cudaEventElapsedTime(&fms, ev0, ev1), "elapsed");
-    ms = fms;
     cuda_check(cudaGetLastError(), "kernel launch");
-    check_tc();
+    ms_pending = true;
+    if (probe_pending) {
+      cuda_check(cudaEventSynchronize(ev1), "event sync");
+      probe_pending = false;
+      last_step_ms();
+      check_tc();
+    }
     check_finite();
   }
-  double last_step_ms() const override { return ms; }
+  mutable bool ms_pending = false;
+  double last_step_ms() const override {
+    if (ms_pending) {
+      float fms = 0;
+      if (cudaEventSynchronize(ev1) != cudaSuccess || cudaEventElapsedTime(&fms, ev0, ev1) != cudaSuccess) return -1.0;
+      ms = fms;
+      ms_pending = false;
+    }
+    return ms;
+  }
   long long launches() const override { return nlaunch; }
   void synchronize() override {
     join_dft();
