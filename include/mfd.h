@@ -117,7 +117,9 @@ int mfd_add_dft(mfd_sim *sim, int c, const int lo[3], const int hi[3], const dou
                 double dV, int include_weights, double scale_re, double scale_im, int centered,
                 size_t nfreq, const double *freq, int decimation, int *id);
 
-/* Advance n full time steps (fields::step, src/step.cpp:35-139). */
+/* Advance n full time steps (fields::step, src/step.cpp:35-139).  Returns
+ * once the steps are queued on the GPU (a call whose steps ran a divergence
+ * probe waits for it); the calls that read results wait for them. */
 int mfd_step(mfd_sim *sim, int n);
 
 /* Current step count t (fields::t) and dt. */
@@ -281,7 +283,8 @@ const char *mfd_noalloc_last_error(void);
 /* Number of kernel launches issued by this handle so far (for accounting). */
 int64_t mfd_kernel_launches(const mfd_sim *sim);
 
-/* Device-side timing of the last mfd_step call, milliseconds (CUDA events). */
+/* Device-side timing of the last mfd_step call, milliseconds (CUDA events;
+ * waits for that call's steps), -1 when the wait fails. */
 double mfd_last_step_ms(const mfd_sim *sim);
 
 #ifdef __cplusplus
