@@ -679,13 +679,36 @@ __global__ void __launch_bounds__(256, (FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8
   if (band_coords(bd, k)) b3_point<R, CND, FX, FY, FZ>(a, k);
 }
 
+// true when every z point of this block's part of the band lies between the
+// z slabs: both half-pixel positions of each point in the middle region, so
+// the code without z PML gives the same arithmetic there (band_flags)
+template <typename R> __device__ __forceinline__ bool z_interior_block(const FusedArgs<R> &a, const Band &bd) {
+  const Span &s = bd.s[2];
+  if (s.split < s.n) return false; // two runs: the general code
+  const int t0 = (int)(blockIdx.x * blockDim.x);
+  const int t1 = min(t0 + (int)blockDim.x, s.n) - 1;
+  const bool lo = a.T[2][0] <= 0 || t0 + s.a0 >= a.T[2][0] + 1;
+  const bool hi = a.T[2][1] <= 0 || t1 + s.a0 <= a.N[2] - a.T[2][1] - 1;
+  return lo && hi;
+}
+
 // with poles in registers every operand of a point is loaded before any
-// store: 64 registers (half occupancy, each thread keeps ~30 loads in flight)
+// store: 64 registers (half occupancy, each thread keeps ~30 loads in flight).
+// Without poles, rows that hold z slabs (FZ) run the code without z PML in
+// their blocks between the slabs (block-uniform branch; 7 us per step on the
+// 256^3 rows, measured slower with the pole kernels).
 template <typename R, bool CND, int NP, bool FX, bool FY, bool FZ>
 __global__ void __launch_bounds__(256, NP > 0 ? 4 : ((FX || FY) ? (sizeof(R) == 8 ? 4 : 6) : 8))
     de3_band_kernel(const FusedArgs<R> a, const Band bd) {
   int k[3];
-  if (band_coords(bd, k)) de3_point<R, CND, NP, FX, FY, FZ>(a, k);
+  if (!band_coords(bd, k)) return;
+  if constexpr (FZ && NP == 0) {
+    if (z_interior_block(a, bd)) {
+      de3_point<R, CND, NP, FX, FY, false>(a, k);
+      return;
+    }
+  }
+  de3_point<R, CND, NP, FX, FY, FZ>(a, k);
 }
 
 // The shell of a 3-D half-step in one launch: the z-interior x and y faces,
