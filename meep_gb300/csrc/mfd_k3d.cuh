@@ -748,6 +748,16 @@ __device__ __forceinline__ bool shell_coords(const ShellSet &s, int &q, int k[3]
   return true;
 }
 
+// the x-y edge band of a shell (band 4): this block's z points all lie
+// between the z slabs (z_interior_block for the shell's block numbering)
+template <typename R> __device__ __forceinline__ bool shell_z_interior(const FusedArgs<R> &a, const ShellSet &s) {
+  const Span &z = s.b[4].s[2];
+  if (z.split < z.n) return false;
+  const int lb = (int)blockIdx.x - s.first[4];
+  const int t0 = lb % s.gz[4] * 32, t1 = min(t0 + 32, z.n) - 1;
+  return (a.T[2][0] <= 0 || t0 + z.a0 >= a.T[2][0] + 1) && (a.T[2][1] <= 0 || t1 + z.a0 <= a.N[2] - a.T[2][1] - 1);
+}
+
 template <typename R, bool CND, bool ZP>
 __global__ void __launch_bounds__(256, sizeof(R) == 8 ? 4 : 6) b3_shell_kernel(const FusedArgs<R> a, const ShellSet s) {
   int q, k[3];
@@ -757,7 +767,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 8 ? 4 : 6) b3_shell_kernel(c
     case 1: b3_point<R, CND, false, true, false>(a, k); break;
     case 2: b3_point<R, CND, true, false, ZP>(a, k); break;
     case 3: b3_point<R, CND, false, true, ZP>(a, k); break;
-    default: b3_point<R, CND, true, true, ZP>(a, k); break;
+    default:
+      if (ZP && shell_z_interior(a, s)) b3_point<R, CND, true, true, false>(a, k);
+      else b3_point<R, CND, true, true, ZP>(a, k);
+      break;
   }
 }
 
@@ -771,7 +784,10 @@ __global__ void __launch_bounds__(256, NP > 0 ? 4 : (sizeof(R) == 8 ? 4 : 6))
     case 1: de3_point<R, CND, NP, false, true, false>(a, k); break;
     case 2: de3_point<R, CND, NP, true, false, ZP>(a, k); break;
     case 3: de3_point<R, CND, NP, false, true, ZP>(a, k); break;
-    default: de3_point<R, CND, NP, true, true, ZP>(a, k); break;
+    default:
+      if (NP == 0 && ZP && shell_z_interior(a, s)) de3_point<R, CND, NP, true, true, false>(a, k);
+      else de3_point<R, CND, NP, true, true, ZP>(a, k);
+      break;
   }
 }
 
