@@ -1,6 +1,9 @@
 """GPU: the 3-D step without poles or current sources, its integrated
 sources away from the E slabs, runs as one CUDA graph (its source values set
-on the graph's nodes each step): against the oracle, FP64 bit for bit."""
+on the graph's nodes each step): against the oracle, FP64 bit for bit.  With
+up to four source points, all in the rows, the row kernel itself sets E at
+them (nsrc=1: one source of four points); with more, the source kernel
+after the D/E launches does (nsrc=3)."""
 import pytest
 
 from harness import random_problem, relerr
@@ -18,15 +21,17 @@ def _run(lib, seed, prec, **kw):
 GRAPH = dict(n=(20, 18, 40), poles=False, ecur=False, hcur=False, src_box=((7, 7, 12), (12, 10, 28)), steps=60)
 
 
-def test_graph_step_fp64_bitwise(engine_lib, oracle_lib):
-    g = _run(engine_lib, 81, 64, **GRAPH)
-    o = _run(oracle_lib, 81, 64, **GRAPH)
+@pytest.mark.parametrize("nsrc", [3, 1])
+def test_graph_step_fp64_bitwise(nsrc, engine_lib, oracle_lib):
+    g = _run(engine_lib, 81, 64, nsrc=nsrc, **GRAPH)
+    o = _run(oracle_lib, 81, 64, nsrc=nsrc, **GRAPH)
     for k in o:
         assert relerr(g[k], o[k]) <= 1e-12, (k, relerr(g[k], o[k]))
 
 
-def test_graph_step_fp32(engine_lib, oracle_lib):
-    g = _run(engine_lib, 82, 32, **GRAPH)
-    o = _run(oracle_lib, 82, 32, **GRAPH)
+@pytest.mark.parametrize("nsrc", [3, 1])
+def test_graph_step_fp32(nsrc, engine_lib, oracle_lib):
+    g = _run(engine_lib, 82, 32, nsrc=nsrc, **GRAPH)
+    o = _run(oracle_lib, 82, 32, nsrc=nsrc, **GRAPH)
     for k in o:
         assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
