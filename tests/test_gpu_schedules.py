@@ -1,9 +1,7 @@
 """GPU: the 3-D step without poles or current sources, its integrated
 sources away from the E slabs, runs as one CUDA graph (its source values set
-on the graph's nodes each step): against the oracle, FP64 bit for bit.  With
-up to four source points, all in the rows, the row kernel itself sets E at
-them (nsrc=1: one source of four points); with more, the source kernel
-after the D/E launches does (nsrc=3)."""
+on the graph's nodes each step): against the oracle, FP64 bit for bit, with
+one source of four points (nsrc=1) and with three (nsrc=3)."""
 import pytest
 
 from harness import random_problem, relerr
