@@ -719,9 +719,10 @@ def main():
         "flux_steps": FULL_STEPS,
         "e2e": {"value": e2e, "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 8 * NFREQ,
-                "note": "fields::step() + dft_flux::flux() every step through the meep:: C++ API (wall time); "
-                        "flux() recomputes and copies the spectrum on the steps that added a DFT sample and "
-                        "returns the unchanged spectrum otherwise"},
+                "note": "fields::step() + dft_flux::flux() every step through the meep:: C++ API (wall time "
+                        "up to the completion of the last step); a step returns once queued, flux() recomputes "
+                        "and copies the spectrum (waiting for the steps) on the steps that added a DFT sample "
+                        "and returns the unchanged spectrum otherwise"},
         "e2e_python": pye2e,
         "gpu_launches": int(r32["launches"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
