@@ -1200,12 +1200,30 @@ public:
   // a nonzero conductivity somewhere in the segment
   unsigned *d_amask = nullptr;
   int amask_nseg = 0;
+  std::vector<unsigned> h_amask;
+  // the activity word shared by every segment of band b (single runs along x
+  // and y, z segments whole), with bit 31 set; 0 when they differ
+  unsigned uniform_am(const Band &b) const {
+    if (h_amask.empty() || b.s[0].split < b.s[0].n || b.s[1].split < b.s[1].n || b.s[2].split < b.s[2].n ||
+        b.s[2].a0 % 32 || b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0)
+      return 0u;
+    const int nseg = amask_nseg, ext1 = (int)(h_amask.size() / nseg) / std::max(1, geo_ext0);
+    const int g0 = b.s[2].a0 / 32, g1 = (b.s[2].a0 + b.s[2].n - 1) / 32;
+    const unsigned w = h_amask[((size_t)b.s[0].a0 * ext1 + b.s[1].a0) * nseg + g0];
+    for (int k0 = b.s[0].a0; k0 < b.s[0].a0 + b.s[0].n; k0++)
+      for (int k1 = b.s[1].a0; k1 < b.s[1].a0 + b.s[1].n; k1++)
+        for (int g = g0; g <= g1; g++)
+          if (h_amask[((size_t)k0 * ext1 + k1) * nseg + g] != w) return 0u;
+    return w | (1u << 31);
+  }
+  int geo_ext0 = 1;
   void build_active_mask(const Plan &p) {
     if (p.g.dim != 3) return;
     bool any = !poles.empty();
     for (int d = 0; d < 3; d++)
       any = any || cnd[comp(MFD_D, d)] || cnd[comp(MFD_B, d)];
     if (!any) return;
+    geo_ext0 = p.ext[0];
     const int nseg = (p.ext[2] + 31) / 32;
     std::vector<unsigned> m((size_t)p.ext[0] * p.ext[1] * nseg, 0u);
     auto mark = [&](const std::vector<double> &dense, unsigned bit) {
@@ -1227,6 +1245,7 @@ public:
     }
     d_amask = dupload(m);
     amask_nseg = nseg;
+    h_amask = m;
     // z extent of the segments where some pole is active anywhere: rows
     // outside it take the pole-free D/E kernel
     const unsigned pole_bits = (1u << (3 * MAX_POLES)) - 1u;
@@ -1241,6 +1260,8 @@ public:
     pole_z1 = s1 >= s0 ? std::min(32 * (s1 + 1), p.ext[2]) : 0;
   }
   int pole_z0 = 0, pole_z1 = -1; // z points [pole_z0, pole_z1) hold every active pole (-1: unknown)
+  unsigned bp_am = 0;
+  bool bp_am_done = false;
 
   static constexpr int MASK3 = 0xFFF;
   static constexpr int MASK_TM = (1 << 2) | (1 << 3) | (1 << 4) | (1 << 8) | (1 << 9) | (1 << 10);
@@ -1938,7 +1959,15 @@ public:
         if (z1 > pole_z0) {
           Band bp = band_rows;
           bp.s[2] = span_run(pole_z0, z1 - 1);
-          launch_de_band<false, false>(bp, a, cndD, zp, stream);
+          // the pole rows: their segments' activity word as a parameter
+          // when it is the same everywhere there
+          if (!bp_am_done) {
+            bp_am = uniform_am(bp);
+            bp_am_done = true;
+          }
+          FusedArgs<R> ab = a;
+          ab.am_all = bp_am;
+          launch_de_band<false, false>(bp, ab, cndD, zp, stream);
         }
       }
       else

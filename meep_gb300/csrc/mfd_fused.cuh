@@ -53,6 +53,9 @@ template <typename R> struct FusedArgs {
   // everything active.
   const unsigned *amask;
   int mext1, mnseg;
+  // nonzero: every segment of this launch has the activity bits am_all
+  // (bit 31 set as the mark), so no word is loaded
+  unsigned am_all;
   __device__ __forceinline__ R tbs(int d, int p) const { return sig[d][p]; }
   __device__ __forceinline__ R tbk(int d, int p) const { return kap[d][p]; }
   __device__ __forceinline__ R tbsi(int d, int p) const { return siginv[d][p]; }

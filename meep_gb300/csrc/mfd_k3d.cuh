@@ -144,6 +144,7 @@ __device__ __forceinline__ bool chunk_has(unsigned mask, int rx, int ry, int rz)
 // activity bits of the row segment holding point k (FusedArgs::amask)
 constexpr int AM_DCOND = 12, AM_BCOND = 15;
 template <typename R> __device__ __forceinline__ unsigned seg_active(const FusedArgs<R> &a, const int k[3]) {
+  if (a.am_all) return a.am_all;
   return a.amask ? __ldg(a.amask + ((size_t)k[0] * a.mext1 + k[1]) * a.mnseg + (k[2] >> 5)) : ~0u;
 }
 template <typename R>

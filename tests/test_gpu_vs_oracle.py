@@ -173,3 +173,17 @@ def test_bcond_and_layered_poles_fp32(seed, n, kw, engine_lib, oracle_lib):
     o = _run(oracle_lib, seed, 3, 32, **kw)
     for k in o:
         assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
+
+
+# the pole rows of the FP32 step take their activity word as a parameter when
+# every segment there has the same one (poles on everywhere below z = 64, no
+# conductivity): against the FP32 oracle, where a wrong bit shows as an O(1)
+# error
+@pytest.mark.parametrize("seed,n", [(75, (17, 15, 130)), (76, (18, 16, 100))])
+def test_uniform_pole_layer_fp32(seed, n, engine_lib, oracle_lib):
+    kw = dict(n=n, poles_below=64, cond=False, ecur=False, steps=60)
+    g = _run(engine_lib, seed, 3, 32, **kw)
+    o = _run(oracle_lib, seed, 3, 32, **kw)
+    for k in o:
+        assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
+
