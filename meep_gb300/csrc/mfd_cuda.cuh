@@ -1201,20 +1201,31 @@ public:
   unsigned *d_amask = nullptr;
   int amask_nseg = 0;
   std::vector<unsigned> h_amask;
-  // the activity word shared by every segment of band b (single runs along x
-  // and y, z segments whole), with bit 31 set; 0 when they differ
-  unsigned uniform_am(const Band &b) const {
-    if (h_amask.empty() || b.s[0].split < b.s[0].n || b.s[1].split < b.s[1].n || b.s[2].split < b.s[2].n ||
-        b.s[2].a0 % 32 || b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0)
-      return 0u;
+  // the activity word shared by every segment that holds points of the
+  // bands (single runs along x and y), with bit 31 set; 0 when they differ
+  unsigned uniform_am(std::initializer_list<Band> bands) const {
+    if (h_amask.empty()) return 0u;
     const int nseg = amask_nseg, ext1 = (int)(h_amask.size() / nseg) / std::max(1, geo_ext0);
-    const int g0 = b.s[2].a0 / 32, g1 = (b.s[2].a0 + b.s[2].n - 1) / 32;
-    const unsigned w = h_amask[((size_t)b.s[0].a0 * ext1 + b.s[1].a0) * nseg + g0];
-    for (int k0 = b.s[0].a0; k0 < b.s[0].a0 + b.s[0].n; k0++)
-      for (int k1 = b.s[1].a0; k1 < b.s[1].a0 + b.s[1].n; k1++)
-        for (int g = g0; g <= g1; g++)
-          if (h_amask[((size_t)k0 * ext1 + k1) * nseg + g] != w) return 0u;
-    return w | (1u << 31);
+    bool first = true;
+    unsigned w = 0;
+    for (const Band &b : bands) {
+      if (b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0) continue;
+      if (b.s[0].split < b.s[0].n || b.s[1].split < b.s[1].n) return 0u;
+      const Span &z = b.s[2];
+      const int runs[2][2] = {{z.a0, z.a0 + z.split}, {z.a1 + z.split, z.a1 + z.n}}; // [lo, hi)
+      for (const auto &r : runs) {
+        if (r[1] <= r[0]) continue;
+        const int g0 = r[0] / 32, g1 = (r[1] - 1) / 32;
+        for (int k0 = b.s[0].a0; k0 < b.s[0].a0 + b.s[0].n; k0++)
+          for (int k1 = b.s[1].a0; k1 < b.s[1].a0 + b.s[1].n; k1++)
+            for (int g = g0; g <= g1; g++) {
+              const unsigned v = h_amask[((size_t)k0 * ext1 + k1) * nseg + g];
+              if (first) w = v, first = false;
+              else if (v != w) return 0u;
+            }
+      }
+    }
+    return first ? 0u : (w | (1u << 31));
   }
   int geo_ext0 = 1;
   void build_active_mask(const Plan &p) {
@@ -1260,8 +1271,10 @@ public:
     pole_z1 = s1 >= s0 ? std::min(32 * (s1 + 1), p.ext[2]) : 0;
   }
   int pole_z0 = 0, pole_z1 = -1; // z points [pole_z0, pole_z1) hold every active pole (-1: unknown)
-  unsigned bp_am = 0;
-  bool bp_am_done = false;
+  // uniform activity words of the pole rows, the pole-free rows and the
+  // pole-free z interior of the faces (0: loaded per segment)
+  unsigned bp_am = 0, bn_am = 0, qf_am = 0;
+  bool bp_am_done = false, bn_am_done = false, qf_am_done = false;
 
   static constexpr int MASK3 = 0xFFF;
   static constexpr int MASK_TM = (1 << 2) | (1 << 3) | (1 << 4) | (1 << 8) | (1 << 9) | (1 << 10);
@@ -1925,7 +1938,15 @@ public:
           split = true;
         }
         if (split && zq.n % 4 == 0 && zq.a0 % 4 == 0) {
-          launch_de_qfaces(a, cndD, S(1), &zq);
+          if (!qf_am_done) {
+            Band f0 = band_xface_zi, f1 = band_yface_zi;
+            f0.s[2] = f1.s[2] = zq;
+            qf_am = uniform_am({f0, f1});
+            qf_am_done = true;
+          }
+          FusedArgs<R> aq = a;
+          aq.am_all = qf_am;
+          launch_de_qfaces(aq, cndD, S(1), &zq);
           launch_de_shell(a, cndD, zp, false, S(0), &zs);
         }
         else
@@ -1953,7 +1974,13 @@ public:
         dim3 g, blk;
         band_shape(bn, g, blk);
         if (g.x) {
-          launch_de_band_p<false, false, 0>(bn, g, blk, a, cndD, zp, S(2));
+          if (!bn_am_done) {
+            bn_am = uniform_am({bn});
+            bn_am_done = true;
+          }
+          FusedArgs<R> an = a;
+          an.am_all = bn_am;
+          launch_de_band_p<false, false, 0>(bn, g, blk, an, cndD, zp, S(2));
           nlaunch++;
         }
         if (z1 > pole_z0) {
@@ -1962,7 +1989,7 @@ public:
           // the pole rows: their segments' activity word as a parameter
           // when it is the same everywhere there
           if (!bp_am_done) {
-            bp_am = uniform_am(bp);
+            bp_am = uniform_am({bp});
             bp_am_done = true;
           }
           FusedArgs<R> ab = a;
