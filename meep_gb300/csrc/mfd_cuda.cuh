@@ -1202,28 +1202,35 @@ public:
   int amask_nseg = 0;
   std::vector<unsigned> h_amask;
   // the activity word shared by every segment that holds points of the
-  // bands (single runs along x and y), with bit 31 set; 0 when they differ
+  // bands, with bit 31 set; 0 when they differ
   unsigned uniform_am(std::initializer_list<Band> bands) const {
     if (h_amask.empty()) return 0u;
     const int nseg = amask_nseg, ext1 = (int)(h_amask.size() / nseg) / std::max(1, geo_ext0);
+    // the two runs [lo, hi) of a span
+    auto runs = [](const Span &z, int r[2][2]) {
+      r[0][0] = z.a0, r[0][1] = z.a0 + z.split;
+      r[1][0] = z.a1 + z.split, r[1][1] = z.a1 + z.n;
+    };
     bool first = true;
     unsigned w = 0;
     for (const Band &b : bands) {
       if (b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0) continue;
-      if (b.s[0].split < b.s[0].n || b.s[1].split < b.s[1].n) return 0u;
-      const Span &z = b.s[2];
-      const int runs[2][2] = {{z.a0, z.a0 + z.split}, {z.a1 + z.split, z.a1 + z.n}}; // [lo, hi)
-      for (const auto &r : runs) {
-        if (r[1] <= r[0]) continue;
-        const int g0 = r[0] / 32, g1 = (r[1] - 1) / 32;
-        for (int k0 = b.s[0].a0; k0 < b.s[0].a0 + b.s[0].n; k0++)
-          for (int k1 = b.s[1].a0; k1 < b.s[1].a0 + b.s[1].n; k1++)
-            for (int g = g0; g <= g1; g++) {
-              const unsigned v = h_amask[((size_t)k0 * ext1 + k1) * nseg + g];
-              if (first) w = v, first = false;
-              else if (v != w) return 0u;
-            }
-      }
+      int rx[2][2], ry[2][2], rz[2][2];
+      runs(b.s[0], rx);
+      runs(b.s[1], ry);
+      runs(b.s[2], rz);
+      for (const auto &x : rx)
+        for (int k0 = x[0]; k0 < x[1]; k0++)
+          for (const auto &y : ry)
+            for (int k1 = y[0]; k1 < y[1]; k1++)
+              for (const auto &z : rz) {
+                if (z[1] <= z[0]) continue;
+                for (int g = z[0] / 32; g <= (z[1] - 1) / 32; g++) {
+                  const unsigned v = h_amask[((size_t)k0 * ext1 + k1) * nseg + g];
+                  if (first) w = v, first = false;
+                  else if (v != w) return 0u;
+                }
+              }
     }
     return first ? 0u : (w | (1u << 31));
   }
@@ -1383,6 +1390,23 @@ public:
     s.a1 = hi + 1 - lo;
     return s;
   }
+  // the points of s in [z0, z1)
+  static Span span_clip(const Span &s, int z0, int z1) {
+    const int lo0 = std::max(s.a0, z0), hi0 = std::min(s.a0 + s.split, z1);
+    const int lo1 = std::max(s.a1 + s.split, z0), hi1 = std::min(s.a1 + s.n, z1);
+    const int n0 = std::max(0, hi0 - lo0), n1 = std::max(0, hi1 - lo1);
+    if (n0 > 0 && n1 > 0) {
+      Span r{};
+      r.n = n0 + n1;
+      r.split = n0;
+      r.a0 = lo0;
+      r.a1 = lo1 - n0;
+      return r;
+    }
+    if (n0 > 0) return span_run(lo0, hi0 - 1);
+    if (n1 > 0) return span_run(lo1, hi1 - 1);
+    return span_run(0, -1);
+  }
   // short z spans (the z ends of the rows) take whole blocks of several rows
   // so no lane idles; long spans take warps of 32 consecutive z points
   static void band_shape(const Band &b, dim3 &g, dim3 &blk) {
@@ -1438,13 +1462,15 @@ public:
   // the shell bands of a half-step as one launch (ShellSet)
   // skip_zi: the z-interior faces run elsewhere (FP32: quads); zi: their z
   // span when only part of it stays in the shell (null: all of it)
-  ShellSet shell_set(bool skip_zi, const Span *zi = nullptr) const {
+  // z0, z1: only the points with z in [z0, z1)
+  ShellSet shell_set(bool skip_zi, const Span *zi = nullptr, int z0 = 0, int z1 = 1 << 30) const {
     ShellSet s{};
     const Band *bands[5] = {&band_xface_zi, &band_yface_zi, &band_xzedge, &band_yzedge, &band_xyedge};
     int total = 0;
     for (int q = 0; q < 5; q++) {
       Band b = *bands[q];
       if (zi && q < 2) b.s[2] = *zi;
+      if (z0 > 0 || z1 < (1 << 30)) b.s[2] = span_clip(b.s[2], z0, z1);
       s.b[q] = b;
       const bool empty = b.s[0].n <= 0 || b.s[1].n <= 0 || b.s[2].n <= 0 || (skip_zi && q < 2);
       s.gz[q] = empty ? 1 : (b.s[2].n + 31) / 32;
@@ -1472,6 +1498,40 @@ public:
     else if (cnd) de3_shell_kernel<R, true, NP, false><<<g, blk, 0, st>>>(a, s);
     else if (zp) de3_shell_kernel<R, false, NP, true><<<g, blk, 0, st>>>(a, s);
     else de3_shell_kernel<R, false, NP, false><<<g, blk, 0, st>>>(a, s);
+  }
+  // the D/E shell with the poles in z [pole_z0, pole_z1) cut at pole_z1
+  // (pole_z0 = 0): the part below with the pole kernel, the part above with
+  // the pole-free one, each with its segments' activity word when uniform
+  ShellSet sh_lo{}, sh_hi{};
+  unsigned sh_lo_am = 0, sh_hi_am = 0;
+  bool sh_done = false;
+  void launch_de_shell_split(const FusedArgs<R> &a, bool cnd, bool zp, const Span *zi) {
+    if (pole_z0 != 0 || a.npoles > 2) {
+      launch_de_shell(a, cnd, zp, false, S(0), zi);
+      return;
+    }
+    if (!sh_done) {
+      sh_lo = shell_set(false, zi, 0, pole_z1);
+      sh_hi = shell_set(false, zi, pole_z1, 1 << 30);
+      auto am_of = [&](const ShellSet &ss) {
+        return uniform_am({ss.b[0], ss.b[1], ss.b[2], ss.b[3], ss.b[4]});
+      };
+      sh_lo_am = am_of(sh_lo);
+      sh_hi_am = am_of(sh_hi);
+      sh_done = true;
+    }
+    FusedArgs<R> al = a, ah = a;
+    al.am_all = sh_lo_am;
+    ah.am_all = sh_hi_am;
+    if (sh_lo.first[5] > 0) {
+      if (a.npoles == 1) launch_de_shell_p<1>(sh_lo, al, cnd, zp, S(0));
+      else launch_de_shell_p<2>(sh_lo, al, cnd, zp, S(0));
+      nlaunch++;
+    }
+    if (sh_hi.first[5] > 0) {
+      launch_de_shell_p<0>(sh_hi, ah, cnd, zp, S(3));
+      nlaunch++;
+    }
   }
   void launch_de_shell(const FusedArgs<R> &a, bool cnd, bool zp, bool skip_zi, cudaStream_t st,
                        const Span *zi = nullptr) {
@@ -1947,7 +2007,7 @@ public:
           FusedArgs<R> aq = a;
           aq.am_all = qf_am;
           launch_de_qfaces(aq, cndD, S(1), &zq);
-          launch_de_shell(a, cndD, zp, false, S(0), &zs);
+          launch_de_shell_split(a, cndD, zp, &zs);
         }
         else
           split = false;
