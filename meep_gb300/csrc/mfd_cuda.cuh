@@ -784,11 +784,6 @@ public:
   bool dft_pending = false, fl_pending = false;
   void join_samples() {
     fork_from = nullptr;
-    if (capturing) {
-      // in the step graph: wait for whatever the samples recorded last
-      cuda_check(cudaStreamWaitEvent(stream, dft_out_ev, cudaEventWaitExternal), "stream wait");
-      return;
-    }
     if (!dft_pending) return;
     cuda_check(cudaEventRecord(dft_out_ev, dstream), "event record");
     cuda_check(cudaStreamWaitEvent(stream, dft_out_ev, 0), "stream wait");
@@ -2084,8 +2079,8 @@ public:
   }
 
   // The 3-D step as one CUDA graph, captured at the first step: the side
-  // streams' forks and joins become graph edges, and the wait for the
-  // previous step's E/D samples an external event node.  Each step sets its
+  // streams' forks and joins become graph edges; the main stream waits for
+  // the previous step's E/D samples before the launch.  Each step sets its
   // source values on the source kernels' nodes.  Steps with current sources
   // or off-diagonal chi1inv, or integrated sources that need the kernels
   // around the D/E launches, keep the stream launches, and so do steps with
@@ -2114,6 +2109,9 @@ public:
   }
   bool graph_step(Plan &p, const DipoleVals &curb, const DipoleVals &curd, const DipoleVals &dip) {
     if (graph_off || !graph_eligible(p)) return false;
+    // the previous step's E/D samples finish before the graph starts (the
+    // graph holds no wait on them)
+    join_samples();
     if (!sgexec) {
       // capture (the side streams join it through the fork events)
       fork_from = nullptr;
@@ -2544,11 +2542,7 @@ public:
     for (const QueuedSample &q : queued)
       dft_launch(p, q.id, q.time, q.tn, dstream);
     queued.clear();
-    if (sgexec) {
-      // the step graph waits on this event for the samples
-      cuda_check(cudaEventRecord(dft_out_ev, dstream), "event record");
-    }
-    else {
+    if (!sgexec) {
       // the next fork waits on the same event as the samples (nothing is
       // queued on the main stream behind it before then; every other call
       // joins first)

@@ -82,7 +82,7 @@ def compare_records(out, ref, case, skip=("t", "realnum_bytes")):
 def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, pml=True,
                    nsrc=3, steps=60, n=None, bloch=None, bloch_pml=False, offdiag=False, ecur=True,
                    boxed=False, palette=False, bcond=False, poles_below=None, hcur=True, hmon=True,
-                   src_box=None):
+                   src_box=None, decimation=2):
     """Build the same seeded random problem on one engine and return outputs.
 
     Random inverse permittivities, conductivities and Lorentz/Drude sigma
@@ -103,7 +103,7 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
     dispersive medium at the low z end, as the dispersive benchmark has).
     hcur=False: no H current source; hmon=False: the second monitor on a D
     component instead of H (no flux); src_box=(lo, hi): E source points only
-    inside that index box (inclusive)."""
+    inside that index box (inclusive); decimation: of both monitors."""
     rng = np.random.default_rng(seed)
     nrand = n
     if dim == 2:
@@ -207,7 +207,7 @@ def random_problem(sim_factory, seed, dim, precision=64, poles=True, cond=True, 
         hi = [ext[d] - 3 if ext[d] > 1 else 0 for d in range(3)]
         w = [rng.uniform(0.2, 1.0, size=hi[d] - lo[d] + 1) if ext[d] > 1 else None for d in range(3)]
         mons.append(sim.add_dft(c, lo, hi, w, dV=0.01, include_weights=True, scale=0.3 - 0.2j,
-                                centered=True, freqs=np.linspace(0.3, 0.9, 5), decimation=2))
+                                centered=True, freqs=np.linspace(0.3, 0.9, 5), decimation=decimation))
     sim.step(steps)
     out = {"c%d" % c: sim.get_field(c) for c in comps}
     if bloch is not None:

@@ -19,17 +19,19 @@ def _run(lib, seed, prec, **kw):
 GRAPH = dict(n=(20, 18, 40), poles=False, ecur=False, hcur=False, src_box=((7, 7, 12), (12, 10, 28)), steps=60)
 
 
-@pytest.mark.parametrize("nsrc", [3, 1])
-def test_graph_step_fp64_bitwise(nsrc, engine_lib, oracle_lib):
-    g = _run(engine_lib, 81, 64, nsrc=nsrc, **GRAPH)
-    o = _run(oracle_lib, 81, 64, nsrc=nsrc, **GRAPH)
+# decimation 1: an E sample after every step, each waited for before the
+# next step's graph starts
+@pytest.mark.parametrize("nsrc,dec", [(3, 2), (1, 2), (3, 1)])
+def test_graph_step_fp64_bitwise(nsrc, dec, engine_lib, oracle_lib):
+    g = _run(engine_lib, 81, 64, nsrc=nsrc, decimation=dec, **GRAPH)
+    o = _run(oracle_lib, 81, 64, nsrc=nsrc, decimation=dec, **GRAPH)
     for k in o:
         assert relerr(g[k], o[k]) <= 1e-12, (k, relerr(g[k], o[k]))
 
 
-@pytest.mark.parametrize("nsrc", [3, 1])
-def test_graph_step_fp32(nsrc, engine_lib, oracle_lib):
-    g = _run(engine_lib, 82, 32, nsrc=nsrc, **GRAPH)
-    o = _run(oracle_lib, 82, 32, nsrc=nsrc, **GRAPH)
+@pytest.mark.parametrize("nsrc,dec", [(3, 2), (1, 2), (3, 1)])
+def test_graph_step_fp32(nsrc, dec, engine_lib, oracle_lib):
+    g = _run(engine_lib, 82, 32, nsrc=nsrc, decimation=dec, **GRAPH)
+    o = _run(oracle_lib, 82, 32, nsrc=nsrc, decimation=dec, **GRAPH)
     for k in o:
         assert relerr(g[k], o[k]) <= 2e-5, (k, relerr(g[k], o[k]))
